@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 WCSPH right-hand side: particle-steps/s of the 3D dam break.
+
+Workload (N=1 line): the 3D WCSPH dam break in its plain Float64 GPU drop-in form -- fluid block
+1.0 x 0.5 x 1.0 m at dx = 0.008 in a 3.2 x 1.0 x 1.4 m tank with 3 wall layers, h = 1.75 dx,
+WendlandC2, Cole EOS (gamma 7, c = 20 sqrt(9.81)), Monaghan alpha 0.02, Molteni-Colagrossi delta
+0.1, Adami walls, gravity -9.81, CarpenterKennedy2N54 at dt = 5e-5.  One step = one CK2N54 step
+(5 RHS evaluations + the fused 2N update).  particle-steps/s = (n_fluid + n_wall) * steps / s.
+
+The `forms` object adds the precision form (FP32 pair arithmetic) and the FP64 drop-in on the
+finer dx = 0.0064 geometry, with the FP32-vs-FP64 field errors after the timed steps.
+
+Synthetic data: the inputs are the reference's own dam-break setup (RectangularTank with
+hydrostatic density), generated here; no dataset is involved.  The state (> 300 MB) is larger
+than the 129 MB L2, so no L2 flush is needed between steps.
+
+--impl reference: the FP64 CPU restatement of the reference (oracle/, OpenMP on all host cores)
+on the same workload; each timed step is one full CK2N54 step of the full state.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s (3D WCSPH) FP32 vs FP64 at stated error; % of HBM roofline"
+UNIT = "particle-steps/s"
+
+# SURVEY-derived algorithmic byte model (compulsory unique bytes per RHS stage, 3D).
+BYTES_STAGE = {"float64": (352, 88), "float32": (248, 56)}   # (per fluid, per wall)
+BYTES_PAIR = {"float64": (288, 48), "float32": (196, 24)}    # pair kernel + fused update share
+
+CFG1 = dict(name="3D WCSPH dam break FP64 drop-in, dx=0.008 (fluid 1.0x0.5x1.0 m, tank "
+                 "3.2x1.0x1.4 m, 3 layers), CarpenterKennedy2N54 dt=5e-5",
+            dx=0.008, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), layers=3, dt=5e-5)
+CFG2 = dict(name="3D WCSPH dam break dx=0.0064 (same geometry)", dx=0.0064,
+            fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), layers=3, dt=5e-5)
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary (profiles/*.md)."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            if line.startswith(f"traffic_bytes_per_launch[{kernel}]:"):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}",
+                                      f"--query-gpu={self.Q}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if len(s) > 5 + k and s[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def make_case(pkg, cfg, precision, device):
+    tank, eos = pkg.dam_break(3, cfg["dx"], cfg["fluid"], cfg["tank"], n_layers=cfg["layers"])
+    semi = pkg.dam_break_semidiscretization(tank, eos, 1.75 * cfg["dx"], precision=precision,
+                                            device=device)
+    return semi, tank
+
+
+def run_form(pkg, torch, semi, ode, steps, warmup, dt, precision, with_timing=True):
+    """Device-resident timing of `steps` CK2N54 steps (one fused library call)."""
+    v, u = ode.v0.clone(), ode.u0.clone()
+    lib = semi._lib
+    semi._set_stream()
+    if warmup:
+        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(dt), ctypes.c_int64(warmup))
+    semi.sync()
+    lib.tp_enable_timing(semi._handle, 1 if with_timing else 0)
+    l0 = lib.tp_kernel_launches(semi._handle)
+    stream = torch.cuda.current_stream(semi.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+               ctypes.c_double(dt), ctypes.c_int64(steps))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    semi.sync()
+    ms = e0.elapsed_time(e1)
+    launches = lib.tp_kernel_launches(semi._handle) - l0
+    ph = (ctypes.c_double * 3)()
+    lib.tp_phase_times(semi._handle, ph, 3)
+    lib.tp_enable_timing(semi._handle, 0)
+    return v, u, ms, launches, list(ph)
+
+
+def roofline_for(precision, nf, nw, stages, pair_ms, hbm, peak_kind, kernel):
+    bf, bw = BYTES_PAIR[precision]
+    bytes_launch = nf * bf + nw * bw
+    avg_s = pair_ms / 1e3 / stages
+    achieved = bytes_launch / avg_s / 1e9
+    traffic = load_traffic(kernel)
+    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 2),
+            "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+            "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "bytes_per_launch": bytes_launch, "avg_launch_ms": round(pair_ms / stages, 4),
+            "traffic": traffic}
+
+
+def e2e_run(pkg, torch, semi, ode, steps, dt):
+    """Through the public C ABI with HOST buffers: every step copies the state host->device from
+    pinned memory, advances one CK2N54 step and reads the result back to pinned memory."""
+    v_h = ode.v0.cpu().pin_memory()
+    u_h = ode.u0.cpu().pin_memory()
+    v_d, u_d = torch.empty_like(ode.v0), torch.empty_like(ode.u0)
+    stream = torch.cuda.current_stream(semi.device)
+    semi._set_stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        v_d.copy_(v_h, non_blocking=True)
+        u_d.copy_(u_h, non_blocking=True)
+        semi._call("tp_integrate_ck2n54", v_d.data_ptr(), u_d.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(dt), ctypes.c_int64(1))
+        v_h.copy_(v_d, non_blocking=True)
+        u_h.copy_(u_d, non_blocking=True)
+    stream.synchronize()
+    el = time.perf_counter() - t0
+    semi.sync()
+    nbytes = (v_h.numel() + u_h.numel()) * 8
+    return el, nbytes
+
+
+def cpu_baseline(semi, tank, cfg, threads=None):
+    """Bounded CPU sample: one full CK2N54 step of the same state with the FP64 oracle."""
+    import __graft_entry__ as g
+
+    orc = g.load_oracle()
+    orc.build()
+    model = orc.Model(semi.config, tank.boundary.coordinates, tank.boundary.mass,
+                      tank.fluid.mass)
+    nd = 3
+    v = np.zeros((tank.fluid.n_particles, nd + 1))
+    v[:, nd] = tank.fluid.density
+    u = tank.fluid.coordinates.copy()
+    t0 = time.perf_counter()
+    model.integrate(v, u, cfg["dt"], 1)
+    el = time.perf_counter() - t0
+    n = tank.fluid.n_particles + tank.boundary.n_particles
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"1 CarpenterKennedy2N54 step (5 RHS) of the full workload "
+                      f"({n} particles) with the FP64 C++ oracle, OpenMP, {el:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the oracle (C++ FP64 restatement of the reference) on host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import __graft_entry__ as g
+
+    pkg = g.load_package()
+    orc = g.load_oracle()
+    orc.build()
+    tank, eos = pkg.dam_break(3, CFG1["dx"], CFG1["fluid"], CFG1["tank"], n_layers=3)
+    semi = pkg.dam_break_semidiscretization(tank, eos, 1.75 * CFG1["dx"])
+    model = orc.Model(semi.config, tank.boundary.coordinates, tank.boundary.mass,
+                      tank.fluid.mass)
+    v = np.zeros((tank.fluid.n_particles, 4))
+    v[:, 3] = tank.fluid.density
+    u = tank.fluid.coordinates.copy()
+    n = tank.fluid.n_particles + tank.boundary.n_particles
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 2))
+    for _ in range(warm):
+        v, u, _ = model.integrate(v, u, CFG1["dt"], 1)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        v, u, st = model.integrate(v, u, CFG1["dt"], 1)
+    el = time.perf_counter() - t0
+    val = n * steps / el
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": CFG1["name"], "n_fluid": tank.fluid.n_particles,
+                       "n_wall": tank.boundary.n_particles, "parallelism": "host threads"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{steps} full CarpenterKennedy2N54 steps of the "
+                                       f"workload (Julia is absent: the C++ FP64 oracle stands "
+                                       f"in for the reference's threaded CPU path)"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-forms", action="store_true", help="skip the dx=0.0064 form comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+
+    pkg = g.load_package()
+    if rank == 0:
+        pkg.build()
+    if dist:
+        dist.barrier()
+    pkg.load_library()
+    hbm, peak_kind = load_peaks()
+
+    semi, tank = make_case(pkg, CFG1, "float64", local)
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    nf, nw = semi.n_fluid, semi.n_wall
+    ntot = nf + nw
+    dt = CFG1["dt"]
+
+    # warm-up + timed region (barrier + synchronize on both sides, max over ranks)
+    v, u = ode.v0.clone(), ode.u0.clone()
+    semi._set_stream()
+    if args.warmup:
+        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(dt), ctypes.c_int64(args.warmup))
+    semi.sync()
+    lib = semi._lib
+    lib.tp_enable_timing(semi._handle, 1)
+    l0 = lib.tp_kernel_launches(semi._handle)
+    stream = torch.cuda.current_stream(semi.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(dt), ctypes.c_int64(args.steps))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    semi.sync()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = lib.tp_kernel_launches(semi._handle) - l0
+    ph = (ctypes.c_double * 3)()
+    lib.tp_phase_times(semi._handle, ph, 3)
+    lib.tp_enable_timing(semi._handle, 0)
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device=semi.device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = ntot * args.steps * world / (ms_max / 1e3)
+    stages = 5 * args.steps
+    bf, bw = BYTES_STAGE["float64"]
+    step_bytes = 5 * (nf * bf + nw * bw)
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(1, min(args.steps, 10))
+    el, nbytes = e2e_run(pkg, torch, semi, ode, e2e_steps, dt)
+    e2e_val = ntot * e2e_steps * world / el
+
+    out = None
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": CFG1["name"], "n_fluid": nf, "n_wall": nw,
+                       "particles": ntot, "dx": CFG1["dx"], "dt": dt,
+                       "l2": "inputs larger than L2 (state + records > 300 MB), no flush",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "roofline": roofline_for("float64", nf, nw, stages, ph[2], hbm, peak_kind,
+                                     "k_pair64"),
+            "step_roofline": {"bytes_per_step": step_bytes,
+                              "achieved_gbs": round(step_bytes / (ms_max / args.steps / 1e3)
+                                                    / 1e9, 2),
+                              "frac": round(step_bytes / (ms_max / args.steps / 1e3) / 1e9
+                                            / hbm, 4)},
+            "phase_ms_per_step": {"update nhs": ph[0] / args.steps,
+                                  "compute boundary pressure": ph[1] / args.steps,
+                                  "system interaction": ph[2] / args.steps},
+            "e2e": {"value": e2e_val, "unit": UNIT, "steps": e2e_steps,
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+    semi.close()
+    del ode
+
+    # precision forms on the finer geometry (rank 0 only, not part of the timed value)
+    if rank == 0 and not args.no_forms:
+        k = max(1, min(args.steps, 5))
+        forms = {}
+        res = {}
+        for prec in ("float64", "float32"):
+            s2, t2 = make_case(pkg, CFG2, prec, local)
+            o2 = pkg.semidiscretize(s2, (0.0, 1.0))
+            v2, u2, ms2, l2, ph2 = run_form(pkg, torch, s2, o2, k, 1, CFG2["dt"], prec)
+            n2 = s2.n_fluid + s2.n_wall
+            forms[prec] = {
+                "value": n2 * k / (ms2 / 1e3), "ms_per_step": ms2 / k, "steps": k,
+                "n_fluid": s2.n_fluid, "n_wall": s2.n_wall,
+                "roofline": roofline_for(prec, s2.n_fluid, s2.n_wall, 5 * k, ph2[2], hbm,
+                                         peak_kind, "k_pair64" if prec == "float64"
+                                         else "k_pair32"),
+                "step_hbm_frac": round(5 * (s2.n_fluid * BYTES_STAGE[prec][0] + s2.n_wall
+                                            * BYTES_STAGE[prec][1]) / (ms2 / k / 1e3) / 1e9
+                                       / hbm, 4),
+            }
+            res[prec] = (v2.view(-1, 4).cpu().numpy(), u2.view(-1, 3).cpu().numpy())
+            s2.close()
+        (v64, u64), (v32, u32) = res["float64"], res["float32"]
+
+        def rl2(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+        forms["fp32_vs_fp64"] = {
+            "speedup": forms["float32"]["value"] / forms["float64"]["value"],
+            "after_steps": k,
+            "rel_l2_rho": rl2(v32[:, 3], v64[:, 3]),
+            "rel_l2_v": rl2(v32[:, :3], v64[:, :3]),
+            "rel_l2_x": rl2(u32, u64)}
+        forms["workload"] = CFG2["name"]
+        out["forms"] = forms
+
+    if rank == 0 and not args.no_cpu:
+        semi_c, tank_c = make_case(pkg, CFG1, "float64", local)
+        out["cpu_baseline"] = cpu_baseline(semi_c, tank_c, CFG1)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

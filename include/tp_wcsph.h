@@ -1,0 +1,212 @@
+/*
+ * tp_wcsph.h — C ABI of the GB300 (sm_103a) weakly-compressible SPH right-hand side.
+ *
+ * This library is a drop-in backend for the WCSPH hot path of TrixiParticles.jl:
+ * the fluid/wall system pair
+ *   WeaklyCompressibleSPHSystem(ContinuityDensity, WendlandC2Kernel, StateEquationCole,
+ *                               ArtificialViscosityMonaghan, DensityDiffusionMolteniColagrossi)
+ *   WallBoundarySystem(BoundaryModelDummyParticles(AdamiPressureExtrapolation))
+ * under Semidiscretization(...; neighborhood_search=GridNeighborhoodSearch{d}(;
+ * cell_list=FullGridCellList(...)), parallelization_backend=<GPU>).
+ *
+ * Each entry point names the reference function it replaces (paths are relative to the
+ * TrixiParticles.jl source tree).  All array arguments of the compute entry points are
+ * DEVICE pointers (CUDA global memory) in the reference's column-major SoA layout:
+ *   u_ode : (ndims,   n_fluid)  -> particle i, component k at u_ode[i*ndims + k]
+ *   v_ode : (ndims+1, n_fluid)  -> velocity in rows 0..ndims-1, density in row ndims
+ *   dv_ode: same layout as v_ode;  du_ode: same layout as u_ode.
+ * (src/general/semidiscretization.jl:457-508 wrap_u/wrap_v;
+ *  src/schemes/fluid/weakly_compressible_sph/system.jl:232-242 v_nvariables.)
+ *
+ * Calls on one handle are serialised on the handle's CUDA stream and are asynchronous
+ * with respect to the host: call tp_sync() (or synchronise the stream) before reading
+ * results on the host.  Errors found on the device (a particle outside the cell grid,
+ * a non-finite coordinate) are latched in a device word and returned by the next
+ * tp_sync() as TP_ERR_OUT_OF_GRID / TP_ERR_NONFINITE.  No entry point aborts the process.
+ */
+#ifndef TP_WCSPH_H
+#define TP_WCSPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TP_ABI_VERSION 1
+
+typedef enum tp_status {
+    TP_OK = 0,
+    TP_ERR_ARGUMENT = 1,        /* invalid argument (null pointer, bad size, bad config)  */
+    TP_ERR_CUDA = 2,            /* a CUDA runtime call failed                             */
+    TP_ERR_OUT_OF_GRID = 3,     /* a particle left the FullGridCellList bounding box      */
+    TP_ERR_NOT_READY = 4,       /* wall geometry / masses not set yet                     */
+    TP_ERR_UNSUPPORTED = 5,     /* configuration outside the implemented hot path         */
+    TP_ERR_NONFINITE = 6,       /* NaN or Inf coordinate seen by the neighbour search     */
+    TP_ERR_CAPACITY = 7         /* request larger than a fixed capacity                   */
+} tp_status;
+
+/* Arithmetic form of the pair kernels. */
+enum {
+    TP_PRECISION_FP64 = 0, /* plain drop-in: every quantity in Float64, like the reference  */
+    TP_PRECISION_FP32 = 1  /* precision form: FP32 pair arithmetic on cell-relative offsets,
+                              Kahan-compensated FP32 sums, FP64 positions and reductions  */
+};
+
+enum { TP_VISCOSITY_NONE = 0, TP_VISCOSITY_MONAGHAN = 1 };
+enum { TP_DIFFUSION_NONE = 0, TP_DIFFUSION_MOLTENI_COLAGROSSI = 1 };
+
+/*
+ * Plain-old-data configuration.  Field meanings follow the reference constructors:
+ *   smoothing_length      WeaklyCompressibleSPHSystem(...; smoothing_length) and the wall
+ *                         BoundaryModelDummyParticles smoothing length (must be equal here);
+ *                         the kernel is WendlandC2Kernel{ndims} (compact support 2h).
+ *   reference_density,sound_speed,exponent,background_pressure
+ *                         StateEquationCole (state_equations.jl:100-139); the same EOS is used
+ *                         by the fluid and by the Adami wall model.
+ *   fluid_clip_negative_pressure   StateEquationCole(...; clip_negative_pressure)
+ *   wall_clip_negative_pressure    BoundaryModelDummyParticles(...; clip_negative_pressure)
+ *   viscosity_*           ArtificialViscosityMonaghan(alpha, beta, epsilon) (viscosity.jl:68-132)
+ *   density_diffusion_delta  DensityDiffusionMolteniColagrossi(delta) (density_diffusion.jl:41-55)
+ *   acceleration          fluid system gravity (semidiscretization.jl:701-731)
+ *   pressure_offset       AdamiPressureExtrapolation(pressure_offset) (dummy_particles.jl:142-149)
+ *   min_corner/max_corner FullGridCellList(; min_corner, max_corner); every particle must stay
+ *                         inside this box (the grid adds one padding layer of cells per side).
+ */
+typedef struct tp_config {
+    int32_t ndims;                       /* 2 or 3                                          */
+    int32_t precision;                   /* TP_PRECISION_*                                  */
+    int64_t n_fluid;                     /* integrated fluid particles (>= 0)               */
+    int64_t n_wall;                      /* dummy wall particles (>= 0)                     */
+    double smoothing_length;
+    double reference_density;
+    double sound_speed;
+    double exponent;
+    double background_pressure;
+    int32_t fluid_clip_negative_pressure;
+    int32_t wall_clip_negative_pressure;
+    int32_t viscosity_model;             /* TP_VISCOSITY_*                                  */
+    int32_t density_diffusion_model;     /* TP_DIFFUSION_*                                  */
+    double viscosity_alpha;
+    double viscosity_beta;
+    double viscosity_epsilon;
+    double density_diffusion_delta;
+    double acceleration[3];
+    double pressure_offset;
+    double min_corner[3];
+    double max_corner[3];
+} tp_config;
+
+typedef struct tp_handle tp_handle;
+
+/* Version of this ABI (TP_ABI_VERSION). */
+int32_t tp_abi_version(void);
+
+/* Fill *cfg with the reference defaults (Monaghan alpha=0.02 beta=0 epsilon=0.01,
+ * Molteni-Colagrossi delta=0.1, no clipping, zero offsets).  Sizes and bounds stay zero. */
+void tp_config_default(tp_config* cfg);
+
+/*
+ * Create a handle: validates the configuration, lays out the cell grid and allocates the
+ * device buffers.  Replaces the device-side part of
+ * semidiscretize (src/general/semidiscretization.jl:293-396: allocate, initialize NHS,
+ * Adapt systems to the device) for the supported system pair.
+ */
+tp_status tp_create(const tp_config* cfg, tp_handle** out);
+tp_status tp_destroy(tp_handle* h);
+
+/* Use `stream` (a cudaStream_t, may be NULL = legacy default stream) for every launch. */
+tp_status tp_set_stream(tp_handle* h, void* stream);
+
+/*
+ * Static wall: coordinates (ndims, n_wall) and hydrodynamic masses (n_wall), device pointers.
+ * Builds the wall cell list once (walls do not move: WallBoundarySystem.ismoving = false,
+ * neighborhood_search.jl:509-519, 671-686).
+ */
+tp_status tp_set_wall(tp_handle* h, const double* x_wall, const double* m_wall);
+
+/* Fluid masses (n_fluid), device pointer (WeaklyCompressibleSPHSystem.mass). */
+tp_status tp_set_fluid_mass(tp_handle* h, const double* m_fluid);
+
+/*
+ * One right-hand-side evaluation dv = kick!(v, u) (semidiscretization.jl:589-612):
+ * zero dv -> neighbour search update -> fluid EOS -> Adami wall pressure -> fluid-fluid and
+ * fluid-wall interactions (weakly_compressible_sph/rhs.jl:5-127) -> gravity.
+ * `dv_ode` must not alias `v_ode`/`u_ode`.  `t` is accepted for interface parity (unused:
+ * the supported RHS is autonomous).
+ */
+tp_status tp_kick(tp_handle* h, double* dv_ode, const double* v_ode, const double* u_ode,
+                  double t);
+
+/* du = drift!(v, u) (semidiscretization.jl:522-536, 561-571): du[:, i] = v[1:ndims, i]. */
+tp_status tp_drift(tp_handle* h, double* du_ode, const double* v_ode, const double* u_ode,
+                   double t);
+
+/*
+ * `n_steps` steps of the five-stage fourth-order low-storage Runge-Kutta method
+ * CarpenterKennedy2N54(williamson_condition=false) at fixed `dt`, advancing v_ode and u_ode
+ * in place (device pointers).  Every stage evaluates kick!/drift! exactly as tp_kick/tp_drift,
+ * fused with the 2N register update.  Replaces the OrdinaryDiffEq stage loop that calls
+ * kick!/drift! five times per step.  Particles are kept physically ordered by cell inside the
+ * library (the SortingCallback idea, src/callbacks/sorting.jl:116-158); v_ode/u_ode are
+ * written back in the caller's particle order.
+ */
+tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double t0,
+                              double dt, int64_t n_steps);
+
+/* Fluid pressure (n_fluid) from the last kick, in caller order (system.jl:426-438). */
+tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid);
+
+/* Wall pressure, density and kernel volume sum (n_wall each, caller order) from the last
+ * Adami update (dummy_particles.jl:489-569).  Any pointer may be NULL. */
+tp_status tp_wall_state(tp_handle* h, double* p_wall, double* rho_wall, double* volume_wall);
+
+/*
+ * Neighbour-search diagnostics for coordinates u_ode (device pointers, all int32, any may be
+ * NULL):  cell[i]      linear cell index of fluid particle i (x fastest) in the padded grid,
+ *         order[k]     fluid particle index at position k of the cell-sorted order
+ *                      (stable: ties broken by ascending particle index),
+ *         nnb_ff[i]    fluid neighbours b of fluid particle i with |x_i - x_b|^2 <= (2h)^2
+ *                      (i itself included, as the reference's foreach_neighbor visits it),
+ *         nnb_fw[i]    wall neighbours of fluid particle i, same criterion,
+ *         nnb_wf[w]    fluid neighbours of wall particle w, same criterion.
+ */
+tp_status tp_nhs_debug(tp_handle* h, const double* u_ode, int32_t* cell, int32_t* order,
+                       int32_t* nnb_ff, int32_t* nnb_fw, int32_t* nnb_wf);
+
+/* Grid layout: dims[0..2] cells per dimension (padding included), *cell_size = 2h. */
+tp_status tp_grid_info(tp_handle* h, int32_t dims[3], double* cell_size, double lo[3]);
+
+/*
+ * Conservation reductions over the fluid in FP64 (the quantities of
+ * src/general/custom_quantities.jl:6-57): out[0] = total mass, out[1..3] = linear momentum
+ * (out[3] = 0 in 2D), out[4] = kinetic energy.  v_ode is a device pointer, `out` is HOST
+ * memory; the call synchronises the handle's stream.  Partial sums are combined in a fixed
+ * order, so the result is deterministic.
+ */
+tp_status tp_conservation(tp_handle* h, const double* v_ode, double out[5]);
+
+/* Block until all work on the handle's stream is done; returns latched device errors. */
+tp_status tp_sync(tp_handle* h);
+
+/* Per-phase device time (ms), summed over the RHS evaluations of the last tp_kick /
+ * tp_integrate_ck2n54 call, when timing is enabled.  Phases carry the reference's TimerOutputs
+ * labels (semidiscretization.jl:596-609): 0 "update nhs" (neighbour search incl. the fluid EOS
+ * pack), 1 "compute boundary pressure" (Adami), 2 "system interaction" (pair kernel with the
+ * fused Runge-Kutta update).  Events are read back once at the end of the call, so timing adds
+ * no synchronisation inside the stage loop.  Returns the number of phases. */
+int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n);
+tp_status tp_enable_timing(tp_handle* h, int32_t enable);
+
+/* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
+int64_t tp_kernel_launches(const tp_handle* h);
+
+/* Last error message of the handle (or of the last failed tp_create when h is NULL). */
+const char* tp_last_error(const tp_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TP_WCSPH_H */

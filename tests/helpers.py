@@ -1,0 +1,78 @@
+"""Shared setups of the tests: dam-break cases and the 2D validation run."""
+from __future__ import annotations
+
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def dam_break_case(pkg, ndims, dx, fluid, tank, layers=3, precision="float64", h_factor=1.75,
+                   jitter=0.0, seed=0, alpha=0.02, delta=0.1):
+    """A dam-break Semidiscretization (not yet on the device) plus its tank."""
+    tank_, eos = pkg.dam_break(ndims, dx, fluid, tank, n_layers=layers)
+    if jitter:
+        rng = np.random.default_rng(seed)
+        tank_.fluid.coordinates += rng.uniform(-jitter * dx, jitter * dx,
+                                               tank_.fluid.coordinates.shape)
+    semi = pkg.dam_break_semidiscretization(tank_, eos, h_factor * dx, precision=precision,
+                                            alpha=alpha, delta=delta)
+    return semi, tank_
+
+
+def initial_state(tank):
+    nd = tank.fluid.ndims
+    v = np.zeros((tank.fluid.n_particles, nd + 1))
+    v[:, nd] = tank.fluid.density
+    return v, tank.fluid.coordinates.copy()
+
+
+def oracle_model(orc, semi, tank):
+    return orc.Model(semi.config, tank.boundary.coordinates, tank.boundary.mass, tank.fluid.mass)
+
+
+def load_validation():
+    return json.loads((GOLDEN / "validation_wcsph_40.json").read_text())
+
+
+def validation_case(pkg, precision="float64"):
+    """validation/dam_break_2d setup at 40 particles per H (setup_marrone_2011.jl)."""
+    g = load_validation()
+    P = g["params"]
+    H, dx, grav = P["H"], P["particle_spacing"], 9.81
+    tank_x = math.floor(5.366 * H / dx) * dx
+    eos = pkg.StateEquationCole(sound_speed=P["sound_speed"], reference_density=1000.0,
+                                exponent=P["exponent"])
+    tank = pkg.RectangularTank(dx, (P["W"], H), (tank_x, 4.0), 1000.0, n_layers=P["n_layers"],
+                               acceleration=(0.0, -grav), state_equation=eos)
+    semi = pkg.dam_break_semidiscretization(tank, eos, P["smoothing_length"], precision=precision,
+                                            alpha=P["alpha"], delta=P["delta"])
+    return semi, tank, g
+
+
+def validation_schedule(g, n_samples):
+    """Step sizes of the reference run: dt_max steps, shortened to land on every save time."""
+    save = 0.01 / math.sqrt(9.81 / g["params"]["H"])
+    dtmax = g["params"]["dt_max"]
+    t = 0.0
+    sched = []
+    for k in range(1, n_samples):
+        tstop = k * save
+        steps = []
+        while t < tstop - 1e-12:
+            dt = min(dtmax, tstop - t)
+            steps.append(dt)
+            t = t + dt
+            if abs(t - tstop) < 1e-12:
+                t = tstop
+        sched.append(steps)
+    return sched
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

@@ -1,0 +1,70 @@
+"""Neighbour search on the GPU: cell indices, sorted order and neighbour counts are bit-exact
+against the oracle (PointNeighbors convention restated there)."""
+import numpy as np
+import pytest
+
+from helpers import dam_break_case
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    dict(ndims=2, dx=0.02, fluid=(2.0, 1.0), tank=(5.366, 4.0), jitter=0.0),
+    dict(ndims=2, dx=0.02, fluid=(2.0, 1.0), tank=(5.366, 4.0), jitter=0.3),
+    dict(ndims=3, dx=0.05, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.0),
+    dict(ndims=3, dx=0.05, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.45),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c['ndims']}d-j{c['jitter']}")
+def test_nhs_bit_exact(pkg, orc, cuda, case):
+    semi, tank = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"],
+                                jitter=case["jitter"], seed=7)
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    got = semi.nhs_debug(ode.u0)
+    semi.sync()
+    ref, st = orc.nhs(semi.config, tank.fluid.coordinates, tank.boundary.coordinates)
+    assert st == 0
+    for k in ("cell", "order", "nnb_ff", "nnb_fw", "nnb_wf"):
+        g = got[k].cpu().numpy()
+        assert np.array_equal(g, ref[k]), k
+    # sanity: every fluid particle sees itself, interior particles see the lattice neighbours
+    assert ref["nnb_ff"].min() >= 1
+    semi.close()
+
+
+def test_nhs_empty_fluid_cells_and_repeat(pkg, orc, cuda):
+    # repeated rebuilds reuse the zeroed histogram: results must not drift between calls
+    semi, tank = dam_break_case(pkg, 2, 0.05, (1.0, 0.5), (2.0, 1.0), jitter=0.2, seed=3)
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    a = semi.nhs_debug(ode.u0)
+    b = semi.nhs_debug(ode.u0)
+    semi.sync()
+    for k in a:
+        assert np.array_equal(a[k].cpu().numpy(), b[k].cpu().numpy()), k
+    semi.close()
+
+
+def test_out_of_grid_and_nonfinite_are_reported(pkg, cuda):
+    torch = cuda
+    semi, tank = dam_break_case(pkg, 2, 0.05, (1.0, 0.5), (2.0, 1.0))
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    u = ode.u0.clone()
+    u[0] = 1.0e3  # far outside the FullGridCellList bounding box
+    semi.nhs_debug(u)
+    with pytest.raises(pkg.TpError) as e:
+        semi.sync()
+    assert e.value.status == 3
+    u = ode.u0.clone()
+    u[1] = float("nan")
+    semi.nhs_debug(u)
+    with pytest.raises(pkg.TpError) as e:
+        semi.sync()
+    assert e.value.status == 6
+    # the latched error is cleared once reported
+    semi.nhs_debug(ode.u0)
+    semi.sync()
+    dv = torch.zeros_like(ode.v0)
+    pkg.kick(dv, ode.v0, ode.u0, ode.p, 0.0)
+    semi.sync()
+    assert torch.isfinite(dv).all()
+    semi.close()

@@ -1,0 +1,56 @@
+"""Host-side mirror of the reference surface: configuration checks without a GPU."""
+import numpy as np
+import pytest
+
+from helpers import dam_break_case
+
+
+def test_config_from_dam_break(pkg):
+    semi, tank = dam_break_case(pkg, 2, 0.02, (2.0, 1.0), (5.366, 4.0))
+    c = semi.config
+    assert (c.ndims, c.n_fluid, c.n_wall) == (2, 5000, 2844)
+    assert c.smoothing_length == 1.75 * 0.02
+    assert c.sound_speed == 20 * np.sqrt(9.81)
+    assert c.viscosity_alpha == 0.02 and c.density_diffusion_delta == 0.1
+    assert c.wall_clip_negative_pressure == 1 and c.fluid_clip_negative_pressure == 0
+    assert c.min_corner[0] == tank.boundary.coordinates[:, 0].min()
+    assert c.max_corner[1] == tank.boundary.coordinates[:, 1].max()
+
+
+def _systems(pkg):
+    semi, tank = dam_break_case(pkg, 2, 0.05, (1.0, 0.5), (2.0, 1.0))
+    return semi.fluid, semi.wall, semi.neighborhood_search
+
+
+def test_rejects_single_system(pkg):
+    f, w, nhs = _systems(pkg)
+    with pytest.raises(ValueError, match="ArgumentError"):
+        pkg.Semidiscretization(f, neighborhood_search=nhs,
+                               parallelization_backend=pkg.GB300Backend())
+
+
+def test_rejects_other_kernel_and_models(pkg):
+    import dataclasses
+
+    f, w, nhs = _systems(pkg)
+    for change in [dict(smoothing_kernel=pkg.WendlandC2Kernel(3)), dict(correction="shepard"),
+                   dict(viscosity="morris"), dict(density_diffusion="antuono"),
+                   dict(density_calculator=None)]:
+        f2 = dataclasses.replace(f, **change)
+        with pytest.raises(ValueError, match="ArgumentError"):
+            pkg.Semidiscretization(f2, w, neighborhood_search=nhs,
+                                   parallelization_backend=pkg.GB300Backend())
+
+
+def test_rejects_missing_cell_list_and_wall_eos(pkg):
+    import dataclasses
+
+    f, w, nhs = _systems(pkg)
+    with pytest.raises(ValueError, match="FullGridCellList"):
+        pkg.Semidiscretization(f, w, neighborhood_search=pkg.GridNeighborhoodSearch(2),
+                               parallelization_backend=pkg.GB300Backend())
+    bm = dataclasses.replace(w.boundary_model, state_equation=None)
+    w2 = dataclasses.replace(w, boundary_model=bm)
+    with pytest.raises(ValueError, match="state_equation"):
+        pkg.Semidiscretization(f, w2, neighborhood_search=nhs,
+                               parallelization_backend=pkg.GB300Backend())

@@ -1,0 +1,40 @@
+"""GB300 (sm_103a) backend for the weakly-compressible SPH right-hand side of TrixiParticles.jl.
+
+The compute path is libtp_wcsph.so (CUDA C++ behind the C ABI of include/tp_wcsph.h); this
+package is the host-side mirror of the reference's drop-in surface (Semidiscretization,
+semidiscretize, kick!/drift!, solve with CarpenterKennedy2N54) plus the dam-break setup.
+"""
+from ._abi import TpConfig, TpError, default_config, load_library
+from .build import build
+from .semidiscretization import (
+    AdamiPressureExtrapolation,
+    ArtificialViscosityMonaghan,
+    BoundaryModelDummyParticles,
+    CarpenterKennedy2N54,
+    ContinuityDensity,
+    DensityDiffusionMolteniColagrossi,
+    FullGridCellList,
+    GB300Backend,
+    GridNeighborhoodSearch,
+    ODEProblem,
+    Semidiscretization,
+    WallBoundarySystem,
+    WeaklyCompressibleSPHSystem,
+    WendlandC2Kernel,
+    dam_break_semidiscretization,
+    drift,
+    kick,
+    semidiscretize,
+    solve,
+)
+from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
+
+__all__ = [
+    "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
+    "CarpenterKennedy2N54", "ContinuityDensity", "DensityDiffusionMolteniColagrossi",
+    "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
+    "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole", "TpConfig",
+    "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
+    "build", "dam_break", "dam_break_semidiscretization", "default_config", "drift", "kick",
+    "load_library", "semidiscretize", "solve",
+]

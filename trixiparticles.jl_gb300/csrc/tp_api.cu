@@ -1,0 +1,844 @@
+// tp_api.cu — C ABI of the sm_103a WCSPH library: handle, neighbour-search orchestration,
+// kick!/drift! and the fused CarpenterKennedy2N54 integrator.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tp_api_internal.h"
+#include "tp_nhs.cuh"
+
+using namespace tp;
+
+namespace {
+
+std::string g_create_error;  // message of the last failed tp_create
+
+inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
+
+tp_status fail(tp_handle* h, tp_status st, const std::string& msg) {
+    if (h) h->last_error = msg;
+    return st;
+}
+
+tp_status cuda_fail(tp_handle* h, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fail(h, TP_ERR_CUDA, m);
+}
+
+#define TP_CUDA(h, call)                                   \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+    } while (0)
+
+#define TP_LAUNCHED(h, where)                              \
+    do {                                                   \
+        cudaError_t e_ = cudaGetLastError();               \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, where); \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+// CarpenterKennedy2N54 (Carpenter & Kennedy 1994, (5,4) 2N-storage, solution 3).
+const double kA[5] = {0.0,
+                      -567301805773.0 / 1357537059087.0,
+                      -2404267990393.0 / 2016746695238.0,
+                      -3550918686646.0 / 2091501179385.0,
+                      -1275806237668.0 / 842570457699.0};
+const double kB[5] = {1432997174477.0 / 9575080441755.0,
+                      5161836677717.0 / 13612068292357.0,
+                      1720146321549.0 / 2090206949498.0,
+                      3134564353537.0 / 4481467310338.0,
+                      2277821191437.0 / 14882151754819.0};
+
+// ---------------------------------------------------------------------------------------
+// Small kernels of the API layer
+// ---------------------------------------------------------------------------------------
+template <int ND>
+__global__ void k_drift(double* __restrict__ du, const double* __restrict__ v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) du[(size_t)i * ND + d] = v[(size_t)i * (ND + 1) + d];
+}
+
+__global__ void k_iota(int* __restrict__ id, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) id[i] = i;
+}
+
+// FP32 form: caller FP64 (v, rho) and masses -> float4 {v, rho - rho0}, float m.
+template <int ND>
+__global__ void k_load32(const double* __restrict__ v, const double* __restrict__ m, double rho0,
+                         float4* __restrict__ v32, float* __restrict__ m32, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* vv = v + (size_t)i * (ND + 1);
+    v32[i] = make_float4((float)vv[0], (float)vv[1], ND == 3 ? (float)vv[2] : 0.0f,
+                         (float)(vv[ND] - rho0));
+    m32[i] = (float)m[i];
+}
+
+// Slot-ordered integrator state -> caller order.
+template <int ND, bool F32>
+__global__ void k_store(const double* __restrict__ u, const void* __restrict__ v,
+                        const int* __restrict__ id, double rho0, double* __restrict__ u_out,
+                        double* __restrict__ v_out, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = id[s];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) u_out[(size_t)i * ND + d] = u[(size_t)s * ND + d];
+    if (F32) {
+        const float4 w = ((const float4*)v)[s];
+        const float a[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) v_out[(size_t)i * (ND + 1) + d] = (double)a[d];
+        v_out[(size_t)i * (ND + 1) + ND] = rho0 + (double)w.w;
+    } else {
+        const double* vv = (const double*)v;
+#pragma unroll
+        for (int d = 0; d <= ND; ++d)
+            v_out[(size_t)i * (ND + 1) + d] = vv[(size_t)s * (ND + 1) + d];
+    }
+}
+
+template <bool F32>
+__global__ void k_scatter_pressure(const void* __restrict__ pos, const int* __restrict__ perm,
+                                   double* __restrict__ p, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    p[perm[s]] = F32 ? (double)((const float4*)pos)[s].w : ((const double4_32a*)pos)[s].w;
+}
+
+template <bool F32>
+__global__ void k_scatter_wall(const void* __restrict__ state, const double* __restrict__ vol,
+                               const int* __restrict__ perm, double rho0, double* __restrict__ p,
+                               double* __restrict__ rho, double* __restrict__ volume, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = perm[s];
+    double ps, rs;
+    if (F32) {
+        const float2 st = ((const float2*)state)[s];
+        ps = st.x;
+        rs = rho0 + (double)st.y;
+    } else {
+        const double2 st = ((const double2*)state)[s];
+        ps = st.x;
+        rs = st.y;
+    }
+    if (p) p[i] = ps;
+    if (rho) rho[i] = rs;
+    if (volume) volume[i] = vol[s];
+}
+
+// FP64 conservation partial sums per block: mass, momentum (3), kinetic energy.
+template <int ND>
+__global__ void __launch_bounds__(256) k_conservation(const double* __restrict__ v,
+                                                      const double* __restrict__ m, int n,
+                                                      double* __restrict__ partial) {
+    __shared__ double sm[5][8];
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double mi = m[i];
+        double e = 0.0;
+        acc[0] += mi;
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double vd = v[(size_t)i * (ND + 1) + d];
+            acc[1 + d] += mi * vd;
+            e += vd * vd;
+        }
+        acc[4] += 0.5 * mi * e;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        double x = acc[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        if ((threadIdx.x & 31) == 0) sm[k][threadIdx.x >> 5] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double x = 0.0;
+        for (int w = 0; w < 8; ++w) x += sm[threadIdx.x][w];
+        partial[blockIdx.x * 5 + threadIdx.x] = x;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Host helpers
+// ---------------------------------------------------------------------------------------
+tp_status check_config(const tp_config* c, std::string& msg) {
+    if (!c) { msg = "null config"; return TP_ERR_ARGUMENT; }
+    if (c->ndims != 2 && c->ndims != 3) { msg = "ndims must be 2 or 3"; return TP_ERR_ARGUMENT; }
+    if (c->precision != TP_PRECISION_FP64 && c->precision != TP_PRECISION_FP32) {
+        msg = "precision must be TP_PRECISION_FP64 or TP_PRECISION_FP32";
+        return TP_ERR_ARGUMENT;
+    }
+    if (c->n_fluid < 0 || c->n_wall < 0 || c->n_fluid >= (int64_t(1) << 30) ||
+        c->n_wall >= (int64_t(1) << 30)) {
+        msg = "particle counts must be in [0, 2^30)";
+        return TP_ERR_ARGUMENT;
+    }
+    if (!(c->smoothing_length > 0.0) || !std::isfinite(c->smoothing_length)) {
+        msg = "smoothing_length must be positive and finite";
+        return TP_ERR_ARGUMENT;
+    }
+    if (!(c->reference_density > 0.0) || !(c->sound_speed > 0.0) || !(c->exponent > 0.0)) {
+        msg = "reference_density, sound_speed and exponent must be positive";
+        return TP_ERR_ARGUMENT;
+    }
+    if (c->viscosity_model != TP_VISCOSITY_NONE && c->viscosity_model != TP_VISCOSITY_MONAGHAN) {
+        msg = "unsupported viscosity model";
+        return TP_ERR_UNSUPPORTED;
+    }
+    if (c->density_diffusion_model != TP_DIFFUSION_NONE &&
+        c->density_diffusion_model != TP_DIFFUSION_MOLTENI_COLAGROSSI) {
+        msg = "unsupported density diffusion model";
+        return TP_ERR_UNSUPPORTED;
+    }
+    for (int d = 0; d < c->ndims; ++d) {
+        if (!std::isfinite(c->min_corner[d]) || !std::isfinite(c->max_corner[d]) ||
+            !(c->min_corner[d] <= c->max_corner[d])) {
+            msg = "FullGridCellList bounds must be finite with min_corner <= max_corner";
+            return TP_ERR_ARGUMENT;
+        }
+    }
+    return TP_OK;
+}
+
+void setup_phys(tp_handle* h) {
+    const tp_config& c = h->cfg;
+    Phys& P = h->phys;
+    const double pi = 3.141592653589793;
+    P.nd = c.ndims;
+    P.h = c.smoothing_length;
+    P.h_inv = 1.0 / P.h;
+    P.two_h = 2.0 * P.h;
+    P.sr2 = P.two_h * P.two_h;
+    P.almostzero = std::sqrt(std::nextafter(P.sr2, INFINITY) - P.sr2);
+    P.hi2 = P.h_inv * P.h_inv;
+    P.wc2_norm = (c.ndims == 2) ? (7.0 / (4.0 * pi)) * (P.h_inv * P.h_inv)
+                                : (21.0 / (16.0 * pi)) * ((P.h_inv * P.h_inv) * P.h_inv);
+    P.wc2_dnorm = -5.0 * P.wc2_norm;
+    P.rho0 = c.reference_density;
+    P.c = c.sound_speed;
+    P.gamma = c.exponent;
+    P.p_bg = c.background_pressure;
+    P.B = (P.rho0 * (P.c * P.c)) / P.gamma;
+    P.inv_gamma = 1.0 / P.gamma;
+    P.fluid_clip = c.fluid_clip_negative_pressure != 0;
+    P.wall_clip = c.wall_clip_negative_pressure != 0;
+    P.visc = c.viscosity_model == TP_VISCOSITY_MONAGHAN;
+    P.alpha = c.viscosity_alpha;
+    P.beta = c.viscosity_beta;
+    P.eps_visc = c.viscosity_epsilon;
+    P.visc_h = (P.h + P.h) / 2.0;
+    P.visc_eps_h2 = P.eps_visc * (P.visc_h * P.visc_h);
+    P.visc_mac = P.alpha * P.c;
+    P.diff = c.density_diffusion_model == TP_DIFFUSION_MOLTENI_COLAGROSSI;
+    P.delta = c.density_diffusion_delta;
+    P.diff_coef = (P.delta * ((P.h + P.h) / 2.0)) * P.c;
+    for (int d = 0; d < 3; ++d) P.g[d] = (d < c.ndims) ? c.acceleration[d] : 0.0;
+    P.p_off = c.pressure_offset;
+
+    Phys32& Q = h->phys32;
+    const float h32 = (float)P.h;
+    Q.cs = (float)h->grid.cs;
+    Q.h_inv = 1.0f / h32;
+    Q.two_h = 2.0f * h32;
+    Q.sr2 = Q.two_h * Q.two_h;
+    Q.almostzero = std::sqrt(std::nextafter(Q.sr2, INFINITY) - Q.sr2);
+    Q.hi2 = Q.h_inv * Q.h_inv;
+    Q.wc2_norm = (c.ndims == 2) ? (float)(7.0 / (4.0 * pi)) * (Q.h_inv * Q.h_inv)
+                                : (float)(21.0 / (16.0 * pi)) * ((Q.h_inv * Q.h_inv) * Q.h_inv);
+    Q.wc2_dnorm = -5.0f * Q.wc2_norm;
+    Q.rho0 = (float)P.rho0;
+    Q.B = (float)P.B;
+    Q.gamma = (float)P.gamma;
+    Q.inv_gamma = (float)P.inv_gamma;
+    Q.p_bg = (float)P.p_bg;
+    Q.fluid_clip = P.fluid_clip;
+    Q.wall_clip = P.wall_clip;
+    Q.visc = P.visc;
+    Q.diff = P.diff;
+    Q.beta = (float)P.beta;
+    Q.visc_h = (float)P.visc_h;
+    Q.visc_eps_h2 = (float)P.visc_eps_h2;
+    Q.visc_ac = (float)(P.alpha * P.c);
+    Q.diff_coef = (float)P.diff_coef;
+    for (int d = 0; d < 3; ++d) Q.g[d] = (float)P.g[d];
+    Q.p_off = (float)P.p_off;
+}
+
+bool setup_grid(tp_handle* h, std::string& msg) {
+    const tp_config& c = h->cfg;
+    GridDesc& g = h->grid;
+    g.nd = c.ndims;
+    g.cs = 2.0 * c.smoothing_length;
+    long long total = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (d < c.ndims) {
+            const double lo = std::floor(c.min_corner[d] / g.cs) - 1.0;
+            const double hi = std::floor(c.max_corner[d] / g.cs) + 1.0;
+            if (!(std::fabs(lo) < 1e9 && std::fabs(hi) < 1e9)) {
+                msg = "bounding box too large for the cell size";
+                return false;
+            }
+            g.cmin[d] = (int)lo;
+            g.n[d] = (int)(hi - lo) + 1;
+        } else {
+            g.cmin[d] = 0;
+            g.n[d] = 1;
+        }
+        total *= g.n[d];
+        if (total >= (1LL << 30)) {
+            msg = "cell grid larger than 2^30 cells";
+            return false;
+        }
+    }
+    g.ncells = (int)total;
+    return true;
+}
+
+tp_status scan_cells(tp_handle* h, int* count, int* start, int* cursor) {
+    const int n = h->grid.ncells;
+    const int nb = nblk(n, kScanTile);
+    k_scan_reduce<<<nb, kScanThreads, 0, h->stream>>>(count, n, h->scan_partial);
+    k_scan_partials<<<1, kScanThreads, 0, h->stream>>>(h->scan_partial, nb);
+    k_scan_final<<<nb, kScanThreads, 0, h->stream>>>(count, n, h->scan_partial, start, cursor);
+    TP_LAUNCHED(h, "cell scan");
+    h->launches += 3;
+    return TP_OK;
+}
+
+// Counting sort of `n` particles with coordinates `u` into key/tmp/start (no packing yet).
+tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start) {
+    if (n > 0) {
+        if (h->cfg.ndims == 2)
+            k_cell_keys<2><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
+                                                                 h->d_err);
+        else
+            k_cell_keys<3><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
+                                                                 h->d_err);
+        TP_LAUNCHED(h, "cell keys");
+        h->launches += 1;
+    }
+    tp_status st = scan_cells(h, h->f_count, start, h->f_cursor);
+    if (st != TP_OK) return st;
+    if (n > 0) {
+        k_scatter<<<nblk(n, 256), 256, 0, h->stream>>>(key, n, h->f_cursor, tmp);
+        TP_LAUNCHED(h, "cell scatter");
+        h->launches += 1;
+    }
+    return TP_OK;
+}
+
+// Records the boundary `k` (0..kNumPhases) of the current RHS evaluation's phases.
+void mark(tp_handle* h, int k) {
+    if (!h->timing) return;
+    if (h->ev_used == h->evpool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            h->timing = false;
+            return;
+        }
+        h->evpool.push_back(e);
+    }
+    (void)k;
+    cudaEventRecord(h->evpool[h->ev_used++], h->stream);
+}
+
+void begin_timing(tp_handle* h) {
+    h->ev_used = 0;
+    for (int k = 0; k < kNumPhases; ++k) h->phase_ms[k] = 0.0;
+}
+
+// Sums the phase durations of every RHS evaluation recorded since begin_timing.
+void finish_timing(tp_handle* h) {
+    if (!h->timing || h->ev_used == 0) return;
+    cudaEventSynchronize(h->evpool[h->ev_used - 1]);
+    const size_t per = kNumPhases + 1;
+    for (size_t b = 0; b + per <= h->ev_used; b += per)
+        for (int k = 0; k < kNumPhases; ++k) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, h->evpool[b + k], h->evpool[b + k + 1]) == cudaSuccess)
+                h->phase_ms[k] += ms;
+        }
+}
+
+tp_status ensure_state(tp_handle* h) {
+    if (h->st[0].u) return TP_OK;
+    const size_t nf = (size_t)h->cfg.n_fluid;
+    const int nd = h->cfg.ndims;
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    for (int k = 0; k < 2; ++k) {
+        PhysState& s = h->st[k];
+        TP_CUDA(h, dalloc(&s.u, nf * nd));
+        TP_CUDA(h, dalloc(&s.tu, nf * nd));
+        if (f32) {
+            TP_CUDA(h, dalloc((float4**)&s.v, nf));
+            TP_CUDA(h, dalloc((float4**)&s.tv, nf));
+            TP_CUDA(h, dalloc((float**)&s.m, nf));
+        } else {
+            TP_CUDA(h, dalloc((double**)&s.v, nf * (nd + 1)));
+            TP_CUDA(h, dalloc((double**)&s.tv, nf * (nd + 1)));
+            TP_CUDA(h, dalloc((double**)&s.m, nf));
+        }
+        TP_CUDA(h, dalloc(&s.id, nf));
+    }
+    return TP_OK;
+}
+
+// One RHS evaluation of the cell-sorted pipeline from caller-ordered device arrays.
+tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
+    const int nf = (int)h->cfg.n_fluid;
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    mark(h, 0);
+    tp_status st = sort_particles(h, u, nf, h->f_key, h->f_tmp, h->f_start);
+    if (st != TP_OK) return st;
+    if (f32)
+        fp32_pack(h, u, v, h->m_f, nullptr, nullptr);
+    else if (nf > 0)
+        fp64_pack(h, u, v, h->m_f, nullptr, nullptr);
+    TP_LAUNCHED(h, "pack");
+    h->launches += (nf > 0);
+    mark(h, 1);
+    if (f32)
+        fp32_adami(h);
+    else
+        fp64_adami(h);
+    TP_LAUNCHED(h, "adami");
+    h->launches += (h->cfg.n_wall > 0);
+    mark(h, 2);
+    return TP_OK;
+}
+
+}  // namespace
+
+// =========================================================================================
+// C ABI
+// =========================================================================================
+extern "C" {
+
+int32_t tp_abi_version(void) { return TP_ABI_VERSION; }
+
+void tp_config_default(tp_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->ndims = 3;
+    c->precision = TP_PRECISION_FP64;
+    c->reference_density = 1000.0;
+    c->exponent = 7.0;
+    c->viscosity_model = TP_VISCOSITY_MONAGHAN;
+    c->viscosity_alpha = 0.02;
+    c->viscosity_beta = 0.0;
+    c->viscosity_epsilon = 0.01;
+    c->density_diffusion_model = TP_DIFFUSION_MOLTENI_COLAGROSSI;
+    c->density_diffusion_delta = 0.1;
+}
+
+tp_status tp_create(const tp_config* cfg, tp_handle** out) {
+    if (!out) {
+        g_create_error = "null output handle pointer";
+        return TP_ERR_ARGUMENT;
+    }
+    *out = nullptr;
+    std::string msg;
+    tp_status st = check_config(cfg, msg);
+    if (st != TP_OK) {
+        g_create_error = msg;
+        return st;
+    }
+    tp_handle* h = new (std::nothrow) tp_handle();
+    if (!h) {
+        g_create_error = "out of host memory";
+        return TP_ERR_CUDA;
+    }
+    h->cfg = *cfg;
+    if (!setup_grid(h, msg)) {
+        g_create_error = msg;
+        delete h;
+        return TP_ERR_ARGUMENT;
+    }
+    setup_phys(h);
+    const size_t nf = (size_t)cfg->n_fluid, nw = (size_t)cfg->n_wall;
+    const size_t nc = (size_t)h->grid.ncells;
+    h->scan_blocks = nblk((long)nc, kScanTile);
+    cudaError_t e = cudaSuccess;
+    auto A = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+    };
+    A(dalloc(&h->f_key, nf));
+    A(dalloc(&h->f_tmp, nf));
+    A(dalloc(&h->f_perm, nf));
+    A(dalloc(&h->f_skey, nf));
+    A(dalloc(&h->f_count, nc));
+    A(dalloc(&h->f_start, nc + 1));
+    A(dalloc(&h->f_cursor, nc));
+    A(dalloc(&h->scan_partial, (size_t)h->scan_blocks));
+    A(dalloc((double4_32a**)&h->f_pos, nf));
+    A(dalloc((double4_32a**)&h->f_vel, nf));
+    A(dalloc((double**)&h->f_mass, nf));
+    A(dalloc(&h->m_f, nf));
+    A(dalloc(&h->w_key, nw));
+    A(dalloc(&h->w_tmp, nw));
+    A(dalloc(&h->w_perm, nw));
+    A(dalloc(&h->w_skey, nw));
+    A(dalloc(&h->w_start, nc + 1));
+    A(dalloc((double4_32a**)&h->w_pos, nw));
+    A(dalloc((double4_32a**)&h->w_pos64, nw));
+    A(dalloc((double2**)&h->w_state, nw));
+    A(dalloc(&h->w_vol, nw));
+    h->red_blocks = 256;
+    A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
+    A(dalloc(&h->d_err, 1));
+    A(cudaMallocHost((void**)&h->h_err, sizeof(int)));
+    if (e == cudaSuccess) e = cudaMemset(h->f_count, 0, nc * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->w_start, 0, (nc + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        g_create_error = std::string("device allocation failed: ") + cudaGetErrorString(e);
+        tp_destroy(h);
+        return TP_ERR_CUDA;
+    }
+    *out = h;
+    return TP_OK;
+}
+
+tp_status tp_destroy(tp_handle* h) {
+    if (!h) return TP_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void* ptrs[] = {h->f_key,  h->f_tmp,     h->f_perm,   h->f_skey,   h->f_count, h->f_start,
+                    h->f_cursor, h->scan_partial, h->f_pos, h->f_vel,  h->f_mass,  h->m_f,
+                    h->w_key,  h->w_tmp,     h->w_perm,   h->w_skey,   h->w_start, h->w_pos,
+                    h->w_pos64, h->w_state,  h->w_vol,    h->red_partial, h->d_err};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (int k = 0; k < 2; ++k) {
+        PhysState& s = h->st[k];
+        void* q[] = {s.u, s.tu, s.v, s.tv, s.m, s.id};
+        for (void* p : q)
+            if (p) cudaFree(p);
+    }
+    if (h->h_err) cudaFreeHost(h->h_err);
+    for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
+    delete h;
+    return TP_OK;
+}
+
+tp_status tp_set_stream(tp_handle* h, void* stream) {
+    if (!h) return TP_ERR_ARGUMENT;
+    h->stream = (cudaStream_t)stream;
+    return TP_OK;
+}
+
+tp_status tp_set_wall(tp_handle* h, const double* x_wall, const double* m_wall) {
+    if (!h) return TP_ERR_ARGUMENT;
+    const int nw = (int)h->cfg.n_wall;
+    if (nw > 0 && (!x_wall || !m_wall))
+        return fail(h, TP_ERR_ARGUMENT, "tp_set_wall: null coordinates or masses");
+    tp_status st = sort_particles(h, x_wall, nw, h->w_key, h->w_tmp, h->w_start);
+    if (st != TP_OK) return st;
+    if (nw > 0) {
+        fp64_pack_wall(h, x_wall, m_wall, h->w_pos64);
+        if (h->cfg.precision == TP_PRECISION_FP32)
+            fp32_pack_wall(h, x_wall, m_wall);
+        else
+            fp64_pack_wall(h, x_wall, m_wall, h->w_pos);
+        TP_LAUNCHED(h, "wall pack");
+    }
+    // A wall particle outside the grid is a configuration error: report it now.
+    TP_CUDA(h, cudaMemcpyAsync(h->h_err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TP_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (*h->h_err) {
+        const int bits = *h->h_err;
+        *h->h_err = 0;
+        TP_CUDA(h, cudaMemset(h->d_err, 0, sizeof(int)));
+        return fail(h, (bits & TP_ERRBIT_NONFINITE) ? TP_ERR_NONFINITE : TP_ERR_OUT_OF_GRID,
+                    "tp_set_wall: a wall particle lies outside the FullGridCellList bounds");
+    }
+    h->wall_set = true;
+    return TP_OK;
+}
+
+tp_status tp_set_fluid_mass(tp_handle* h, const double* m_fluid) {
+    if (!h) return TP_ERR_ARGUMENT;
+    const size_t nf = (size_t)h->cfg.n_fluid;
+    if (nf > 0 && !m_fluid) return fail(h, TP_ERR_ARGUMENT, "tp_set_fluid_mass: null masses");
+    if (nf > 0)
+        TP_CUDA(h, cudaMemcpyAsync(h->m_f, m_fluid, nf * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   h->stream));
+    h->mass_set = true;
+    return TP_OK;
+}
+
+static tp_status ready(tp_handle* h) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (!h->wall_set || !h->mass_set)
+        return fail(h, TP_ERR_NOT_READY, "wall geometry (tp_set_wall) and fluid masses "
+                                         "(tp_set_fluid_mass) must be set first");
+    return TP_OK;
+}
+
+tp_status tp_kick(tp_handle* h, double* dv_ode, const double* v_ode, const double* u_ode,
+                  double t) {
+    (void)t;
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    const int nf = (int)h->cfg.n_fluid;
+    if (nf > 0 && (!dv_ode || !v_ode || !u_ode))
+        return fail(h, TP_ERR_ARGUMENT, "tp_kick: null array");
+    if (nf > 0 && (dv_ode == v_ode || (const double*)dv_ode == u_ode))
+        return fail(h, TP_ERR_ARGUMENT, "tp_kick: dv_ode must not alias v_ode or u_ode");
+    begin_timing(h);
+    st = rhs_from_caller(h, u_ode, v_ode);
+    if (st != TP_OK) return st;
+    if (h->cfg.precision == TP_PRECISION_FP32)
+        fp32_pair_kick(h, dv_ode);
+    else
+        fp64_pair_kick(h, dv_ode);
+    TP_LAUNCHED(h, "pair");
+    h->launches += (nf > 0);
+    mark(h, 3);
+    finish_timing(h);
+    return TP_OK;
+}
+
+tp_status tp_drift(tp_handle* h, double* du_ode, const double* v_ode, const double* u_ode,
+                   double t) {
+    (void)u_ode;
+    (void)t;
+    if (!h) return TP_ERR_ARGUMENT;
+    const int nf = (int)h->cfg.n_fluid;
+    if (nf == 0) return TP_OK;
+    if (!du_ode || !v_ode) return fail(h, TP_ERR_ARGUMENT, "tp_drift: null array");
+    if (h->cfg.ndims == 2)
+        k_drift<2><<<nblk(nf, 256), 256, 0, h->stream>>>(du_ode, v_ode, nf);
+    else
+        k_drift<3><<<nblk(nf, 256), 256, 0, h->stream>>>(du_ode, v_ode, nf);
+    TP_LAUNCHED(h, "drift");
+    return TP_OK;
+}
+
+tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double t0, double dt,
+                              int64_t n_steps) {
+    (void)t0;
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    if (n_steps < 0 || !std::isfinite(dt))
+        return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: bad step count or dt");
+    const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
+    if (nf == 0 || n_steps == 0) return TP_OK;
+    if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: null array");
+    st = ensure_state(h);
+    if (st != TP_OK) return st;
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    begin_timing(h);
+
+    // Load the caller state into slot-ordered storage (identity order to begin with).
+    PhysState& s0 = h->st[h->cur];
+    TP_CUDA(h, cudaMemcpyAsync(s0.u, u_ode, (size_t)nf * nd * sizeof(double),
+                               cudaMemcpyDeviceToDevice, h->stream));
+    if (f32) {
+        if (nd == 2)
+            k_load32<2><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, h->m_f,
+                                                              h->cfg.reference_density,
+                                                              (float4*)s0.v, (float*)s0.m, nf);
+        else
+            k_load32<3><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, h->m_f,
+                                                              h->cfg.reference_density,
+                                                              (float4*)s0.v, (float*)s0.m, nf);
+    } else {
+        TP_CUDA(h, cudaMemcpyAsync(s0.v, v_ode, (size_t)nf * (nd + 1) * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+        TP_CUDA(h, cudaMemcpyAsync(s0.m, h->m_f, (size_t)nf * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+    }
+    k_iota<<<nblk(nf, 256), 256, 0, h->stream>>>(s0.id, nf);
+    TP_LAUNCHED(h, "integrator load");
+    h->launches += f32 ? 2 : 1;
+
+    for (int64_t step = 0; step < n_steps; ++step) {
+        for (int stage = 0; stage < 5; ++stage) {
+            PhysState& src = h->st[h->cur];
+            PhysState& dst = h->st[1 - h->cur];
+            mark(h, 0);
+            st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start);
+            if (st != TP_OK) return st;
+            if (f32)
+                fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst);
+            else
+                fp64_pack(h, src.u, (const double*)src.v, (const double*)src.m, &src, &dst);
+            TP_LAUNCHED(h, "pack");
+            mark(h, 1);
+            if (f32)
+                fp32_adami(h);
+            else
+                fp64_adami(h);
+            TP_LAUNCHED(h, "adami");
+            mark(h, 2);
+            if (f32)
+                fp32_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
+            else
+                fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
+            TP_LAUNCHED(h, "pair stage");
+            mark(h, 3);
+            h->launches += 2 + (h->cfg.n_wall > 0);
+            h->cur = 1 - h->cur;
+        }
+    }
+
+    PhysState& sf = h->st[h->cur];
+    const double rho0 = h->cfg.reference_density;
+    if (nd == 2) {
+        if (f32)
+            k_store<2, true><<<nblk(nf, 256), 256, 0, h->stream>>>(sf.u, sf.v, sf.id, rho0, u_ode,
+                                                                    v_ode, nf);
+        else
+            k_store<2, false><<<nblk(nf, 256), 256, 0, h->stream>>>(sf.u, sf.v, sf.id, rho0,
+                                                                     u_ode, v_ode, nf);
+    } else {
+        if (f32)
+            k_store<3, true><<<nblk(nf, 256), 256, 0, h->stream>>>(sf.u, sf.v, sf.id, rho0, u_ode,
+                                                                    v_ode, nf);
+        else
+            k_store<3, false><<<nblk(nf, 256), 256, 0, h->stream>>>(sf.u, sf.v, sf.id, rho0,
+                                                                     u_ode, v_ode, nf);
+    }
+    TP_LAUNCHED(h, "integrator store");
+    h->launches += 1;
+    finish_timing(h);
+    return TP_OK;
+}
+
+tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid) {
+    if (!h) return TP_ERR_ARGUMENT;
+    const int nf = (int)h->cfg.n_fluid;
+    if (nf == 0) return TP_OK;
+    if (!p_fluid) return fail(h, TP_ERR_ARGUMENT, "tp_fluid_pressure: null array");
+    if (h->cfg.precision == TP_PRECISION_FP32)
+        k_scatter_pressure<true><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, h->f_perm,
+                                                                        p_fluid, nf);
+    else
+        k_scatter_pressure<false><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, h->f_perm,
+                                                                         p_fluid, nf);
+    TP_LAUNCHED(h, "fluid pressure");
+    return TP_OK;
+}
+
+tp_status tp_wall_state(tp_handle* h, double* p_wall, double* rho_wall, double* volume_wall) {
+    if (!h) return TP_ERR_ARGUMENT;
+    const int nw = (int)h->cfg.n_wall;
+    if (nw == 0) return TP_OK;
+    const double rho0 = h->cfg.reference_density;
+    if (h->cfg.precision == TP_PRECISION_FP32)
+        k_scatter_wall<true><<<nblk(nw, 256), 256, 0, h->stream>>>(
+            h->w_state, h->w_vol, h->w_perm, rho0, p_wall, rho_wall, volume_wall, nw);
+    else
+        k_scatter_wall<false><<<nblk(nw, 256), 256, 0, h->stream>>>(
+            h->w_state, h->w_vol, h->w_perm, rho0, p_wall, rho_wall, volume_wall, nw);
+    TP_LAUNCHED(h, "wall state");
+    return TP_OK;
+}
+
+tp_status tp_nhs_debug(tp_handle* h, const double* u_ode, int32_t* cell, int32_t* order,
+                       int32_t* nnb_ff, int32_t* nnb_fw, int32_t* nnb_wf) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (!h->wall_set) return fail(h, TP_ERR_NOT_READY, "tp_nhs_debug: wall not set");
+    const int nf = (int)h->cfg.n_fluid;
+    if (nf > 0 && !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_nhs_debug: null coordinates");
+    tp_status st = sort_particles(h, u_ode, nf, h->f_key, h->f_tmp, h->f_start);
+    if (st != TP_OK) return st;
+    fp64_pack_pos(h, u_ode);
+    TP_LAUNCHED(h, "nhs pack");
+    if (cell && nf)
+        TP_CUDA(h, cudaMemcpyAsync(cell, h->f_key, (size_t)nf * sizeof(int),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+    if (order && nf)
+        TP_CUDA(h, cudaMemcpyAsync(order, h->f_perm, (size_t)nf * sizeof(int),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+    fp64_count(h, nnb_ff, nnb_fw, nnb_wf);
+    TP_LAUNCHED(h, "neighbour counts");
+    return TP_OK;
+}
+
+tp_status tp_grid_info(tp_handle* h, int32_t dims[3], double* cell_size, double lo[3]) {
+    if (!h) return TP_ERR_ARGUMENT;
+    for (int d = 0; d < 3; ++d) {
+        if (dims) dims[d] = h->grid.n[d];
+        if (lo) lo[d] = (double)h->grid.cmin[d] * h->grid.cs;
+    }
+    if (cell_size) *cell_size = h->grid.cs;
+    return TP_OK;
+}
+
+tp_status tp_conservation(tp_handle* h, const double* v_ode, double out[5]) {
+    if (!h || !out) return TP_ERR_ARGUMENT;
+    const int nf = (int)h->cfg.n_fluid;
+    for (int k = 0; k < 5; ++k) out[k] = 0.0;
+    if (nf == 0) return TP_OK;
+    if (!v_ode) return fail(h, TP_ERR_ARGUMENT, "tp_conservation: null array");
+    const int nb = h->red_blocks;
+    if (h->cfg.ndims == 2)
+        k_conservation<2><<<nb, 256, 0, h->stream>>>(v_ode, h->m_f, nf, h->red_partial);
+    else
+        k_conservation<3><<<nb, 256, 0, h->stream>>>(v_ode, h->m_f, nf, h->red_partial);
+    TP_LAUNCHED(h, "conservation");
+    std::vector<double> part((size_t)nb * 5);
+    TP_CUDA(h, cudaMemcpyAsync(part.data(), h->red_partial, part.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+    TP_CUDA(h, cudaStreamSynchronize(h->stream));
+    // Fixed summation order over the block partials: the result is deterministic.
+    for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < 5; ++k) out[k] += part[(size_t)b * 5 + k];
+    return TP_OK;
+}
+
+tp_status tp_sync(tp_handle* h) {
+    if (!h) return TP_ERR_ARGUMENT;
+    TP_CUDA(h, cudaMemcpyAsync(h->h_err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TP_CUDA(h, cudaStreamSynchronize(h->stream));
+    const int bits = *h->h_err;
+    if (bits) {
+        *h->h_err = 0;
+        TP_CUDA(h, cudaMemset(h->d_err, 0, sizeof(int)));
+        if (bits & TP_ERRBIT_NONFINITE)
+            return fail(h, TP_ERR_NONFINITE, "a particle coordinate became NaN or Inf");
+        return fail(h, TP_ERR_OUT_OF_GRID,
+                    "a particle left the FullGridCellList bounding box (its cell was clamped)");
+    }
+    return TP_OK;
+}
+
+int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n) {
+    if (!h) return 0;
+    for (int k = 0; k < n && k < kNumPhases; ++k) ms[k] = h->phase_ms[k];
+    return kNumPhases;
+}
+
+int64_t tp_kernel_launches(const tp_handle* h) { return h ? (int64_t)h->launches : 0; }
+
+tp_status tp_enable_timing(tp_handle* h, int32_t enable) {
+    if (!h) return TP_ERR_ARGUMENT;
+    h->timing = enable != 0;
+    return TP_OK;
+}
+
+const char* tp_last_error(const tp_handle* h) {
+    if (!h) return g_create_error.c_str();
+    return h->last_error.c_str();
+}
+
+}  // extern "C"

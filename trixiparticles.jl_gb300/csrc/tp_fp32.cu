@@ -1,0 +1,473 @@
+// tp_fp32.cu — FP32 precision form of the WCSPH right-hand side (sm_103a).
+//
+// Same passes and neighbour order as the FP64 drop-in, with these precision choices:
+//   * positions enter the pair arithmetic as FP32 offsets inside their cell,
+//     o = x - floor(x / cs) * cs32 (FP64 on input, rounded once to FP32), so a pair difference
+//     is (o_a - shift) - o_b with shift = (cell_b - cell_a) * cs32 and stays accurate to FP32
+//     relative precision of the smoothing length whatever the domain size;
+//   * density is stored as the deviation rho - rho0 in FP32, so differences of densities and
+//     the Cole EOS, evaluated as B * expm1(gamma * log1p((rho - rho0) / rho0)), do not cancel;
+//   * per-particle sums (dv, drho, Adami pressure and volume) use Kahan-compensated FP32;
+//   * `div_fast` divisions use __fdividef, the CUDA Float32 fast division the reference's
+//     Float32 GPU path compiles to;
+//   * positions and their Runge-Kutta register stay FP64 (the drift! accumulation); velocity
+//     and density registers are FP32.
+#include "tp_api_internal.h"
+#include "tp_nhs.cuh"
+
+namespace tp {
+
+struct Kahan {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ float eos32(float drho, const Phys32& P, int clip) {
+    float p = P.B * expm1f(P.gamma * log1pf(drho / P.rho0)) + P.p_bg;
+    if (clip) p = (p != p || p > 0.0f) ? p : 0.0f;
+    return p;
+}
+
+__device__ __forceinline__ float eos32_inverse_dev(float p, const Phys32& P) {
+    return P.rho0 * expm1f(log1pf((p - P.p_bg) / P.B) * P.inv_gamma);
+}
+
+template <int ND>
+__device__ __forceinline__ void cell_offsets(const double* x, double cs, double cs32, float o[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d < ND) {
+            const double fl = floor(__ddiv_rn(x[d], cs));
+            o[d] = (float)__dsub_rn(x[d], __dmul_rn(fl, cs32));
+        } else {
+            o[d] = 0.0f;
+        }
+    }
+}
+
+// Source state -> fluid record slot.  SRC32: the integrator's FP32 velocity/density state
+// (float4 {v, rho - rho0}) and FP32 masses; otherwise the caller's FP64 v_ode and masses.
+template <int ND, bool SRC32>
+struct Pack32 {
+    const double* u;
+    const void* v;
+    const void* m;
+    const double* tu;
+    const float4* tv;
+    const int* id_in;
+    double* u_out;  // integrator: FP64 positions moved to slot order
+    double* tu_out;
+    float4* tv_out;
+    int* id_out;
+    float4* pos;
+    float4* vel;
+    float* mass;
+    double cs, cs32, rho0;
+    Phys32 P;
+    __device__ void operator()(int i, int s) const {
+        double x[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
+        float o[3];
+        cell_offsets<ND>(x, cs, cs32, o);
+        float4 w;
+        float mi;
+        if (SRC32) {
+            w = ((const float4*)v)[i];
+            mi = ((const float*)m)[i];
+        } else {
+            const double* vv = (const double*)v + (size_t)i * (ND + 1);
+            w.x = (float)vv[0];
+            w.y = (float)vv[1];
+            w.z = (ND == 3) ? (float)vv[2] : 0.0f;
+            w.w = (float)(vv[ND] - rho0);
+            mi = (float)((const double*)m)[i];
+        }
+        const float p = eos32(w.w, P, P.fluid_clip);
+        pos[s] = make_float4(o[0], o[1], o[2], p);
+        vel[s] = w;
+        mass[s] = mi;
+        if (u_out) {
+#pragma unroll
+            for (int d = 0; d < ND; ++d) {
+                u_out[(size_t)s * ND + d] = x[d];
+                tu_out[(size_t)s * ND + d] = tu[(size_t)i * ND + d];
+            }
+            tv_out[s] = tv[i];
+            id_out[s] = id_in[i];
+        }
+    }
+};
+
+template <int ND>
+struct PackWall32 {
+    const double* x;
+    const double* m;
+    float4* pos;
+    double cs, cs32;
+    __device__ void operator()(int i, int s) const {
+        double y[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) y[d] = x[(size_t)i * ND + d];
+        float o[3];
+        cell_offsets<ND>(y, cs, cs32, o);
+        pos[s] = make_float4(o[0], o[1], o[2], (float)m[i]);
+    }
+};
+
+template <int ND>
+__global__ void __launch_bounds__(128) k_adami32(Phys32 P, GridDesc g, int nw,
+                                                 const float4* __restrict__ wpos,
+                                                 const int* __restrict__ wskey,
+                                                 float2* __restrict__ wstate,
+                                                 double* __restrict__ wvol,
+                                                 const float4* __restrict__ fpos,
+                                                 const float4* __restrict__ fvel,
+                                                 const int* __restrict__ fstart) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    const float4 xw = wpos[w];
+    int c[3];
+    key_to_coords(wskey[w], g, c);
+    Kahan Ps, V;
+    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            const float s1 = xw.y - (float)dy * P.cs, s2 = xw.z - (float)dz * P.cs;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const float s0 = xw.x - (float)dx * P.cs;
+                const int b1 = fstart[row + dx + 2];
+                for (int b = fstart[row + dx + 1]; b < b1; ++b) {
+                    const float4 xb = fpos[b];
+                    const float pd0 = s0 - xb.x, pd1 = s1 - xb.y;
+                    const float pd2 = (ND == 3) ? s2 - xb.z : 0.0f;
+                    float d2 = pd0 * pd0 + pd1 * pd1;
+                    if (ND == 3) d2 += pd2 * pd2;
+                    if (d2 > P.sr2) continue;
+                    const float r = sqrtf(d2);
+                    const float rho_f = P.rho0 + fvel[b].w;
+                    float hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
+                    if (ND == 3) hp += P.g[2] * (rho_f * pd2);
+                    const float sum = (P.p_off + xb.w) + hp;
+                    float W = 0.0f;
+                    if (r < P.two_h) {
+                        const float q = r * P.h_inv;
+                        const float t = 1.0f - 0.5f * q;
+                        const float t2 = t * t;
+                        W = (P.wc2_norm * (t2 * t2)) * (2.0f * q + 1.0f);
+                    }
+                    Ps.add(sum * W);
+                    V.add(W);
+                }
+            }
+        }
+    }
+    float pw = Ps.s - Ps.c;
+    const float vw = V.s - V.c;
+    if ((double)vw > 2.220446049250313e-16) pw = pw / vw;
+    if (P.wall_clip) pw = (pw != pw || pw > 0.0f) ? pw : 0.0f;
+    wstate[w] = make_float2(pw, eos32_inverse_dev(pw, P));
+    wvol[w] = (double)vw;
+}
+
+struct Update32 {
+    double* dv;       // kick: dv_ode (caller order, FP64) indexed by perm
+    const int* perm;
+    double g[3];
+    // integrator (slot order, in place on the state written by this stage's pack)
+    double* u;
+    double* tu;
+    float4* v_out;
+    float4* tv;
+    double A, B, dt;
+    float Af, Bf, dtf;
+    int first;
+};
+
+template <int ND, bool INTEGRATE>
+__global__ void __launch_bounds__(128) k_pair32(Phys32 P, GridDesc g, int nf,
+                                                const float4* __restrict__ fpos,
+                                                const float4* __restrict__ fvel,
+                                                const float* __restrict__ fmass,
+                                                const int* __restrict__ fstart,
+                                                const int* __restrict__ fskey,
+                                                const float4* __restrict__ wpos,
+                                                const float2* __restrict__ wstate,
+                                                const int* __restrict__ wstart, Update32 U) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const float4 pa = fpos[s];
+    const float4 va = fvel[s];
+    const float p_a = pa.w;
+    const float drho_a = va.w;
+    const float rho_a = P.rho0 + drho_a;
+    int c[3];
+    key_to_coords(fskey[s], g, c);
+    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+
+    Kahan a0, a1, a2, ar;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            const float s1 = pa.y - (float)dy * P.cs, s2 = pa.z - (float)dz * P.cs;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const float s0 = pa.x - (float)dx * P.cs;
+                const int b1 = fstart[row + dx + 2];
+                for (int b = fstart[row + dx + 1]; b < b1; ++b) {
+                    const float4 pb = fpos[b];
+                    const float pd0 = s0 - pb.x, pd1 = s1 - pb.y;
+                    const float pd2 = (ND == 3) ? s2 - pb.z : 0.0f;
+                    float d2 = pd0 * pd0 + pd1 * pd1;
+                    if (ND == 3) d2 += pd2 * pd2;
+                    if (d2 > P.sr2) continue;
+                    const float r = sqrtf(d2);
+                    if (r < P.almostzero) continue;
+                    const float4 vb = fvel[b];
+                    const float m_b = fmass[b];
+                    const float rho_b = P.rho0 + vb.w;
+                    const float q = r * P.h_inv;
+                    const float t = 1.0f - 0.5f * q;
+                    const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+                    const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+                    const float coef = -m_b * __fdividef(p_a + pb.w, rho_a * rho_b);
+                    float e0 = coef * g0, e1 = coef * g1, e2 = coef * g2;
+                    const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
+                    const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
+                    if (P.visc) {
+                        float vr = vd0 * pd0 + vd1 * pd1;
+                        if (ND == 3) vr += vd2 * pd2;
+                        if (vr < 0.0f) {
+                            const float rho_mean = 0.5f * (rho_a + rho_b);
+                            const float mu = __fdividef(P.visc_h * vr, r * r + P.visc_eps_h2);
+                            const float num = (m_b * P.visc_ac) * mu + (m_b * P.beta) * (mu * mu);
+                            const float f = __fdividef(num, rho_mean);
+                            e0 += f * g0;
+                            e1 += f * g1;
+                            e2 += f * g2;
+                        }
+                    }
+                    a0.add(e0);
+                    a1.add(e1);
+                    if (ND == 3) a2.add(e2);
+                    float vg = vd0 * g0 + vd1 * g1;
+                    if (ND == 3) vg += vd2 * g2;
+                    float er = (__fdividef(rho_a, rho_b) * m_b) * vg;
+                    if (P.diff) {
+                        const float vol_b = __fdividef(m_b, rho_b);
+                        const float pc = __fdividef(2.0f * (drho_a - vb.w), r * r);
+                        float pg = pd0 * g0 + pd1 * g1;
+                        if (ND == 3) pg += pd2 * g2;
+                        er += P.diff_coef * (vol_b * (pc * pg));
+                    }
+                    ar.add(er);
+                }
+            }
+        }
+    }
+
+    Kahan w0, w1, w2, wr;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            const float s1 = pa.y - (float)dy * P.cs, s2 = pa.z - (float)dz * P.cs;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const float s0 = pa.x - (float)dx * P.cs;
+                const int b1 = wstart[row + dx + 2];
+                for (int b = wstart[row + dx + 1]; b < b1; ++b) {
+                    const float4 pb = wpos[b];
+                    const float pd0 = s0 - pb.x, pd1 = s1 - pb.y;
+                    const float pd2 = (ND == 3) ? s2 - pb.z : 0.0f;
+                    float d2 = pd0 * pd0 + pd1 * pd1;
+                    if (ND == 3) d2 += pd2 * pd2;
+                    if (d2 > P.sr2) continue;
+                    const float r = sqrtf(d2);
+                    if (r < P.almostzero) continue;
+                    const float2 sb = wstate[b];
+                    const float m_b = pb.w, p_b = sb.x, rho_b = P.rho0 + sb.y;
+                    const float q = r * P.h_inv;
+                    const float t = 1.0f - 0.5f * q;
+                    const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+                    const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+                    const float coef = -m_b * __fdividef(p_a + p_b, rho_a * rho_b);
+                    w0.add(coef * g0);
+                    w1.add(coef * g1);
+                    if (ND == 3) w2.add(coef * g2);
+                    float vg = va.x * g0 + va.y * g1;
+                    if (ND == 3) vg += va.z * g2;
+                    wr.add((__fdividef(rho_a, rho_b) * m_b) * vg);
+                }
+            }
+        }
+    }
+
+    double k[4];
+    k[0] = (a0.value() + w0.value()) + U.g[0];
+    k[1] = (a1.value() + w1.value()) + U.g[1];
+    k[2] = (ND == 3) ? (a2.value() + w2.value()) + U.g[2] : 0.0;
+    k[ND] = ar.value() + wr.value();
+
+    if (!INTEGRATE) {
+        const int i = U.perm[s];
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
+    } else {
+        const float vin[4] = {va.x, va.y, va.z, va.w};
+        float kv[4] = {(float)k[0], (float)k[1], (float)k[2], 0.0f};
+        kv[ND] = (float)k[ND];
+        float4 tv = U.tv[s];
+        float tva[4] = {tv.x, tv.y, tv.z, tv.w};
+        float vout[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            const int src = (d == 3) ? ND : d;  // slot 3 of the float4 is the density
+            if (d < ND || d == 3) {
+                const float kk = (d == 3) ? kv[ND] : kv[d];
+                const float t = U.first ? U.dtf * kk : fmaf(U.dtf, kk, U.Af * tva[d]);
+                tva[d] = t;
+                vout[d] = fmaf(U.Bf, t, (d == 3) ? vin[3] : vin[src]);
+            }
+        }
+        U.tv[s] = make_float4(tva[0], tva[1], tva[2], tva[3]);
+        U.v_out[s] = make_float4(vout[0], vout[1], vout[2], vout[3]);
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double ku = (double)vin[d];
+            const double t = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
+            U.tu[(size_t)s * ND + d] = t;
+            U.u[(size_t)s * ND + d] = fma(U.B, t, U.u[(size_t)s * ND + d]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host launchers
+// ------------------------------------------------------------------------------------------
+namespace {
+inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
+}
+
+void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
+               const PhysState* src, PhysState* dst) {
+    const int n = (int)h->cfg.n_fluid;
+    if (n == 0) return;
+    const double cs = h->grid.cs, cs32 = (double)(float)h->grid.cs;
+    auto run = [&](auto ndc, auto srcc) {
+        constexpr int ND = decltype(ndc)::value;
+        constexpr bool S32 = decltype(srcc)::value;
+        Pack32<ND, S32> pk{};
+        pk.u = S32 ? src->u : u;
+        pk.v = S32 ? (const void*)src->v : (const void*)v;
+        pk.m = S32 ? (const void*)src->m : (const void*)m;
+        if (S32) {
+            pk.tu = src->tu;
+            pk.tv = (const float4*)src->tv;
+            pk.id_in = src->id;
+            pk.u_out = dst->u;
+            pk.tu_out = dst->tu;
+            pk.tv_out = (float4*)dst->tv;
+            pk.id_out = dst->id;
+            pk.mass = (float*)dst->m;
+        } else {
+            pk.mass = (float*)h->f_mass;
+        }
+        pk.pos = (float4*)h->f_pos;
+        pk.vel = (float4*)h->f_vel;
+        pk.cs = cs;
+        pk.cs32 = cs32;
+        pk.rho0 = h->cfg.reference_density;
+        pk.P = h->phys32;
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n,
+                                                          h->f_perm, h->f_skey, pk);
+    };
+    const bool s32 = src != nullptr;
+    if (h->cfg.ndims == 2) {
+        if (s32) run(std::integral_constant<int, 2>{}, std::true_type{});
+        else run(std::integral_constant<int, 2>{}, std::false_type{});
+    } else {
+        if (s32) run(std::integral_constant<int, 3>{}, std::true_type{});
+        else run(std::integral_constant<int, 3>{}, std::false_type{});
+    }
+}
+
+void fp32_pack_wall(tp_handle* h, const double* x, const double* m) {
+    const int n = (int)h->cfg.n_wall;
+    if (n == 0) return;
+    const double cs = h->grid.cs, cs32 = (double)(float)h->grid.cs;
+    if (h->cfg.ndims == 2) {
+        PackWall32<2> pk{x, m, (float4*)h->w_pos, cs, cs32};
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
+                                                          h->w_perm, h->w_skey, pk);
+    } else {
+        PackWall32<3> pk{x, m, (float4*)h->w_pos, cs, cs32};
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
+                                                          h->w_perm, h->w_skey, pk);
+    }
+}
+
+void fp32_adami(tp_handle* h) {
+    const int nw = (int)h->cfg.n_wall;
+    if (nw == 0) return;
+    if (h->cfg.ndims == 2)
+        k_adami32<2><<<nblk(nw, 128), 128, 0, h->stream>>>(
+            h->phys32, h->grid, nw, (const float4*)h->w_pos, h->w_skey, (float2*)h->w_state,
+            h->w_vol, (const float4*)h->f_pos, (const float4*)h->f_vel, h->f_start);
+    else
+        k_adami32<3><<<nblk(nw, 128), 128, 0, h->stream>>>(
+            h->phys32, h->grid, nw, (const float4*)h->w_pos, h->w_skey, (float2*)h->w_state,
+            h->w_vol, (const float4*)h->f_pos, (const float4*)h->f_vel, h->f_start);
+}
+
+template <int ND, bool INTEG>
+static void launch_pair32(tp_handle* h, const float* fmass, const Update32& U) {
+    const int nf = (int)h->cfg.n_fluid;
+    k_pair32<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
+        h->phys32, h->grid, nf, (const float4*)h->f_pos, (const float4*)h->f_vel, fmass,
+        h->f_start, h->f_skey, (const float4*)h->w_pos, (const float2*)h->w_state, h->w_start,
+        U);
+}
+
+void fp32_pair_kick(tp_handle* h, double* dv) {
+    if (h->cfg.n_fluid == 0) return;
+    Update32 U{};
+    U.dv = dv;
+    U.perm = h->f_perm;
+    for (int d = 0; d < 3; ++d) U.g[d] = h->cfg.acceleration[d];
+    if (h->cfg.ndims == 2)
+        launch_pair32<2, false>(h, (const float*)h->f_mass, U);
+    else
+        launch_pair32<3, false>(h, (const float*)h->f_mass, U);
+}
+
+void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first) {
+    if (h->cfg.n_fluid == 0) return;
+    Update32 U{};
+    U.perm = h->f_perm;
+    for (int d = 0; d < 3; ++d) U.g[d] = h->cfg.acceleration[d];
+    U.u = st.u;
+    U.tu = st.tu;
+    U.v_out = (float4*)st.v;
+    U.tv = (float4*)st.tv;
+    U.A = A;
+    U.B = B;
+    U.dt = dt;
+    U.Af = (float)A;
+    U.Bf = (float)B;
+    U.dtf = (float)dt;
+    U.first = first;
+    if (h->cfg.ndims == 2)
+        launch_pair32<2, true>(h, (const float*)st.m, U);
+    else
+        launch_pair32<3, true>(h, (const float*)st.m, U);
+}
+
+}  // namespace tp

@@ -1,0 +1,485 @@
+// tp_fp64.cu — plain FP64 drop-in form of the WCSPH right-hand side (sm_103a).
+//
+// Every quantity is Float64, as in the reference's Float64 GPU path.  Divisions the reference
+// writes as `div_fast` use its CUDA Float64 definition x * fast_inv(y)
+// (ext/TrixiParticlesCUDAExt.jl:12-32): approximate reciprocal `rcp.approx.ftz.f64` refined by
+// one cubic iteration e = 1 - a r; e = e + e^2; r = r + e r (the method the reference takes from
+// Oceananigans.jl PR 5140).  Plain `/` in the reference stays IEEE division here.
+// Squared distances use explicitly rounded products and sums (no FMA contraction) so that the
+// neighbour set {b : |x_a - x_b|^2 <= (2h)^2} is decided exactly as on the CPU.
+#include "tp_api_internal.h"
+#include "tp_nhs.cuh"
+
+namespace tp {
+
+__device__ __forceinline__ double fast_inv(double a) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(a));
+    double e = fma(r, -a, 1.0);
+    e = fma(e, e, e);
+    return fma(e, r, r);
+}
+
+__device__ __forceinline__ double div_fast(double x, double y) { return x * fast_inv(y); }
+
+template <int ND>
+__device__ __forceinline__ double dist2_rn(double p0, double p1, double p2) {
+    double d2 = __dadd_rn(__dmul_rn(p0, p0), __dmul_rn(p1, p1));
+    if (ND == 3) d2 = __dadd_rn(d2, __dmul_rn(p2, p2));
+    return d2;
+}
+
+// ------------------------------------------------------------------------------------------
+// Pack: source particle i -> fluid record slot s (EOS evaluated here: compute_pressure!,
+// weakly_compressible_sph/system.jl:426-438).
+// ------------------------------------------------------------------------------------------
+template <int ND>
+struct Pack64 {
+    const double* u;   // (ND, n) source order
+    const double* v;   // (ND+1, n)
+    const double* m;   // (n)
+    const double* tu;  // optional: integrator registers (source order), copied with the state
+    const double* tv;
+    const int* id_in;
+    double* tu_out;
+    double* tv_out;
+    int* id_out;
+    double4_32a* pos;
+    double4_32a* vel;
+    double* mass;
+    Phys P;
+    __device__ void operator()(int i, int s) const {
+        double x[3] = {0, 0, 0}, w[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) w[d] = v[(size_t)i * (ND + 1) + d];
+        const double rho = w[ND];
+        const double p = eos_pressure(rho, P, P.fluid_clip);
+        pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
+        vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
+        mass[s] = m[i];
+        if (tu_out) {
+#pragma unroll
+            for (int d = 0; d < ND; ++d) tu_out[(size_t)s * ND + d] = tu[(size_t)i * ND + d];
+#pragma unroll
+            for (int d = 0; d <= ND; ++d)
+                tv_out[(size_t)s * (ND + 1) + d] = tv[(size_t)i * (ND + 1) + d];
+            id_out[s] = id_in[i];
+        }
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// Adami pressure extrapolation (dummy_particles.jl:489-569, 586-606, 637-672), one thread per
+// wall slot, gathering its fluid neighbours in PointNeighbors order.
+// ------------------------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(128) k_adami64(Phys P, GridDesc g, int nw,
+                                                 const double4_32a* __restrict__ wpos,
+                                                 const int* __restrict__ wskey,
+                                                 double2* __restrict__ wstate,
+                                                 double* __restrict__ wvol,
+                                                 const double4_32a* __restrict__ fpos,
+                                                 const double4_32a* __restrict__ fvel,
+                                                 const int* __restrict__ fstart) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    const double4_32a xw = wpos[w];
+    int c[3];
+    key_to_coords(wskey[w], g, c);
+    double Ps = 0.0, V = 0.0;
+    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            const int b1 = fstart[row + 3];
+            for (int b = fstart[row]; b < b1; ++b) {
+                const double4_32a xb = fpos[b];
+                const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
+                const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
+                const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+                if (d2 > P.sr2) continue;
+                const double r = sqrt(d2);
+                const double rho_f = fvel[b].w;
+                double hp = __dadd_rn(__dmul_rn(P.g[0], __dmul_rn(rho_f, pd0)),
+                                      __dmul_rn(P.g[1], __dmul_rn(rho_f, pd1)));
+                if (ND == 3) hp = __dadd_rn(hp, __dmul_rn(P.g[2], __dmul_rn(rho_f, pd2)));
+                const double sum = ((P.p_off + xb.w) + 0.0) + hp;
+                double W = 0.0;
+                if (r < P.two_h) {
+                    const double q = r * P.h_inv;
+                    const double t = 1.0 - q / 2.0;
+                    const double t2 = t * t;
+                    W = (P.wc2_norm * (t2 * t2)) * (2.0 * q + 1.0);
+                }
+                Ps = __dadd_rn(Ps, __dmul_rn(sum, W));
+                V = __dadd_rn(V, W);
+            }
+        }
+    }
+    if (V > 2.220446049250313e-16) Ps = Ps / V;
+    if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
+    wstate[w] = make_double2(Ps, eos_inverse(Ps, P));
+    wvol[w] = V;
+}
+
+// ------------------------------------------------------------------------------------------
+// Fused fluid pair kernel: fluid-fluid then fluid-wall interactions of one fluid slot
+// (weakly_compressible_sph/rhs.jl:30-124), plus gravity (semidiscretization.jl:701-731), then
+// either the dv write (kick!) or the CarpenterKennedy2N54 register update of the slot.
+// ------------------------------------------------------------------------------------------
+struct Update64 {
+    double* dv;        // kick mode: dv_ode in source order (indexed by perm)
+    const int* perm;
+    // integrate mode (ping-pong in slot order):
+    const double* tu;  // registers of the slot (already moved to slot order by the pack)
+    const double* tv;
+    double* u_out;
+    double* v_out;
+    double* tu_out;
+    double* tv_out;
+    double A, B, dt;
+    int first;
+};
+
+template <int ND, bool INTEGRATE>
+__global__ void __launch_bounds__(128) k_pair64(Phys P, GridDesc g, int nf,
+                                                const double4_32a* __restrict__ fpos,
+                                                const double4_32a* __restrict__ fvel,
+                                                const double* __restrict__ fmass,
+                                                const int* __restrict__ fstart,
+                                                const int* __restrict__ fskey,
+                                                const double4_32a* __restrict__ wpos,
+                                                const double2* __restrict__ wstate,
+                                                const int* __restrict__ wstart, Update64 U) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const double4_32a pa = fpos[s];
+    const double4_32a va = fvel[s];
+    const double p_a = pa.w, rho_a = va.w;
+    int c[3];
+    key_to_coords(fskey[s], g, c);
+    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+
+    // ---- fluid-fluid ----
+    double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            const int b1 = fstart[row + 3];
+            for (int b = fstart[row]; b < b1; ++b) {
+                const double4_32a pb = fpos[b];
+                const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
+                const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
+                const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+                if (d2 > P.sr2) continue;
+                const double r = sqrt(d2);
+                if (r < P.almostzero) continue;
+                const double4_32a vb = fvel[b];
+                const double m_b = fmass[b];
+                const double rho_b = vb.w;
+                // WendlandC2 kernel_deriv_div_r_unsafe * pos_diff
+                const double q = r * P.h_inv;
+                const double t = 1.0 - q / 2.0;
+                const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+                const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+                // pressure_acceleration_continuity_density
+                const double coef = (-m_b) * div_fast(p_a + pb.w, rho_a * rho_b);
+                dv0 += coef * g0;
+                dv1 += coef * g1;
+                if (ND == 3) dv2 += coef * g2;
+                const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
+                const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
+                if (P.visc) {
+                    double vr = vd0 * pd0 + vd1 * pd1;
+                    if (ND == 3) vr += vd2 * pd2;
+                    if (vr < 0.0) {
+                        const double rho_mean = (rho_a + rho_b) / 2.0;
+                        const double mu = div_fast(P.visc_h * vr, r * r + P.visc_eps_h2);
+                        const double num =
+                            ((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu);
+                        const double f = div_fast(num, rho_mean);
+                        dv0 += f * g0;
+                        dv1 += f * g1;
+                        if (ND == 3) dv2 += f * g2;
+                    }
+                }
+                double vg = vd0 * g0 + vd1 * g1;
+                if (ND == 3) vg += vd2 * g2;
+                drho += (div_fast(rho_a, rho_b) * m_b) * vg;
+                if (P.diff) {
+                    const double vol_b = div_fast(m_b, rho_b);
+                    const double pc = div_fast(2.0 * (rho_a - rho_b), r * r);
+                    double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
+                    if (ND == 3) pg += (pc * pd2) * g2;
+                    drho += P.diff_coef * (vol_b * pg);
+                }
+            }
+        }
+    }
+
+    // ---- fluid-wall (wall viscosity = nothing, no density diffusion) ----
+    double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            const int b1 = wstart[row + 3];
+            for (int b = wstart[row]; b < b1; ++b) {
+                const double4_32a pb = wpos[b];
+                const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
+                const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
+                const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+                if (d2 > P.sr2) continue;
+                const double r = sqrt(d2);
+                if (r < P.almostzero) continue;
+                const double2 sb = wstate[b];
+                const double m_b = pb.w, p_b = sb.x, rho_b = sb.y;
+                const double q = r * P.h_inv;
+                const double t = 1.0 - q / 2.0;
+                const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+                const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+                const double coef = (-m_b) * div_fast(p_a + p_b, rho_a * rho_b);
+                ew0 += coef * g0;
+                ew1 += coef * g1;
+                if (ND == 3) ew2 += coef * g2;
+                double vg = va.x * g0 + va.y * g1;
+                if (ND == 3) vg += va.z * g2;
+                erho += (div_fast(rho_a, rho_b) * m_b) * vg;
+            }
+        }
+    }
+
+    // dv = ((0 + S_ff) + S_fw) + g ;  drho = S_ff + S_fw
+    double k[4];
+    k[0] = (dv0 + ew0) + P.g[0];
+    k[1] = (dv1 + ew1) + P.g[1];
+    k[2] = (ND == 3) ? (dv2 + ew2) + P.g[2] : 0.0;
+    k[ND] = drho + erho;
+
+    if (!INTEGRATE) {
+        const int i = U.perm[s];
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
+    } else {
+        // CarpenterKennedy2N54 stage: tmp = A*tmp + dt*k ; u = u + B*tmp (du = v at stage start)
+        const double va_arr[4] = {va.x, va.y, va.z, va.w};
+        const double xa_arr[3] = {pa.x, pa.y, pa.z};
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) {
+            const double kv = (d == ND) ? k[ND] : k[d];
+            double tv = U.first ? U.dt * kv : fma(U.dt, kv, U.A * U.tv[(size_t)s * (ND + 1) + d]);
+            U.tv_out[(size_t)s * (ND + 1) + d] = tv;
+            U.v_out[(size_t)s * (ND + 1) + d] = fma(U.B, tv, va_arr[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double ku = va_arr[d];
+            double tu = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
+            U.tu_out[(size_t)s * ND + d] = tu;
+            U.u_out[(size_t)s * ND + d] = fma(U.B, tu, xa_arr[d]);
+        }
+    }
+}
+
+// Neighbour counting (diagnostics): fluid-fluid, fluid-wall for fluid slots, or wall-fluid.
+template <int ND>
+__global__ void k_count64(GridDesc g, double sr2, int n, const double4_32a* __restrict__ qpos,
+                          const int* __restrict__ qskey, const int* __restrict__ qperm,
+                          const double4_32a* __restrict__ npos, const int* __restrict__ nstart,
+                          int* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double4_32a pa = qpos[s];
+    int c[3];
+    key_to_coords(qskey[s], g, c);
+    int cnt = 0;
+    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz)
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
+            for (int b = nstart[row]; b < nstart[row + 3]; ++b) {
+                const double4_32a pb = npos[b];
+                const double d2 = dist2_rn<ND>(pa.x - pb.x, pa.y - pb.y,
+                                               (ND == 3) ? pa.z - pb.z : 0.0);
+                cnt += (d2 <= sr2);
+            }
+        }
+    out[qperm[s]] = cnt;
+}
+
+// Wall record pack (setup): caller order -> slot order.
+template <int ND>
+struct PackWall64 {
+    const double* x;
+    const double* m;
+    double4_32a* pos;
+    __device__ void operator()(int i, int s) const {
+        double y[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) y[d] = x[(size_t)i * ND + d];
+        pos[s] = make_double4_32a(y[0], y[1], y[2], m[i]);
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// Host launchers
+// ------------------------------------------------------------------------------------------
+namespace {
+inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
+}
+
+template <int ND>
+static void pack_fluid64(tp_handle* h, const double* u, const double* v, const double* m,
+                         const PhysState* src, PhysState* dst) {
+    Pack64<ND> pk{};
+    pk.u = u;
+    pk.v = v;
+    pk.m = m;
+    if (src) {
+        pk.tu = src->tu;
+        pk.tv = (const double*)src->tv;
+        pk.id_in = src->id;
+        pk.tu_out = dst->tu;
+        pk.tv_out = (double*)dst->tv;
+        pk.id_out = dst->id;
+    }
+    pk.pos = (double4_32a*)h->f_pos;
+    pk.vel = (double4_32a*)h->f_vel;
+    // Integrator: the slot-ordered mass array of the next state doubles as the record mass.
+    pk.mass = dst ? (double*)dst->m : (double*)h->f_mass;
+    pk.P = h->phys;
+    const int n = (int)h->cfg.n_fluid;
+    k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n, h->f_perm,
+                                                      h->f_skey, pk);
+}
+
+void fp64_pack(tp_handle* h, const double* u, const double* v, const double* m,
+               const PhysState* src, PhysState* dst) {
+    if (h->cfg.ndims == 2)
+        pack_fluid64<2>(h, u, v, m, src, dst);
+    else
+        pack_fluid64<3>(h, u, v, m, src, dst);
+}
+
+// Positions only (p = 0): neighbour-count diagnostics.
+template <int ND>
+struct PackPos64 {
+    const double* u;
+    double4_32a* pos;
+    __device__ void operator()(int i, int s) const {
+        double x[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
+        pos[s] = make_double4_32a(x[0], x[1], x[2], 0.0);
+    }
+};
+
+void fp64_pack_pos(tp_handle* h, const double* u) {
+    const int n = (int)h->cfg.n_fluid;
+    if (n == 0) return;
+    if (h->cfg.ndims == 2) {
+        PackPos64<2> pk{u, (double4_32a*)h->f_pos};
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n,
+                                                          h->f_perm, h->f_skey, pk);
+    } else {
+        PackPos64<3> pk{u, (double4_32a*)h->f_pos};
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n,
+                                                          h->f_perm, h->f_skey, pk);
+    }
+}
+
+// Wall records: `out` is h->w_pos (FP64 form) or h->w_pos64 (diagnostic copy).
+void fp64_pack_wall(tp_handle* h, const double* x, const double* m, void* out) {
+    const int n = (int)h->cfg.n_wall;
+    if (n == 0) return;
+    if (h->cfg.ndims == 2) {
+        PackWall64<2> pk{x, m, (double4_32a*)out};
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
+                                                          h->w_perm, h->w_skey, pk);
+    } else {
+        PackWall64<3> pk{x, m, (double4_32a*)out};
+        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
+                                                          h->w_perm, h->w_skey, pk);
+    }
+}
+
+void fp64_adami(tp_handle* h) {
+    const int nw = (int)h->cfg.n_wall;
+    if (nw == 0) return;
+    if (h->cfg.ndims == 2)
+        k_adami64<2><<<nblk(nw, 128), 128, 0, h->stream>>>(
+            h->phys, h->grid, nw, (const double4_32a*)h->w_pos, h->w_skey, (double2*)h->w_state,
+            h->w_vol, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->f_start);
+    else
+        k_adami64<3><<<nblk(nw, 128), 128, 0, h->stream>>>(
+            h->phys, h->grid, nw, (const double4_32a*)h->w_pos, h->w_skey, (double2*)h->w_state,
+            h->w_vol, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->f_start);
+}
+
+template <int ND, bool INTEG>
+static void launch_pair64(tp_handle* h, const double* fmass, const Update64& U) {
+    const int nf = (int)h->cfg.n_fluid;
+    k_pair64<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
+        h->phys, h->grid, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, fmass,
+        h->f_start, h->f_skey, (const double4_32a*)h->w_pos, (const double2*)h->w_state,
+        h->w_start, U);
+}
+
+void fp64_pair_kick(tp_handle* h, double* dv) {
+    if (h->cfg.n_fluid == 0) return;
+    Update64 U{};
+    U.dv = dv;
+    U.perm = h->f_perm;
+    if (h->cfg.ndims == 2)
+        launch_pair64<2, false>(h, (const double*)h->f_mass, U);
+    else
+        launch_pair64<3, false>(h, (const double*)h->f_mass, U);
+}
+
+// Stage update in place on the slot-ordered state `st` written by the pack of this stage.
+void fp64_pair_stage(tp_handle* h, PhysState& out, double A, double B, double dt, int first) {
+    if (h->cfg.n_fluid == 0) return;
+    Update64 U{};
+    U.perm = h->f_perm;
+    U.tu = out.tu;
+    U.tv = (const double*)out.tv;
+    U.u_out = out.u;
+    U.v_out = (double*)out.v;
+    U.tu_out = out.tu;
+    U.tv_out = (double*)out.tv;
+    U.A = A;
+    U.B = B;
+    U.dt = dt;
+    U.first = first;
+    if (h->cfg.ndims == 2)
+        launch_pair64<2, true>(h, (const double*)out.m, U);
+    else
+        launch_pair64<3, true>(h, (const double*)out.m, U);
+}
+
+void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf) {
+    const int nf = (int)h->cfg.n_fluid, nw = (int)h->cfg.n_wall;
+    const double sr2 = h->phys.sr2;
+    auto run = [&](auto ndc) {
+        constexpr int ND = decltype(ndc)::value;
+        if (nnb_ff && nf)
+            k_count64<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
+                h->grid, sr2, nf, (const double4_32a*)h->f_pos, h->f_skey, h->f_perm,
+                (const double4_32a*)h->f_pos, h->f_start, nnb_ff);
+        if (nnb_fw && nf)
+            k_count64<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
+                h->grid, sr2, nf, (const double4_32a*)h->f_pos, h->f_skey, h->f_perm,
+                (const double4_32a*)h->w_pos64, h->w_start, nnb_fw);
+        if (nnb_wf && nw)
+            k_count64<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
+                h->grid, sr2, nw, (const double4_32a*)h->w_pos64, h->w_skey, h->w_perm,
+                (const double4_32a*)h->f_pos, h->f_start, nnb_wf);
+    };
+    if (h->cfg.ndims == 2)
+        run(std::integral_constant<int, 2>{});
+    else
+        run(std::integral_constant<int, 3>{});
+}
+
+}  // namespace tp

@@ -1,0 +1,92 @@
+// tp_handle.h — host-side handle of the WCSPH library (C ABI object behind tp_handle*).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "tp_internal.cuh"
+
+namespace tp {
+
+// Timed phases of one RHS evaluation (labels of the reference's TimerOutputs sections):
+//   0 "update nhs" (cell keys, scan, scatter, rank + pack incl. the fluid EOS),
+//   1 "compute boundary pressure" (Adami), 2 "system interaction" (pair kernel + fused update).
+constexpr int kNumPhases = 3;
+
+// Per-particle physical state of the integrator, one copy of a ping-pong pair.  Slot order
+// (the cell-sorted order of the previous stage).  FP64 form: u/tu = (nd, n) doubles,
+// v/tv = (nd+1, n) doubles.  FP32 form: u/tu doubles as above, v/tv = float4 per particle
+// {vx, vy, vz, rho - rho0}.
+struct PhysState {
+    double* u = nullptr;
+    double* tu = nullptr;
+    void* v = nullptr;
+    void* tv = nullptr;
+    void* m = nullptr;  // double (FP64) or float (FP32)
+    int* id = nullptr;  // original (caller) index of the particle in this slot
+};
+
+}  // namespace tp
+
+struct tp_handle {
+    tp_config cfg{};
+    tp::GridDesc grid{};
+    tp::Phys phys{};
+    tp::Phys32 phys32{};
+    cudaStream_t stream = nullptr;
+    bool wall_set = false;
+    bool mass_set = false;
+    bool timing = false;
+    std::string last_error;
+
+    // ---- fluid neighbour search (n_fluid entries unless noted) ----
+    int* f_key = nullptr;     // cell key of particle i (source order)
+    int* f_tmp = nullptr;     // atomic scatter order
+    int* f_perm = nullptr;    // slot -> source index
+    int* f_skey = nullptr;    // slot -> cell key
+    int* f_count = nullptr;   // ncells, kept zero between uses
+    int* f_start = nullptr;   // ncells + 1
+    int* f_cursor = nullptr;  // ncells
+    int* scan_partial = nullptr;
+    int scan_blocks = 0;
+
+    // ---- fluid records (slot order) ----
+    void* f_pos = nullptr;   // double4 / float4
+    void* f_vel = nullptr;   // double4 / float4
+    void* f_mass = nullptr;  // double / float
+
+    // ---- fluid masses in caller order (FP64) ----
+    double* m_f = nullptr;
+
+    // ---- wall (static, slot order) ----
+    int* w_key = nullptr;
+    int* w_tmp = nullptr;
+    int* w_perm = nullptr;   // slot -> caller index
+    int* w_skey = nullptr;
+    int* w_start = nullptr;  // ncells + 1
+    void* w_pos = nullptr;   // double4 / float4 {x.., m}
+    void* w_pos64 = nullptr; // double4 {x, y, z, m} (diagnostics in both forms)
+    void* w_state = nullptr; // double2 / float2 {p, rho}
+    double* w_vol = nullptr;
+
+    // ---- integrator ping-pong state ----
+    tp::PhysState st[2];
+    int cur = 0;
+
+    // ---- conservation reduction scratch ----
+    double* red_partial = nullptr;
+    int red_blocks = 0;
+
+    // ---- device error word ----
+    int* d_err = nullptr;
+    int* h_err = nullptr;  // pinned
+
+    // Phase timing: kNumPhases + 1 events per RHS evaluation from a pool, read back once at
+    // the end of the call (no synchronisation inside the stage loop).
+    std::vector<cudaEvent_t> evpool;
+    size_t ev_used = 0;
+    double phase_ms[tp::kNumPhases] = {};
+    long long launches = 0;  // kernel launches issued on this handle
+};

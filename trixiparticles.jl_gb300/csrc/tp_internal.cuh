@@ -1,0 +1,128 @@
+// tp_internal.cuh — shared device-side definitions of the sm_103a WCSPH library.
+//
+// Data layout in HBM (all particle arrays are cell-sorted "slots" unless noted):
+//   fluid records, rebuilt once per RHS evaluation by the pack pass of the neighbour search:
+//     FP64 form:  fpos[s] = double4_32a {x, y, z, p}      fvel[s] = double4_32a {vx, vy, vz, rho}
+//                 fmass[s] = double m
+//     FP32 form:  fpos[s] = float4  {ox, oy, oz, p}   (ox.. = offset inside the cell, metres)
+//                 fvel[s] = float4  {vx, vy, vz, rho - rho0}
+//                 fmass[s] = float m
+//   wall records, sorted once (walls are static), pressure/density rewritten by the Adami pass:
+//     FP64:  wpos[s] = double4_32a {x, y, z, m}   wstate[s] = double2 {p, rho}
+//     FP32:  wpos[s] = float4  {ox, oy, oz, m} wstate[s] = float2 {p, rho - rho0}
+//   cell list: start[c] = first slot of cell c (ncells + 1 entries), cells linearised x fastest,
+//   so the three cells (cx-1, cx, cx+1) of one (cy, cz) row are one contiguous slot range.
+// In 2D the z components are unused.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tp_wcsph.h"
+
+#define TP_ERRBIT_OUT_OF_GRID 1
+#define TP_ERRBIT_NONFINITE 2
+
+namespace tp {
+
+// Padded cell grid: cell coordinate along d is floor(x_d / cs) - cmin[d]; valid particle cells
+// are 1..n[d]-2 (one padding layer each side), so every 3^d neighbourhood is inside the grid.
+struct GridDesc {
+    int nd;
+    double cs;
+    int cmin[3];
+    int n[3];
+    int ncells;
+};
+
+// Physical parameters, precomputed on the host in FP64 following the reference expressions.
+struct Phys {
+    int nd;
+    double h;          // smoothing length
+    double h_inv;      // 1 / h
+    double sr2;        // (2h)^2, neighbour criterion d2 <= sr2
+    double two_h;      // compact support 2h (kernel() cut, strict <)
+    double almostzero; // sqrt(eps((2h)^2)), rhs.jl:27-28
+    double wc2_norm;   // WendlandC2 normalisation sigma_d * h_inv^d (smoothing_kernels.jl:450-455)
+    double wc2_dnorm;  // -5 * wc2_norm (kernel_deriv_div_r_unsafe prefactor)
+    double hi2;        // h_inv * h_inv
+    double rho0, c, gamma, p_bg, B, inv_gamma;
+    int fluid_clip, wall_clip;
+    int visc;
+    double alpha, beta, eps_visc;
+    double visc_h;     // (h + h) / 2
+    double visc_eps_h2;  // eps * (visc_h * visc_h)
+    double visc_mac;   // alpha * c  (used as ((m_b*alpha)*c) in FP64 order)
+    int diff;
+    double delta;
+    double diff_coef;  // (delta * ((h + h) / 2)) * c
+    double g[3];
+    double p_off;
+};
+
+// FP32 copies of the constants used by the precision form.
+struct Phys32 {
+    float cs;          // cell size rounded to FP32 (offsets are taken against it)
+    float h_inv, sr2, two_h, almostzero, wc2_norm, wc2_dnorm, hi2;
+    float rho0, B, gamma, inv_gamma, p_bg;
+    int fluid_clip, wall_clip, visc, diff;
+    float beta, visc_h, visc_eps_h2, visc_ac, diff_coef;
+    float g[3];
+    float p_off;
+};
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Cell coordinates of x (FP64).  Returns an error bit (0 = inside the inner grid); the coordinate
+// is clamped into the inner grid so that later passes never index outside the arrays.
+template <int ND>
+__device__ __forceinline__ int cell_coords(const double* x, const GridDesc& g, int c[3]) {
+    int err = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d < ND) {
+            double q = __ddiv_rn(x[d], g.cs);
+            double gd = floor(q) - (double)g.cmin[d];
+            if (!(gd >= 1.0 && gd <= (double)(g.n[d] - 2))) {
+                err |= (x[d] != x[d] || isinf(x[d])) ? TP_ERRBIT_NONFINITE : TP_ERRBIT_OUT_OF_GRID;
+                gd = (gd != gd) ? 1.0 : fmin(fmax(gd, 1.0), (double)(g.n[d] - 2));
+            }
+            c[d] = (int)gd;
+        } else {
+            c[d] = 0;
+        }
+    }
+    return err;
+}
+
+__device__ __forceinline__ int cell_key(const int c[3], const GridDesc& g) {
+    return c[0] + g.n[0] * (c[1] + g.n[1] * c[2]);
+}
+
+__device__ __forceinline__ void key_to_coords(int key, const GridDesc& g, int c[3]) {
+    c[0] = key % g.n[0];
+    int r = key / g.n[0];
+    c[1] = r % g.n[1];
+    c[2] = r / g.n[1];
+}
+
+// StateEquationCole pressure (state_equations.jl:117-129), FP64.
+__device__ __forceinline__ double eos_pressure(double rho, const Phys& P, int clip) {
+    double p = P.B * (pow(rho / P.rho0, P.gamma) - 1.0) + P.p_bg;
+    if (clip) p = (p != p || p > 0.0) ? p : 0.0;
+    return p;
+}
+
+// inverse_state_equation (state_equations.jl:131-139), FP64.
+__device__ __forceinline__ double eos_inverse(double p, const Phys& P) {
+    double tmp = (p - P.p_bg) / P.B + 1.0;
+    return P.rho0 * pow(tmp, P.inv_gamma);
+}
+
+}  // namespace tp

@@ -1,0 +1,429 @@
+"""Host-side mirror of the reference's WCSPH drop-in surface for the GB300 backend.
+
+Names, argument meanings and errors follow the reference:
+    Semidiscretization(fluid_system, boundary_system; neighborhood_search, parallelization_backend)
+        src/general/semidiscretization.jl:106-155
+    semidiscretize(semi, tspan)            src/general/semidiscretization.jl:293-396
+    kick!(dv_ode, v_ode, u_ode, p, t)      src/general/semidiscretization.jl:589-612  -> `kick`
+    drift!(du_ode, v_ode, u_ode, p, t)     src/general/semidiscretization.jl:522-536  -> `drift`
+    solve(ode, CarpenterKennedy2N54(williamson_condition=false); dt)  (OrdinaryDiffEq)
+The ODE state vectors are CUDA float64 tensors (PyTorch provides device memory and streams only);
+every computation runs in libtp_wcsph.so through its C ABI.  Unsupported system combinations
+raise ValueError, as the reference raises ArgumentError (docs/src/development.md:96).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .setups import InitialCondition, StateEquationCole
+
+
+# ------------------------------------------------------------------------------------------
+# Model tags (constructor keywords as in the reference)
+# ------------------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class WendlandC2Kernel:
+    ndims: int
+
+
+@dataclass(frozen=True)
+class ContinuityDensity:
+    pass
+
+
+@dataclass(frozen=True)
+class ArtificialViscosityMonaghan:
+    alpha: float
+    beta: float = 0.0
+    epsilon: float = 0.01
+
+
+@dataclass(frozen=True)
+class DensityDiffusionMolteniColagrossi:
+    delta: float
+
+
+@dataclass(frozen=True)
+class AdamiPressureExtrapolation:
+    pressure_offset: float = 0.0
+    allow_loop_flipping: bool = True
+
+
+@dataclass
+class BoundaryModelDummyParticles:
+    initial_density: np.ndarray
+    hydrodynamic_mass: np.ndarray
+    density_calculator: object
+    smoothing_kernel: WendlandC2Kernel
+    smoothing_length: float
+    viscosity: object = None
+    state_equation: StateEquationCole | None = None
+    correction: object = None
+    clip_negative_pressure: bool = False
+
+
+@dataclass
+class WeaklyCompressibleSPHSystem:
+    initial_condition: InitialCondition
+    smoothing_kernel: WendlandC2Kernel
+    smoothing_length: float
+    density_calculator: object
+    state_equation: StateEquationCole
+    acceleration: tuple | None = None
+    viscosity: object = None
+    density_diffusion: object = None
+    correction: object = None
+    surface_tension: object = None
+    shifting_technique: object = None
+
+    @property
+    def ndims(self) -> int:
+        return self.initial_condition.ndims
+
+
+@dataclass
+class WallBoundarySystem:
+    initial_condition: InitialCondition
+    boundary_model: BoundaryModelDummyParticles
+    prescribed_motion: object = None
+
+
+@dataclass
+class FullGridCellList:
+    min_corner: tuple
+    max_corner: tuple
+
+
+@dataclass
+class GridNeighborhoodSearch:
+    ndims: int
+    cell_list: FullGridCellList | None = None
+
+
+@dataclass
+class GB300Backend:
+    """parallelization_backend for the sm_103a library.  precision: "float64" (plain drop-in) or
+    "float32" (precision form); device: CUDA device index."""
+
+    precision: str = "float64"
+    device: int = 0
+
+
+# ------------------------------------------------------------------------------------------
+# Semidiscretization
+# ------------------------------------------------------------------------------------------
+def _argument_error(msg: str) -> ValueError:
+    return ValueError(f"ArgumentError: {msg}")
+
+
+class Semidiscretization:
+    """Couples one WCSPH fluid system with one Adami dummy-particle wall system."""
+
+    def __init__(self, *systems, neighborhood_search: GridNeighborhoodSearch,
+                 parallelization_backend: GB300Backend):
+        fluids = [s for s in systems if isinstance(s, WeaklyCompressibleSPHSystem)]
+        walls = [s for s in systems if isinstance(s, WallBoundarySystem)]
+        if len(fluids) != 1 or len(walls) != 1 or len(systems) != 2:
+            raise _argument_error("the GB300 backend supports exactly one "
+                                  "WeaklyCompressibleSPHSystem and one WallBoundarySystem")
+        self.fluid, self.wall = fluids[0], walls[0]
+        self.systems = (self.fluid, self.wall)
+        self.neighborhood_search = neighborhood_search
+        self.backend = parallelization_backend
+        self.config = self._config()
+        self._handle = None
+        self._lib = None
+
+    # -- validation + C config (check_configuration, semidiscretization.jl:126) --
+    def _config(self) -> _abi.TpConfig:
+        f, w = self.fluid, self.wall
+        bm = w.boundary_model
+        nd = f.ndims
+        if not isinstance(f.smoothing_kernel, WendlandC2Kernel) or f.smoothing_kernel.ndims != nd:
+            raise _argument_error(f"smoothing kernel must be WendlandC2Kernel{{{nd}}}")
+        if not isinstance(f.density_calculator, ContinuityDensity):
+            raise _argument_error("only ContinuityDensity is supported by the GB300 backend")
+        if f.correction is not None or f.surface_tension is not None or \
+                f.shifting_technique is not None:
+            raise _argument_error("corrections, surface tension and shifting are not supported")
+        if f.viscosity is not None and not isinstance(f.viscosity, ArtificialViscosityMonaghan):
+            raise _argument_error("only ArtificialViscosityMonaghan is supported")
+        if f.density_diffusion is not None and \
+                not isinstance(f.density_diffusion, DensityDiffusionMolteniColagrossi):
+            raise _argument_error("only DensityDiffusionMolteniColagrossi is supported")
+        if not isinstance(bm.density_calculator, AdamiPressureExtrapolation):
+            raise _argument_error("the wall model must use AdamiPressureExtrapolation")
+        if bm.viscosity is not None or bm.correction is not None or \
+                w.prescribed_motion is not None:
+            raise _argument_error("wall viscosity, corrections and moving walls are not supported")
+        if bm.state_equation is None:
+            raise _argument_error("`state_equation` must be given for the wall model "
+                                  "with WeaklyCompressibleSPHSystem")
+        if not isinstance(bm.smoothing_kernel, WendlandC2Kernel) or \
+                float(bm.smoothing_length) != float(f.smoothing_length):
+            raise _argument_error("the wall model must share the fluid's WendlandC2 kernel and "
+                                  "smoothing length")
+        se, sw = f.state_equation, bm.state_equation
+        if (se.sound_speed, se.reference_density, se.exponent, se.background_pressure) != \
+                (sw.sound_speed, sw.reference_density, sw.exponent, sw.background_pressure):
+            raise _argument_error("fluid and wall must share the state equation")
+        nhs = self.neighborhood_search
+        if not isinstance(nhs, GridNeighborhoodSearch) or nhs.cell_list is None:
+            raise _argument_error("GPU execution requires GridNeighborhoodSearch with a "
+                                  "FullGridCellList (docs/src/gpu.md)")
+        if not isinstance(self.backend, GB300Backend):
+            raise _argument_error("parallelization_backend must be GB300Backend()")
+        c = _abi.default_config()
+        c.ndims = nd
+        c.precision = (_abi.TP_PRECISION_FP32 if self.backend.precision == "float32"
+                       else _abi.TP_PRECISION_FP64)
+        c.n_fluid = f.initial_condition.n_particles
+        c.n_wall = w.initial_condition.n_particles
+        c.smoothing_length = float(f.smoothing_length)
+        c.reference_density = se.reference_density
+        c.sound_speed = se.sound_speed
+        c.exponent = se.exponent
+        c.background_pressure = se.background_pressure
+        c.fluid_clip_negative_pressure = int(bool(se.clip_negative_pressure))
+        c.wall_clip_negative_pressure = int(bool(bm.clip_negative_pressure))
+        if f.viscosity is None:
+            c.viscosity_model = _abi.TP_VISCOSITY_NONE
+        else:
+            c.viscosity_model = _abi.TP_VISCOSITY_MONAGHAN
+            c.viscosity_alpha = f.viscosity.alpha
+            c.viscosity_beta = f.viscosity.beta
+            c.viscosity_epsilon = f.viscosity.epsilon
+        if f.density_diffusion is None:
+            c.density_diffusion_model = _abi.TP_DIFFUSION_NONE
+        else:
+            c.density_diffusion_model = _abi.TP_DIFFUSION_MOLTENI_COLAGROSSI
+            c.density_diffusion_delta = f.density_diffusion.delta
+        acc = f.acceleration if f.acceleration is not None else (0.0,) * nd
+        for d in range(3):
+            c.acceleration[d] = float(acc[d]) if d < nd else 0.0
+        c.pressure_offset = float(bm.density_calculator.pressure_offset)
+        cl = nhs.cell_list
+        for d in range(3):
+            c.min_corner[d] = float(cl.min_corner[d]) if d < nd else 0.0
+            c.max_corner[d] = float(cl.max_corner[d]) if d < nd else 0.0
+        return c
+
+    @property
+    def ndims(self) -> int:
+        return self.fluid.ndims
+
+    @property
+    def n_fluid(self) -> int:
+        return self.fluid.initial_condition.n_particles
+
+    @property
+    def n_wall(self) -> int:
+        return self.wall.initial_condition.n_particles
+
+    # -- device side --
+    def _ensure_handle(self):
+        if self._handle is not None:
+            return
+        import torch
+
+        self._lib = _abi.load_library()
+        if not torch.cuda.is_available():
+            raise RuntimeError("GB300Backend needs a CUDA device")
+        dev = torch.device("cuda", self.backend.device)
+        torch.cuda.set_device(dev)
+        h = ctypes.c_void_p()
+        st = self._lib.tp_create(ctypes.byref(self.config), ctypes.byref(h))
+        _abi.check(self._lib, None, st)
+        self._handle = h
+        self.device = dev
+        nd = self.ndims
+        wall = self.wall.initial_condition
+        x_w = torch.as_tensor(np.ascontiguousarray(wall.coordinates, dtype=np.float64),
+                              device=dev).reshape(-1)
+        m_w = torch.as_tensor(np.ascontiguousarray(self.wall.boundary_model.hydrodynamic_mass,
+                                                   dtype=np.float64), device=dev)
+        m_f = torch.as_tensor(np.ascontiguousarray(self.fluid.initial_condition.mass,
+                                                   dtype=np.float64), device=dev)
+        self._x_w, self._m_w, self._m_f = x_w, m_w, m_f
+        self._set_stream()
+        self._call("tp_set_wall", x_w.data_ptr(), m_w.data_ptr())
+        self._call("tp_set_fluid_mass", m_f.data_ptr())
+        assert x_w.numel() == nd * self.n_wall
+
+    def _set_stream(self):
+        import torch
+
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        self._lib.tp_set_stream(self._handle, ctypes.c_void_p(s))
+
+    def _call(self, name: str, *args):
+        st = getattr(self._lib, name)(self._handle, *args)
+        _abi.check(self._lib, self._handle, st)
+
+    def close(self):
+        if self._handle is not None and self._lib is not None:
+            self._lib.tp_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- wrap_v / wrap_u (semidiscretization.jl:457-488) --
+    def wrap_v(self, v_ode):
+        return v_ode.view(self.n_fluid, self.ndims + 1)
+
+    def wrap_u(self, u_ode):
+        return u_ode.view(self.n_fluid, self.ndims)
+
+    def sync(self):
+        """tp_sync: waits for the device and raises latched device errors."""
+        self._call("tp_sync")
+
+    def fluid_pressure(self):
+        import torch
+
+        p = torch.empty(self.n_fluid, dtype=torch.float64, device=self.device)
+        self._set_stream()
+        self._call("tp_fluid_pressure", p.data_ptr())
+        return p
+
+    def wall_state(self):
+        import torch
+
+        out = [torch.empty(self.n_wall, dtype=torch.float64, device=self.device) for _ in range(3)]
+        self._set_stream()
+        self._call("tp_wall_state", *[t.data_ptr() for t in out])
+        return tuple(out)
+
+    def nhs_debug(self, u_ode):
+        import torch
+
+        nf, nw = self.n_fluid, self.n_wall
+        out = [torch.empty(n, dtype=torch.int32, device=self.device)
+               for n in (nf, nf, nf, nf, nw)]
+        self._set_stream()
+        self._call("tp_nhs_debug", u_ode.data_ptr(), *[t.data_ptr() for t in out])
+        return dict(zip(("cell", "order", "nnb_ff", "nnb_fw", "nnb_wf"), out))
+
+    def conservation(self, v_ode):
+        out = (ctypes.c_double * 5)()
+        self._set_stream()
+        self._call("tp_conservation", v_ode.data_ptr(), out)
+        return np.array(list(out))
+
+    def grid_info(self):
+        dims = (ctypes.c_int32 * 3)()
+        cs = ctypes.c_double()
+        lo = (ctypes.c_double * 3)()
+        self._call("tp_grid_info", dims, ctypes.byref(cs), lo)
+        return tuple(dims), cs.value, tuple(lo)
+
+
+@dataclass
+class ODEProblem:
+    """DynamicalODEProblem(kick!, drift!, v0, u0, tspan, p) (semidiscretization.jl:391-395)."""
+
+    v0: object
+    u0: object
+    tspan: tuple
+    p: dict = field(default_factory=dict)
+
+
+def semidiscretize(semi: Semidiscretization, tspan) -> ODEProblem:
+    """Allocate v0/u0 on the device, write the initial conditions (fluid.jl:79-97,
+    weakly_compressible_sph/system.jl:440-445: density in the last v row) and set up the
+    library handle (cell grid, static wall cell list, masses)."""
+    import torch
+
+    semi._ensure_handle()
+    ic = semi.fluid.initial_condition
+    nd = semi.ndims
+    v0 = np.empty((ic.n_particles, nd + 1), dtype=np.float64)
+    v0[:, :nd] = ic.velocity
+    v0[:, nd] = ic.density
+    u0 = np.ascontiguousarray(ic.coordinates, dtype=np.float64)
+    v0_t = torch.as_tensor(v0.reshape(-1), device=semi.device).contiguous()
+    u0_t = torch.as_tensor(u0.reshape(-1), device=semi.device).contiguous()
+    return ODEProblem(v0=v0_t, u0=u0_t, tspan=tuple(tspan), p={"semi": semi})
+
+
+def kick(dv_ode, v_ode, u_ode, p, t):
+    """kick!: dv_ode <- RHS(v_ode, u_ode).  Asynchronous on the current torch stream."""
+    semi = p["semi"]
+    semi._set_stream()
+    semi._call("tp_kick", dv_ode.data_ptr(), v_ode.data_ptr(), u_ode.data_ptr(),
+               ctypes.c_double(float(t)))
+    return dv_ode
+
+
+def drift(du_ode, v_ode, u_ode, p, t):
+    """drift!: du_ode <- v_ode[1:ndims, :]."""
+    semi = p["semi"]
+    semi._set_stream()
+    semi._call("tp_drift", du_ode.data_ptr(), v_ode.data_ptr(), u_ode.data_ptr(),
+               ctypes.c_double(float(t)))
+    return du_ode
+
+
+@dataclass(frozen=True)
+class CarpenterKennedy2N54:
+    williamson_condition: bool = False
+
+
+@dataclass
+class ODESolution:
+    v: object
+    u: object
+    t: float
+    n_steps: int
+    retcode: str = "Success"
+
+
+def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int | None = None,
+          save_everystep: bool = False) -> ODESolution:
+    """Fixed-step CarpenterKennedy2N54 from tspan[0] for `n_steps` steps (default: to tspan[1]).
+    The state is advanced by the fused library integrator; v/u of the result are new tensors."""
+    if not isinstance(alg, CarpenterKennedy2N54):
+        raise _argument_error("only CarpenterKennedy2N54 is provided by the GB300 backend")
+    semi = ode.p["semi"]
+    t0, t1 = ode.tspan
+    if n_steps is None:
+        n_steps = int(math.ceil((t1 - t0) / dt - 1e-9))
+    v = ode.v0.clone()
+    u = ode.u0.clone()
+    semi._set_stream()
+    semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(t0),
+               ctypes.c_double(dt), ctypes.c_int64(n_steps))
+    semi.sync()
+    return ODESolution(v=v, u=u, t=t0 + n_steps * dt, n_steps=n_steps)
+
+
+def dam_break_semidiscretization(tank, eos, smoothing_length: float, *, precision="float64",
+                                 alpha=0.02, delta=0.1, gravity=9.81, wall_clip=True,
+                                 device: int = 0) -> Semidiscretization:
+    """The dam-break system pair of examples/fluid/dam_break_2d.jl with a FullGridCellList over
+    the tank's wall particles (examples/fluid/dam_break_2d_gpu.jl:30-33)."""
+    nd = tank.fluid.ndims
+    kern = WendlandC2Kernel(nd)
+    acc = (0.0, -gravity) if nd == 2 else (0.0, -gravity, 0.0)
+    fluid = WeaklyCompressibleSPHSystem(
+        tank.fluid, smoothing_kernel=kern, smoothing_length=smoothing_length,
+        density_calculator=ContinuityDensity(), state_equation=eos, acceleration=acc,
+        viscosity=ArtificialViscosityMonaghan(alpha=alpha, beta=0.0),
+        density_diffusion=DensityDiffusionMolteniColagrossi(delta=delta))
+    bm = BoundaryModelDummyParticles(
+        tank.boundary.density, tank.boundary.mass, AdamiPressureExtrapolation(), kern,
+        smoothing_length, state_equation=eos, clip_negative_pressure=wall_clip)
+    wall = WallBoundarySystem(tank.boundary, bm)
+    allc = np.concatenate([tank.boundary.coordinates, tank.fluid.coordinates], axis=0)
+    cl = FullGridCellList(tuple(allc.min(axis=0)), tuple(allc.max(axis=0)))
+    return Semidiscretization(fluid, wall, neighborhood_search=GridNeighborhoodSearch(nd, cl),
+                              parallelization_backend=GB300Backend(precision, device))
