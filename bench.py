@@ -255,6 +255,28 @@ def run_reference(args):
     return 0
 
 
+def run_profile_form(args):
+    import torch
+
+    import __graft_entry__ as g
+
+    prec, wl = args.profile_form.split(":")
+    cfg = {"cfg1": CFG1, "cfg2": CFG2}[wl]
+    pkg = g.load_package()
+    pkg.load_library()
+    semi, tank = make_case(pkg, cfg, prec, 0)
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    v, u, ms, launches, ph = run_form(pkg, torch, semi, ode, args.steps, args.warmup, cfg["dt"],
+                                      prec)
+    n = semi.n_fluid + semi.n_wall
+    print(json.dumps({"profile_form": args.profile_form, "n_fluid": semi.n_fluid,
+                      "n_wall": semi.n_wall, "steps": args.steps, "ms_per_step": ms / args.steps,
+                      "value": n * args.steps / (ms / 1e3), "launches": launches,
+                      "phase_ms": ph}), flush=True)
+    semi.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -263,9 +285,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-forms", action="store_true", help="skip the dx=0.0064 form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile-form", default=None, metavar="PRECISION:WORKLOAD",
+                    help="profiling mode (e.g. float32:cfg2): only warm-up + timed steps of that "
+                         "form, one summary line; used under ncu")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_form:
+        return run_profile_form(args)
 
     import torch
 

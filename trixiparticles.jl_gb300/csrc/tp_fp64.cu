@@ -263,11 +263,12 @@ __global__ void __launch_bounds__(128) k_pair64(Phys P, GridDesc g, int nf,
         for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
     } else {
         // CarpenterKennedy2N54 stage: tmp = A*tmp + dt*k ; u = u + B*tmp (du = v at stage start)
-        const double va_arr[4] = {va.x, va.y, va.z, va.w};
+        // state row d of the slot: velocity components, then the density (record .w)
+        const double va_arr[4] = {va.x, va.y, ND == 3 ? va.z : va.w, va.w};
         const double xa_arr[3] = {pa.x, pa.y, pa.z};
 #pragma unroll
         for (int d = 0; d <= ND; ++d) {
-            const double kv = (d == ND) ? k[ND] : k[d];
+            const double kv = k[d];
             double tv = U.first ? U.dt * kv : fma(U.dt, kv, U.A * U.tv[(size_t)s * (ND + 1) + d]);
             U.tv_out[(size_t)s * (ND + 1) + d] = tv;
             U.v_out[(size_t)s * (ND + 1) + d] = fma(U.B, tv, va_arr[d]);
