@@ -112,11 +112,11 @@ __global__ void k_store(const double* __restrict__ u, const void* __restrict__ v
 }
 
 template <bool F32>
-__global__ void k_scatter_pressure(const void* __restrict__ pos, const int* __restrict__ perm,
+__global__ void k_scatter_pressure(const void* __restrict__ rec, const int* __restrict__ perm,
                                    double* __restrict__ p, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    p[perm[s]] = F32 ? (double)((const float4*)pos)[s].w : ((const double4_32a*)pos)[s].w;
+    p[perm[s]] = F32 ? (double)((const float2*)rec)[s].x : ((const double4_32a*)rec)[s].w;
 }
 
 template <bool F32>
@@ -128,11 +128,11 @@ __global__ void k_scatter_wall(const void* __restrict__ state, const double* __r
     const int i = perm[s];
     double ps, rs;
     if (F32) {
-        const float2 st = ((const float2*)state)[s];
+        const float4 st = ((const float4*)state)[s];
         ps = st.x;
         rs = rho0 + (double)st.y;
     } else {
-        const double2 st = ((const double2*)state)[s];
+        const double4_32a st = ((const double4_32a*)state)[s];
         ps = st.x;
         rs = st.y;
     }
@@ -487,9 +487,10 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->f_start, nc + 1));
     A(dalloc(&h->f_cursor, nc));
     A(dalloc(&h->scan_partial, (size_t)h->scan_blocks));
+    A(dalloc(&h->f_test, nf));
     A(dalloc((double4_32a**)&h->f_pos, nf));
     A(dalloc((double4_32a**)&h->f_vel, nf));
-    A(dalloc((double**)&h->f_mass, nf));
+    A(dalloc((double2**)&h->f_aux, nf));
     A(dalloc(&h->m_f, nf));
     A(dalloc(&h->w_key, nw));
     A(dalloc(&h->w_tmp, nw));
@@ -497,8 +498,8 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->w_skey, nw));
     A(dalloc(&h->w_start, nc + 1));
     A(dalloc((double4_32a**)&h->w_pos, nw));
-    A(dalloc((double4_32a**)&h->w_pos64, nw));
-    A(dalloc((double2**)&h->w_state, nw));
+    A(dalloc(&h->w_test, nw));
+    A(dalloc((double4_32a**)&h->w_state, nw));
     A(dalloc(&h->w_vol, nw));
     h->red_blocks = 256;
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
@@ -520,10 +521,11 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
 tp_status tp_destroy(tp_handle* h) {
     if (!h) return TP_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void* ptrs[] = {h->f_key,  h->f_tmp,     h->f_perm,   h->f_skey,   h->f_count, h->f_start,
-                    h->f_cursor, h->scan_partial, h->f_pos, h->f_vel,  h->f_mass,  h->m_f,
-                    h->w_key,  h->w_tmp,     h->w_perm,   h->w_skey,   h->w_start, h->w_pos,
-                    h->w_pos64, h->w_state,  h->w_vol,    h->red_partial, h->d_err};
+    void* ptrs[] = {h->f_key,   h->f_tmp,   h->f_perm,  h->f_skey,        h->f_count,
+                    h->f_start, h->f_cursor, h->scan_partial, h->f_test, h->f_pos,
+                    h->f_vel,   h->f_aux,   h->m_f,     h->w_key,         h->w_tmp,
+                    h->w_perm,  h->w_skey,  h->w_start, h->w_pos,         h->w_test,
+                    h->w_state, h->w_vol,   h->red_partial, h->d_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
@@ -552,11 +554,8 @@ tp_status tp_set_wall(tp_handle* h, const double* x_wall, const double* m_wall) 
     tp_status st = sort_particles(h, x_wall, nw, h->w_key, h->w_tmp, h->w_start);
     if (st != TP_OK) return st;
     if (nw > 0) {
-        fp64_pack_wall(h, x_wall, m_wall, h->w_pos64);
-        if (h->cfg.precision == TP_PRECISION_FP32)
-            fp32_pack_wall(h, x_wall, m_wall);
-        else
-            fp64_pack_wall(h, x_wall, m_wall, h->w_pos);
+        fp64_pack_wall(h, x_wall, m_wall);
+        if (h->cfg.precision == TP_PRECISION_FP32) fp32_init_wall_state(h);
         TP_LAUNCHED(h, "wall pack");
     }
     // A wall particle outside the grid is a configuration error: report it now.
@@ -729,7 +728,7 @@ tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid) {
     if (nf == 0) return TP_OK;
     if (!p_fluid) return fail(h, TP_ERR_ARGUMENT, "tp_fluid_pressure: null array");
     if (h->cfg.precision == TP_PRECISION_FP32)
-        k_scatter_pressure<true><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, h->f_perm,
+        k_scatter_pressure<true><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_aux, h->f_perm,
                                                                         p_fluid, nf);
     else
         k_scatter_pressure<false><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, h->f_perm,

@@ -3,8 +3,8 @@
 // Same passes and neighbour order as the FP64 drop-in, with these precision choices:
 //   * positions enter the pair arithmetic as FP32 offsets inside their cell,
 //     o = x - floor(x / cs) * cs32 (FP64 on input, rounded once to FP32), so a pair difference
-//     is (o_a - shift) - o_b with shift = (cell_b - cell_a) * cs32 and stays accurate to FP32
-//     relative precision of the smoothing length whatever the domain size;
+//     is (o_a - o_b) + (cell_a - cell_b) * cs32 and stays accurate to FP32 relative precision of
+//     the smoothing length whatever the domain size;
 //   * density is stored as the deviation rho - rho0 in FP32, so differences of densities and
 //     the Cole EOS, evaluated as B * expm1(gamma * log1p((rho - rho0) / rho0)), do not cancel;
 //   * per-particle sums (dv, drho, Adami pressure and volume) use Kahan-compensated FP32;
@@ -12,8 +12,10 @@
 //     Float32 GPU path compiles to;
 //   * positions and their Runge-Kutta register stay FP64 (the drift! accumulation); velocity
 //     and density registers are FP32.
+// The neighbour set is the FP32 one: |o_a - o_b + shift|^2 <= (2h)^2 evaluated in FP32.
 #include "tp_api_internal.h"
 #include "tp_nhs.cuh"
+#include "tp_warpnbr.cuh"
 
 namespace tp {
 
@@ -38,17 +40,21 @@ __device__ __forceinline__ float eos32_inverse_dev(float p, const Phys32& P) {
     return P.rho0 * expm1f(log1pf((p - P.p_bg) / P.B) * P.inv_gamma);
 }
 
+// Difference o_a - o_b + shift of a queued candidate, recomputed exactly as the filter did.
 template <int ND>
-__device__ __forceinline__ void cell_offsets(const double* x, double cs, double cs32, float o[3]) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        if (d < ND) {
-            const double fl = floor(__ddiv_rn(x[d], cs));
-            o[d] = (float)__dsub_rn(x[d], __dmul_rn(fl, cs32));
-        } else {
-            o[d] = 0.0f;
-        }
+__device__ __forceinline__ float pair_diff(float4 ta, float cxa, float cs, int e, float4 cb,
+                                           float& pdx, float& pdy, float& pdz) {
+    int dy, dz;
+    row_shift(e >> kSlotBits, dy, dz);
+    pdx = fmaf(cxa - cb.w, cs, ta.x) - cb.x;
+    pdy = (ta.y - (float)dy * cs) - cb.y;
+    float d2 = pdx * pdx + pdy * pdy;
+    pdz = 0.0f;
+    if (ND == 3) {
+        pdz = (ta.z - (float)dz * cs) - cb.z;
+        d2 = fmaf(pdz, pdz, d2);
     }
+    return d2;
 }
 
 // Source state -> fluid record slot.  SRC32: the integrator's FP32 velocity/density state
@@ -65,17 +71,17 @@ struct Pack32 {
     double* tu_out;
     float4* tv_out;
     int* id_out;
-    float4* pos;
+    float* m_out;
+    float4* test;
     float4* vel;
-    float* mass;
-    double cs, cs32, rho0;
+    float2* aux;
+    GridDesc g;
+    double cs32, rho0;
     Phys32 P;
     __device__ void operator()(int i, int s) const {
         double x[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
-        float o[3];
-        cell_offsets<ND>(x, cs, cs32, o);
         float4 w;
         float mi;
         if (SRC32) {
@@ -89,10 +95,9 @@ struct Pack32 {
             w.w = (float)(vv[ND] - rho0);
             mi = (float)((const double*)m)[i];
         }
-        const float p = eos32(w.w, P, P.fluid_clip);
-        pos[s] = make_float4(o[0], o[1], o[2], p);
+        test[s] = test_record<ND>(x, g, cs32);
         vel[s] = w;
-        mass[s] = mi;
+        aux[s] = make_float2(eos32(w.w, P, P.fluid_clip), mi);
         if (u_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) {
@@ -101,80 +106,65 @@ struct Pack32 {
             }
             tv_out[s] = tv[i];
             id_out[s] = id_in[i];
+            m_out[s] = mi;
         }
     }
 };
 
-template <int ND>
-struct PackWall32 {
-    const double* x;
-    const double* m;
-    float4* pos;
-    double cs, cs32;
-    __device__ void operator()(int i, int s) const {
-        double y[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < ND; ++d) y[d] = x[(size_t)i * ND + d];
-        float o[3];
-        cell_offsets<ND>(y, cs, cs32, o);
-        pos[s] = make_float4(o[0], o[1], o[2], (float)m[i]);
-    }
-};
+// FP32 wall state: {p, rho - rho0, m, 0}; masses are set once, p and rho by the Adami pass.
+__global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4* __restrict__ st,
+                                    int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) st[s] = make_float4(0.0f, 0.0f, (float)wpos[s].w, 0.0f);
+}
 
 template <int ND>
 __global__ void __launch_bounds__(128) k_adami32(Phys32 P, GridDesc g, int nw,
-                                                 const float4* __restrict__ wpos,
+                                                 const float4* __restrict__ wtest,
                                                  const int* __restrict__ wskey,
-                                                 float2* __restrict__ wstate,
+                                                 float4* __restrict__ wstate,
                                                  double* __restrict__ wvol,
-                                                 const float4* __restrict__ fpos,
+                                                 const float4* __restrict__ ftest,
                                                  const float4* __restrict__ fvel,
+                                                 const float2* __restrict__ faux,
                                                  const int* __restrict__ fstart) {
+    __shared__ WarpSmem smw[4];
+    WarpSmem& sm = smw[threadIdx.x >> 5];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nw) return;
-    const float4 xw = wpos[w];
+    const bool active = w < nw;
+    const int wi = active ? w : 0;
+    const float4 tw = wtest[wi];
     int c[3];
-    key_to_coords(wskey[w], g, c);
+    key_to_coords(wskey[wi], g, c);
+    const float cxw = (float)c[0];
     Kahan Ps, V;
-    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            const float s1 = xw.y - (float)dy * P.cs, s2 = xw.z - (float)dz * P.cs;
-#pragma unroll
-            for (int dx = -1; dx <= 1; ++dx) {
-                const float s0 = xw.x - (float)dx * P.cs;
-                const int b1 = fstart[row + dx + 2];
-                for (int b = fstart[row + dx + 1]; b < b1; ++b) {
-                    const float4 xb = fpos[b];
-                    const float pd0 = s0 - xb.x, pd1 = s1 - xb.y;
-                    const float pd2 = (ND == 3) ? s2 - xb.z : 0.0f;
-                    float d2 = pd0 * pd0 + pd1 * pd1;
-                    if (ND == 3) d2 += pd2 * pd2;
-                    if (d2 > P.sr2) continue;
-                    const float r = sqrtf(d2);
-                    const float rho_f = P.rho0 + fvel[b].w;
-                    float hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
-                    if (ND == 3) hp += P.g[2] * (rho_f * pd2);
-                    const float sum = (P.p_off + xb.w) + hp;
-                    float W = 0.0f;
-                    if (r < P.two_h) {
-                        const float q = r * P.h_inv;
-                        const float t = 1.0f - 0.5f * q;
-                        const float t2 = t * t;
-                        W = (P.wc2_norm * (t2 * t2)) * (2.0f * q + 1.0f);
-                    }
-                    Ps.add(sum * W);
-                    V.add(W);
-                }
-            }
+    auto gather = [&](int e) {
+        const int b = e & kSlotMask;
+        float pd0, pd1, pd2;
+        const float d2 = pair_diff<ND>(tw, cxw, P.cs, e, ftest[b], pd0, pd1, pd2);
+        const float r = sqrtf(d2);
+        const float rho_f = P.rho0 + fvel[b].w;
+        float hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
+        if (ND == 3) hp += P.g[2] * (rho_f * pd2);
+        const float sum = (P.p_off + faux[b].x) + hp;
+        float W = 0.0f;
+        if (r < P.two_h) {
+            const float q = r * P.h_inv;
+            const float t = 1.0f - 0.5f * q;
+            const float t2 = t * t;
+            W = (P.wc2_norm * (t2 * t2)) * (2.0f * q + 1.0f);
         }
-    }
+        Ps.add(sum * W);
+        V.add(W);
+    };
+    warp_neighbors<ND>(g, P.cs, active, c, tw, fstart, ftest, P.sr2, sm, gather);
+    if (!active) return;
     float pw = Ps.s - Ps.c;
     const float vw = V.s - V.c;
     if ((double)vw > 2.220446049250313e-16) pw = pw / vw;
     if (P.wall_clip) pw = (pw != pw || pw > 0.0f) ? pw : 0.0f;
-    wstate[w] = make_float2(pw, eos32_inverse_dev(pw, P));
+    const float m = wstate[w].z;
+    wstate[w] = make_float4(pw, eos32_inverse_dev(pw, P), m, 0.0f);
     wvol[w] = (double)vw;
 }
 
@@ -193,122 +183,101 @@ struct Update32 {
 };
 
 template <int ND, bool INTEGRATE>
-__global__ void __launch_bounds__(128) k_pair32(Phys32 P, GridDesc g, int nf,
-                                                const float4* __restrict__ fpos,
+__global__ void __launch_bounds__(128, 4) k_pair32(Phys32 P, GridDesc g, int nf,
+                                                const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
-                                                const float* __restrict__ fmass,
+                                                const float2* __restrict__ faux,
                                                 const int* __restrict__ fstart,
                                                 const int* __restrict__ fskey,
-                                                const float4* __restrict__ wpos,
-                                                const float2* __restrict__ wstate,
+                                                const float4* __restrict__ wtest,
+                                                const float4* __restrict__ wstate,
                                                 const int* __restrict__ wstart, Update32 U) {
+    __shared__ WarpSmem smw[4];
+    WarpSmem& sm = smw[threadIdx.x >> 5];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nf) return;
-    const float4 pa = fpos[s];
-    const float4 va = fvel[s];
-    const float p_a = pa.w;
+    const bool active = s < nf;
+    const int si = active ? s : 0;
+    const float4 ta = ftest[si];
+    const float4 va = fvel[si];
+    const float p_a = faux[si].x;
     const float drho_a = va.w;
     const float rho_a = P.rho0 + drho_a;
     int c[3];
-    key_to_coords(fskey[s], g, c);
-    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+    key_to_coords(fskey[si], g, c);
+    const float cxa = (float)c[0];
 
     Kahan a0, a1, a2, ar;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            const float s1 = pa.y - (float)dy * P.cs, s2 = pa.z - (float)dz * P.cs;
-#pragma unroll
-            for (int dx = -1; dx <= 1; ++dx) {
-                const float s0 = pa.x - (float)dx * P.cs;
-                const int b1 = fstart[row + dx + 2];
-                for (int b = fstart[row + dx + 1]; b < b1; ++b) {
-                    const float4 pb = fpos[b];
-                    const float pd0 = s0 - pb.x, pd1 = s1 - pb.y;
-                    const float pd2 = (ND == 3) ? s2 - pb.z : 0.0f;
-                    float d2 = pd0 * pd0 + pd1 * pd1;
-                    if (ND == 3) d2 += pd2 * pd2;
-                    if (d2 > P.sr2) continue;
-                    const float r = sqrtf(d2);
-                    if (r < P.almostzero) continue;
-                    const float4 vb = fvel[b];
-                    const float m_b = fmass[b];
-                    const float rho_b = P.rho0 + vb.w;
-                    const float q = r * P.h_inv;
-                    const float t = 1.0f - 0.5f * q;
-                    const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-                    const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-                    const float coef = -m_b * __fdividef(p_a + pb.w, rho_a * rho_b);
-                    float e0 = coef * g0, e1 = coef * g1, e2 = coef * g2;
-                    const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
-                    const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
-                    if (P.visc) {
-                        float vr = vd0 * pd0 + vd1 * pd1;
-                        if (ND == 3) vr += vd2 * pd2;
-                        if (vr < 0.0f) {
-                            const float rho_mean = 0.5f * (rho_a + rho_b);
-                            const float mu = __fdividef(P.visc_h * vr, r * r + P.visc_eps_h2);
-                            const float num = (m_b * P.visc_ac) * mu + (m_b * P.beta) * (mu * mu);
-                            const float f = __fdividef(num, rho_mean);
-                            e0 += f * g0;
-                            e1 += f * g1;
-                            e2 += f * g2;
-                        }
-                    }
-                    a0.add(e0);
-                    a1.add(e1);
-                    if (ND == 3) a2.add(e2);
-                    float vg = vd0 * g0 + vd1 * g1;
-                    if (ND == 3) vg += vd2 * g2;
-                    float er = (__fdividef(rho_a, rho_b) * m_b) * vg;
-                    if (P.diff) {
-                        const float vol_b = __fdividef(m_b, rho_b);
-                        const float pc = __fdividef(2.0f * (drho_a - vb.w), r * r);
-                        float pg = pd0 * g0 + pd1 * g1;
-                        if (ND == 3) pg += pd2 * g2;
-                        er += P.diff_coef * (vol_b * (pc * pg));
-                    }
-                    ar.add(er);
-                }
+    auto ff = [&](int e) {
+        const int b = e & kSlotMask;
+        float pd0, pd1, pd2;
+        const float d2 = pair_diff<ND>(ta, cxa, P.cs, e, ftest[b], pd0, pd1, pd2);
+        const float r = sqrtf(d2);
+        if (r < P.almostzero) return;
+        const float4 vb = fvel[b];
+        const float2 ab = faux[b];  // {p_b, m_b}
+        const float m_b = ab.y;
+        const float rho_b = P.rho0 + vb.w;
+        const float q = r * P.h_inv;
+        const float t = 1.0f - 0.5f * q;
+        const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+        const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+        const float coef = -m_b * __fdividef(p_a + ab.x, rho_a * rho_b);
+        float e0 = coef * g0, e1 = coef * g1, e2 = coef * g2;
+        const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
+        const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
+        if (P.visc) {
+            float vr = vd0 * pd0 + vd1 * pd1;
+            if (ND == 3) vr += vd2 * pd2;
+            if (vr < 0.0f) {
+                const float rho_mean = 0.5f * (rho_a + rho_b);
+                const float mu = __fdividef(P.visc_h * vr, r * r + P.visc_eps_h2);
+                const float num = (m_b * P.visc_ac) * mu + (m_b * P.beta) * (mu * mu);
+                const float f = __fdividef(num, rho_mean);
+                e0 += f * g0;
+                e1 += f * g1;
+                e2 += f * g2;
             }
         }
-    }
+        a0.add(e0);
+        a1.add(e1);
+        if (ND == 3) a2.add(e2);
+        float vg = vd0 * g0 + vd1 * g1;
+        if (ND == 3) vg += vd2 * g2;
+        float er = (__fdividef(rho_a, rho_b) * m_b) * vg;
+        if (P.diff) {
+            const float vol_b = __fdividef(m_b, rho_b);
+            const float pc = __fdividef(2.0f * (drho_a - vb.w), r * r);
+            float pg = pd0 * g0 + pd1 * g1;
+            if (ND == 3) pg += pd2 * g2;
+            er += P.diff_coef * (vol_b * (pc * pg));
+        }
+        ar.add(er);
+    };
+    warp_neighbors<ND>(g, P.cs, active, c, ta, fstart, ftest, P.sr2, sm, ff);
 
     Kahan w0, w1, w2, wr;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            const float s1 = pa.y - (float)dy * P.cs, s2 = pa.z - (float)dz * P.cs;
-#pragma unroll
-            for (int dx = -1; dx <= 1; ++dx) {
-                const float s0 = pa.x - (float)dx * P.cs;
-                const int b1 = wstart[row + dx + 2];
-                for (int b = wstart[row + dx + 1]; b < b1; ++b) {
-                    const float4 pb = wpos[b];
-                    const float pd0 = s0 - pb.x, pd1 = s1 - pb.y;
-                    const float pd2 = (ND == 3) ? s2 - pb.z : 0.0f;
-                    float d2 = pd0 * pd0 + pd1 * pd1;
-                    if (ND == 3) d2 += pd2 * pd2;
-                    if (d2 > P.sr2) continue;
-                    const float r = sqrtf(d2);
-                    if (r < P.almostzero) continue;
-                    const float2 sb = wstate[b];
-                    const float m_b = pb.w, p_b = sb.x, rho_b = P.rho0 + sb.y;
-                    const float q = r * P.h_inv;
-                    const float t = 1.0f - 0.5f * q;
-                    const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-                    const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-                    const float coef = -m_b * __fdividef(p_a + p_b, rho_a * rho_b);
-                    w0.add(coef * g0);
-                    w1.add(coef * g1);
-                    if (ND == 3) w2.add(coef * g2);
-                    float vg = va.x * g0 + va.y * g1;
-                    if (ND == 3) vg += va.z * g2;
-                    wr.add((__fdividef(rho_a, rho_b) * m_b) * vg);
-                }
-            }
-        }
-    }
+    auto fw = [&](int e) {
+        const int b = e & kSlotMask;
+        float pd0, pd1, pd2;
+        const float d2 = pair_diff<ND>(ta, cxa, P.cs, e, wtest[b], pd0, pd1, pd2);
+        const float r = sqrtf(d2);
+        if (r < P.almostzero) return;
+        const float4 sb = wstate[b];  // {p, rho - rho0, m, 0}
+        const float m_b = sb.z, p_b = sb.x, rho_b = P.rho0 + sb.y;
+        const float q = r * P.h_inv;
+        const float t = 1.0f - 0.5f * q;
+        const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+        const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+        const float coef = -m_b * __fdividef(p_a + p_b, rho_a * rho_b);
+        w0.add(coef * g0);
+        w1.add(coef * g1);
+        if (ND == 3) w2.add(coef * g2);
+        float vg = va.x * g0 + va.y * g1;
+        if (ND == 3) vg += va.z * g2;
+        wr.add((__fdividef(rho_a, rho_b) * m_b) * vg);
+    };
+    warp_neighbors<ND>(g, P.cs, active, c, ta, wstart, wtest, P.sr2, sm, fw);
+    if (!active) return;
 
     double k[4];
     k[0] = (a0.value() + w0.value()) + U.g[0];
@@ -321,23 +290,21 @@ __global__ void __launch_bounds__(128) k_pair32(Phys32 P, GridDesc g, int nf,
 #pragma unroll
         for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
     } else {
+        // float4 slots: velocity components 0..ND-1 and the density deviation in slot 3
+        const float kv[4] = {(float)k[0], (float)k[1], ND == 3 ? (float)k[2] : 0.0f,
+                             (float)k[ND]};
         const float vin[4] = {va.x, va.y, va.z, va.w};
-        float kv[4] = {(float)k[0], (float)k[1], (float)k[2], 0.0f};
-        kv[ND] = (float)k[ND];
-        float4 tv = U.tv[s];
-        float tva[4] = {tv.x, tv.y, tv.z, tv.w};
-        float vout[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const float4 tv = U.tv[s];
+        const float tin[4] = {tv.x, tv.y, tv.z, tv.w};
+        float tout[4], vout[4];
 #pragma unroll
         for (int d = 0; d < 4; ++d) {
-            const int src = (d == 3) ? ND : d;  // slot 3 of the float4 is the density
-            if (d < ND || d == 3) {
-                const float kk = (d == 3) ? kv[ND] : kv[d];
-                const float t = U.first ? U.dtf * kk : fmaf(U.dtf, kk, U.Af * tva[d]);
-                tva[d] = t;
-                vout[d] = fmaf(U.Bf, t, (d == 3) ? vin[3] : vin[src]);
-            }
+            const bool used = (d < ND) || (d == 3);
+            const float t = U.first ? U.dtf * kv[d] : fmaf(U.dtf, kv[d], U.Af * tin[d]);
+            tout[d] = used ? t : 0.0f;
+            vout[d] = used ? fmaf(U.Bf, t, vin[d]) : 0.0f;
         }
-        U.tv[s] = make_float4(tva[0], tva[1], tva[2], tva[3]);
+        U.tv[s] = make_float4(tout[0], tout[1], tout[2], tout[3]);
         U.v_out[s] = make_float4(vout[0], vout[1], vout[2], vout[3]);
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
@@ -360,7 +327,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
                const PhysState* src, PhysState* dst) {
     const int n = (int)h->cfg.n_fluid;
     if (n == 0) return;
-    const double cs = h->grid.cs, cs32 = (double)(float)h->grid.cs;
+    const double cs32 = (double)(float)h->grid.cs;
     auto run = [&](auto ndc, auto srcc) {
         constexpr int ND = decltype(ndc)::value;
         constexpr bool S32 = decltype(srcc)::value;
@@ -376,13 +343,12 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
             pk.tu_out = dst->tu;
             pk.tv_out = (float4*)dst->tv;
             pk.id_out = dst->id;
-            pk.mass = (float*)dst->m;
-        } else {
-            pk.mass = (float*)h->f_mass;
+            pk.m_out = (float*)dst->m;
         }
-        pk.pos = (float4*)h->f_pos;
+        pk.test = h->f_test;
         pk.vel = (float4*)h->f_vel;
-        pk.cs = cs;
+        pk.aux = (float2*)h->f_aux;
+        pk.g = h->grid;
         pk.cs32 = cs32;
         pk.rho0 = h->cfg.reference_density;
         pk.P = h->phys32;
@@ -399,19 +365,13 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
     }
 }
 
-void fp32_pack_wall(tp_handle* h, const double* x, const double* m) {
+// The FP32 form shares the FP64 wall records (w_pos {x, y, z, m}, w_test); it only needs its
+// own state array with the masses filled in.
+void fp32_init_wall_state(tp_handle* h) {
     const int n = (int)h->cfg.n_wall;
     if (n == 0) return;
-    const double cs = h->grid.cs, cs32 = (double)(float)h->grid.cs;
-    if (h->cfg.ndims == 2) {
-        PackWall32<2> pk{x, m, (float4*)h->w_pos, cs, cs32};
-        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
-                                                          h->w_perm, h->w_skey, pk);
-    } else {
-        PackWall32<3> pk{x, m, (float4*)h->w_pos, cs, cs32};
-        k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
-                                                          h->w_perm, h->w_skey, pk);
-    }
+    k_wall_state32_init<<<nblk(n, 256), 256, 0, h->stream>>>((const double4_32a*)h->w_pos,
+                                                             (float4*)h->w_state, n);
 }
 
 void fp32_adami(tp_handle* h) {
@@ -419,21 +379,20 @@ void fp32_adami(tp_handle* h) {
     if (nw == 0) return;
     if (h->cfg.ndims == 2)
         k_adami32<2><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys32, h->grid, nw, (const float4*)h->w_pos, h->w_skey, (float2*)h->w_state,
-            h->w_vol, (const float4*)h->f_pos, (const float4*)h->f_vel, h->f_start);
+            h->phys32, h->grid, nw, h->w_test, h->w_skey, (float4*)h->w_state, h->w_vol,
+            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->f_start);
     else
         k_adami32<3><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys32, h->grid, nw, (const float4*)h->w_pos, h->w_skey, (float2*)h->w_state,
-            h->w_vol, (const float4*)h->f_pos, (const float4*)h->f_vel, h->f_start);
+            h->phys32, h->grid, nw, h->w_test, h->w_skey, (float4*)h->w_state, h->w_vol,
+            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->f_start);
 }
 
 template <int ND, bool INTEG>
-static void launch_pair32(tp_handle* h, const float* fmass, const Update32& U) {
+static void launch_pair32(tp_handle* h, const Update32& U) {
     const int nf = (int)h->cfg.n_fluid;
     k_pair32<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
-        h->phys32, h->grid, nf, (const float4*)h->f_pos, (const float4*)h->f_vel, fmass,
-        h->f_start, h->f_skey, (const float4*)h->w_pos, (const float2*)h->w_state, h->w_start,
-        U);
+        h->phys32, h->grid, nf, h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux,
+        h->f_start, h->f_skey, h->w_test, (const float4*)h->w_state, h->w_start, U);
 }
 
 void fp32_pair_kick(tp_handle* h, double* dv) {
@@ -443,9 +402,9 @@ void fp32_pair_kick(tp_handle* h, double* dv) {
     U.perm = h->f_perm;
     for (int d = 0; d < 3; ++d) U.g[d] = h->cfg.acceleration[d];
     if (h->cfg.ndims == 2)
-        launch_pair32<2, false>(h, (const float*)h->f_mass, U);
+        launch_pair32<2, false>(h, U);
     else
-        launch_pair32<3, false>(h, (const float*)h->f_mass, U);
+        launch_pair32<3, false>(h, U);
 }
 
 void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first) {
@@ -465,9 +424,9 @@ void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt,
     U.dtf = (float)dt;
     U.first = first;
     if (h->cfg.ndims == 2)
-        launch_pair32<2, true>(h, (const float*)st.m, U);
+        launch_pair32<2, true>(h, U);
     else
-        launch_pair32<3, true>(h, (const float*)st.m, U);
+        launch_pair32<3, true>(h, U);
 }
 
 }  // namespace tp

@@ -1,14 +1,20 @@
 // tp_fp64.cu — plain FP64 drop-in form of the WCSPH right-hand side (sm_103a).
 //
-// Every quantity is Float64, as in the reference's Float64 GPU path.  Divisions the reference
-// writes as `div_fast` use its CUDA Float64 definition x * fast_inv(y)
+// Every physical quantity is Float64, as in the reference's Float64 GPU path.  Divisions the
+// reference writes as `div_fast` use its CUDA Float64 definition x * fast_inv(y)
 // (ext/TrixiParticlesCUDAExt.jl:12-32): approximate reciprocal `rcp.approx.ftz.f64` refined by
 // one cubic iteration e = 1 - a r; e = e + e^2; r = r + e r (the method the reference takes from
-// Oceananigans.jl PR 5140).  Plain `/` in the reference stays IEEE division here.
-// Squared distances use explicitly rounded products and sums (no FMA contraction) so that the
-// neighbour set {b : |x_a - x_b|^2 <= (2h)^2} is decided exactly as on the CPU.
+// Oceananigans.jl PR 5140).  fast_inv(rho) of every particle is evaluated once in the pack pass
+// and reused for rho_a / rho_b and m_b / rho_b, which is bitwise the same as evaluating it per
+// pair.  Plain `/` in the reference stays IEEE division here.
+//
+// Neighbour candidates are filtered with an FP32 distance on cell-relative offsets whose bound
+// is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative), then every surviving pair is
+// decided exactly in FP64 with explicitly rounded products and sums (no FMA contraction), so the
+// neighbour set {b : |x_a - x_b|^2 <= (2h)^2} is the one the CPU computes.
 #include "tp_api_internal.h"
 #include "tp_nhs.cuh"
+#include "tp_warpnbr.cuh"
 
 namespace tp {
 
@@ -30,23 +36,27 @@ __device__ __forceinline__ double dist2_rn(double p0, double p1, double p2) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Pack: source particle i -> fluid record slot s (EOS evaluated here: compute_pressure!,
-// weakly_compressible_sph/system.jl:426-438).
+// Pack: source particle i -> fluid record slot s.  The fluid EOS is evaluated here
+// (compute_pressure!, weakly_compressible_sph/system.jl:426-438).
 // ------------------------------------------------------------------------------------------
 template <int ND>
 struct Pack64 {
     const double* u;   // (ND, n) source order
     const double* v;   // (ND+1, n)
     const double* m;   // (n)
-    const double* tu;  // optional: integrator registers (source order), copied with the state
+    const double* tu;  // optional: integrator registers (source order), moved with the state
     const double* tv;
     const int* id_in;
     double* tu_out;
     double* tv_out;
     int* id_out;
+    double* m_out;
+    float4* test;
     double4_32a* pos;
     double4_32a* vel;
-    double* mass;
+    double2* aux;
+    GridDesc g;
+    double cs32;
     Phys P;
     __device__ void operator()(int i, int s) const {
         double x[3] = {0, 0, 0}, w[4] = {0, 0, 0, 0};
@@ -56,9 +66,11 @@ struct Pack64 {
         for (int d = 0; d <= ND; ++d) w[d] = v[(size_t)i * (ND + 1) + d];
         const double rho = w[ND];
         const double p = eos_pressure(rho, P, P.fluid_clip);
+        const double mi = m[i];
+        test[s] = test_record<ND>(x, g, cs32);
         pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
         vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
-        mass[s] = m[i];
+        aux[s] = make_double2(mi, fast_inv(rho));
         if (tu_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) tu_out[(size_t)s * ND + d] = tu[(size_t)i * ND + d];
@@ -66,61 +78,97 @@ struct Pack64 {
             for (int d = 0; d <= ND; ++d)
                 tv_out[(size_t)s * (ND + 1) + d] = tv[(size_t)i * (ND + 1) + d];
             id_out[s] = id_in[i];
+            m_out[s] = mi;
         }
     }
 };
 
+// Positions only (p = 0): neighbour-count diagnostics.
+template <int ND>
+struct PackPos64 {
+    const double* u;
+    double4_32a* pos;
+    __device__ void operator()(int i, int s) const {
+        double x[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
+        pos[s] = make_double4_32a(x[0], x[1], x[2], 0.0);
+    }
+};
+
+// Wall records (setup): FP64 {x, y, z, m} and the FP32 test record.
+template <int ND>
+struct PackWall64 {
+    const double* x;
+    const double* m;
+    double4_32a* pos;
+    float4* test;
+    GridDesc g;
+    double cs32;
+    __device__ void operator()(int i, int s) const {
+        double y[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; ++d) y[d] = x[(size_t)i * ND + d];
+        pos[s] = make_double4_32a(y[0], y[1], y[2], m[i]);
+        test[s] = test_record<ND>(y, g, cs32);
+    }
+};
+
 // ------------------------------------------------------------------------------------------
-// Adami pressure extrapolation (dummy_particles.jl:489-569, 586-606, 637-672), one thread per
-// wall slot, gathering its fluid neighbours in PointNeighbors order.
+// Adami pressure extrapolation (dummy_particles.jl:489-569, 586-606, 637-672): one lane per
+// wall slot gathers its fluid neighbours in PointNeighbors order.
 // ------------------------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(128) k_adami64(Phys P, GridDesc g, int nw,
-                                                 const double4_32a* __restrict__ wpos,
+__global__ void __launch_bounds__(128) k_adami64(Phys P, GridDesc g, float cs32f, float sr2f,
+                                                 int nw, const double4_32a* __restrict__ wpos,
+                                                 const float4* __restrict__ wtest,
                                                  const int* __restrict__ wskey,
-                                                 double2* __restrict__ wstate,
+                                                 double4_32a* __restrict__ wstate,
                                                  double* __restrict__ wvol,
+                                                 const float4* __restrict__ ftest,
                                                  const double4_32a* __restrict__ fpos,
                                                  const double4_32a* __restrict__ fvel,
                                                  const int* __restrict__ fstart) {
+    __shared__ WarpSmem smw[4];
+    WarpSmem& sm = smw[threadIdx.x >> 5];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nw) return;
-    const double4_32a xw = wpos[w];
+    const bool active = w < nw;
+    const int wi = active ? w : 0;
+    const double4_32a xw = wpos[wi];
+    const float4 tw = wtest[wi];
     int c[3];
-    key_to_coords(wskey[w], g, c);
+    key_to_coords(wskey[wi], g, c);
     double Ps = 0.0, V = 0.0;
-    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            const int b1 = fstart[row + 3];
-            for (int b = fstart[row]; b < b1; ++b) {
-                const double4_32a xb = fpos[b];
-                const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
-                const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
-                const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-                if (d2 > P.sr2) continue;
-                const double r = sqrt(d2);
-                const double rho_f = fvel[b].w;
-                double hp = __dadd_rn(__dmul_rn(P.g[0], __dmul_rn(rho_f, pd0)),
-                                      __dmul_rn(P.g[1], __dmul_rn(rho_f, pd1)));
-                if (ND == 3) hp = __dadd_rn(hp, __dmul_rn(P.g[2], __dmul_rn(rho_f, pd2)));
-                const double sum = ((P.p_off + xb.w) + 0.0) + hp;
-                double W = 0.0;
-                if (r < P.two_h) {
-                    const double q = r * P.h_inv;
-                    const double t = 1.0 - q / 2.0;
-                    const double t2 = t * t;
-                    W = (P.wc2_norm * (t2 * t2)) * (2.0 * q + 1.0);
-                }
-                Ps = __dadd_rn(Ps, __dmul_rn(sum, W));
-                V = __dadd_rn(V, W);
-            }
+    auto gather = [&](int e) {
+        const int b = e & kSlotMask;
+        const double4_32a xb = fpos[b];
+        const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
+        const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
+        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        if (d2 > P.sr2) return;
+        const double r = sqrt(d2);
+        const double rho_f = fvel[b].w;
+        double hp = __dadd_rn(__dmul_rn(P.g[0], __dmul_rn(rho_f, pd0)),
+                              __dmul_rn(P.g[1], __dmul_rn(rho_f, pd1)));
+        if (ND == 3) hp = __dadd_rn(hp, __dmul_rn(P.g[2], __dmul_rn(rho_f, pd2)));
+        const double sum = __dadd_rn(__dadd_rn(__dadd_rn(P.p_off, xb.w), 0.0), hp);
+        double W = 0.0;
+        if (r < P.two_h) {
+            const double q = __dmul_rn(r, P.h_inv);
+            const double t = 1.0 - q / 2.0;
+            const double t2 = __dmul_rn(t, t);
+            W = __dmul_rn(__dmul_rn(P.wc2_norm, __dmul_rn(t2, t2)),
+                          __dadd_rn(__dmul_rn(2.0, q), 1.0));
         }
-    }
+        Ps = __dadd_rn(Ps, __dmul_rn(sum, W));
+        V = __dadd_rn(V, W);
+    };
+    warp_neighbors<ND>(g, cs32f, active, c, tw, fstart, ftest, sr2f, sm, gather);
+    if (!active) return;
     if (V > 2.220446049250313e-16) Ps = Ps / V;
     if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
-    wstate[w] = make_double2(Ps, eos_inverse(Ps, P));
+    const double rho_w = eos_inverse(Ps, P);
+    wstate[w] = make_double4_32a(Ps, rho_w, fast_inv(rho_w), 0.0);
     wvol[w] = V;
 }
 
@@ -132,123 +180,118 @@ __global__ void __launch_bounds__(128) k_adami64(Phys P, GridDesc g, int nw,
 struct Update64 {
     double* dv;        // kick mode: dv_ode in source order (indexed by perm)
     const int* perm;
-    // integrate mode (ping-pong in slot order):
-    const double* tu;  // registers of the slot (already moved to slot order by the pack)
-    const double* tv;
+    // integrate mode (slot order, in place on the state written by this stage's pack):
     double* u_out;
     double* v_out;
-    double* tu_out;
-    double* tv_out;
+    double* tu;
+    double* tv;
     double A, B, dt;
     int first;
 };
 
 template <int ND, bool INTEGRATE>
-__global__ void __launch_bounds__(128) k_pair64(Phys P, GridDesc g, int nf,
+__global__ void __launch_bounds__(128, 4) k_pair64(Phys P, GridDesc g, float cs32f, float sr2f,
+                                                int nf, const float4* __restrict__ ftest,
                                                 const double4_32a* __restrict__ fpos,
                                                 const double4_32a* __restrict__ fvel,
-                                                const double* __restrict__ fmass,
+                                                const double2* __restrict__ faux,
                                                 const int* __restrict__ fstart,
                                                 const int* __restrict__ fskey,
+                                                const float4* __restrict__ wtest,
                                                 const double4_32a* __restrict__ wpos,
-                                                const double2* __restrict__ wstate,
+                                                const double4_32a* __restrict__ wstate,
                                                 const int* __restrict__ wstart, Update64 U) {
+    __shared__ WarpSmem smw[4];
+    WarpSmem& sm = smw[threadIdx.x >> 5];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nf) return;
-    const double4_32a pa = fpos[s];
-    const double4_32a va = fvel[s];
+    const bool active = s < nf;
+    const int si = active ? s : 0;
+    const double4_32a pa = fpos[si];
+    const double4_32a va = fvel[si];
+    const float4 ta = ftest[si];
     const double p_a = pa.w, rho_a = va.w;
     int c[3];
-    key_to_coords(fskey[s], g, c);
-    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
+    key_to_coords(fskey[si], g, c);
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            const int b1 = fstart[row + 3];
-            for (int b = fstart[row]; b < b1; ++b) {
-                const double4_32a pb = fpos[b];
-                const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
-                const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
-                const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-                if (d2 > P.sr2) continue;
-                const double r = sqrt(d2);
-                if (r < P.almostzero) continue;
-                const double4_32a vb = fvel[b];
-                const double m_b = fmass[b];
-                const double rho_b = vb.w;
-                // WendlandC2 kernel_deriv_div_r_unsafe * pos_diff
-                const double q = r * P.h_inv;
-                const double t = 1.0 - q / 2.0;
-                const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-                const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-                // pressure_acceleration_continuity_density
-                const double coef = (-m_b) * div_fast(p_a + pb.w, rho_a * rho_b);
-                dv0 += coef * g0;
-                dv1 += coef * g1;
-                if (ND == 3) dv2 += coef * g2;
-                const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
-                const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
-                if (P.visc) {
-                    double vr = vd0 * pd0 + vd1 * pd1;
-                    if (ND == 3) vr += vd2 * pd2;
-                    if (vr < 0.0) {
-                        const double rho_mean = (rho_a + rho_b) / 2.0;
-                        const double mu = div_fast(P.visc_h * vr, r * r + P.visc_eps_h2);
-                        const double num =
-                            ((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu);
-                        const double f = div_fast(num, rho_mean);
-                        dv0 += f * g0;
-                        dv1 += f * g1;
-                        if (ND == 3) dv2 += f * g2;
-                    }
-                }
-                double vg = vd0 * g0 + vd1 * g1;
-                if (ND == 3) vg += vd2 * g2;
-                drho += (div_fast(rho_a, rho_b) * m_b) * vg;
-                if (P.diff) {
-                    const double vol_b = div_fast(m_b, rho_b);
-                    const double pc = div_fast(2.0 * (rho_a - rho_b), r * r);
-                    double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
-                    if (ND == 3) pg += (pc * pd2) * g2;
-                    drho += P.diff_coef * (vol_b * pg);
-                }
+    auto ff = [&](int e) {
+        const int b = e & kSlotMask;
+        const double4_32a pb = fpos[b];
+        const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
+        const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
+        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        if (d2 > P.sr2) return;
+        const double r = sqrt(d2);
+        if (r < P.almostzero) return;
+        const double4_32a vb = fvel[b];
+        const double2 ab = faux[b];  // {m_b, fast_inv(rho_b)}
+        const double m_b = ab.x, rho_b = vb.w;
+        // WendlandC2 kernel_deriv_div_r_unsafe * pos_diff
+        const double q = r * P.h_inv;
+        const double t = 1.0 - q / 2.0;
+        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+        // pressure_acceleration_continuity_density
+        const double coef = (-m_b) * div_fast(p_a + pb.w, rho_a * rho_b);
+        dv0 += coef * g0;
+        dv1 += coef * g1;
+        if (ND == 3) dv2 += coef * g2;
+        const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
+        const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
+        if (P.visc) {
+            double vr = vd0 * pd0 + vd1 * pd1;
+            if (ND == 3) vr += vd2 * pd2;
+            if (vr < 0.0) {
+                const double rho_mean = (rho_a + rho_b) / 2.0;
+                const double mu = div_fast(P.visc_h * vr, r * r + P.visc_eps_h2);
+                const double num = ((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu);
+                const double f = div_fast(num, rho_mean);
+                dv0 += f * g0;
+                dv1 += f * g1;
+                if (ND == 3) dv2 += f * g2;
             }
         }
-    }
+        double vg = vd0 * g0 + vd1 * g1;
+        if (ND == 3) vg += vd2 * g2;
+        drho += ((rho_a * ab.y) * m_b) * vg;
+        if (P.diff) {
+            const double vol_b = m_b * ab.y;
+            const double pc = div_fast(2.0 * (rho_a - rho_b), r * r);
+            double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
+            if (ND == 3) pg += (pc * pd2) * g2;
+            drho += P.diff_coef * (vol_b * pg);
+        }
+    };
+    warp_neighbors<ND>(g, cs32f, active, c, ta, fstart, ftest, sr2f, sm, ff);
 
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion) ----
     double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            const int b1 = wstart[row + 3];
-            for (int b = wstart[row]; b < b1; ++b) {
-                const double4_32a pb = wpos[b];
-                const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
-                const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
-                const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-                if (d2 > P.sr2) continue;
-                const double r = sqrt(d2);
-                if (r < P.almostzero) continue;
-                const double2 sb = wstate[b];
-                const double m_b = pb.w, p_b = sb.x, rho_b = sb.y;
-                const double q = r * P.h_inv;
-                const double t = 1.0 - q / 2.0;
-                const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-                const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-                const double coef = (-m_b) * div_fast(p_a + p_b, rho_a * rho_b);
-                ew0 += coef * g0;
-                ew1 += coef * g1;
-                if (ND == 3) ew2 += coef * g2;
-                double vg = va.x * g0 + va.y * g1;
-                if (ND == 3) vg += va.z * g2;
-                erho += (div_fast(rho_a, rho_b) * m_b) * vg;
-            }
-        }
-    }
+    auto fw = [&](int e) {
+        const int b = e & kSlotMask;
+        const double4_32a pb = wpos[b];
+        const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
+        const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
+        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        if (d2 > P.sr2) return;
+        const double r = sqrt(d2);
+        if (r < P.almostzero) return;
+        const double4_32a sb = wstate[b];  // {p, rho, fast_inv(rho), 0}
+        const double m_b = pb.w, p_b = sb.x, rho_b = sb.y;
+        const double q = r * P.h_inv;
+        const double t = 1.0 - q / 2.0;
+        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+        const double coef = (-m_b) * div_fast(p_a + p_b, rho_a * rho_b);
+        ew0 += coef * g0;
+        ew1 += coef * g1;
+        if (ND == 3) ew2 += coef * g2;
+        double vg = va.x * g0 + va.y * g1;
+        if (ND == 3) vg += va.z * g2;
+        erho += ((rho_a * sb.z) * m_b) * vg;
+    };
+    warp_neighbors<ND>(g, cs32f, active, c, ta, wstart, wtest, sr2f, sm, fw);
+    if (!active) return;
 
     // dv = ((0 + S_ff) + S_fw) + g ;  drho = S_ff + S_fw
     double k[4];
@@ -263,21 +306,20 @@ __global__ void __launch_bounds__(128) k_pair64(Phys P, GridDesc g, int nf,
         for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
     } else {
         // CarpenterKennedy2N54 stage: tmp = A*tmp + dt*k ; u = u + B*tmp (du = v at stage start)
-        // state row d of the slot: velocity components, then the density (record .w)
         const double va_arr[4] = {va.x, va.y, ND == 3 ? va.z : va.w, va.w};
         const double xa_arr[3] = {pa.x, pa.y, pa.z};
 #pragma unroll
         for (int d = 0; d <= ND; ++d) {
             const double kv = k[d];
             double tv = U.first ? U.dt * kv : fma(U.dt, kv, U.A * U.tv[(size_t)s * (ND + 1) + d]);
-            U.tv_out[(size_t)s * (ND + 1) + d] = tv;
+            U.tv[(size_t)s * (ND + 1) + d] = tv;
             U.v_out[(size_t)s * (ND + 1) + d] = fma(U.B, tv, va_arr[d]);
         }
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
             const double ku = va_arr[d];
             double tu = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
-            U.tu_out[(size_t)s * ND + d] = tu;
+            U.tu[(size_t)s * ND + d] = tu;
             U.u_out[(size_t)s * ND + d] = fma(U.B, tu, xa_arr[d]);
         }
     }
@@ -309,26 +351,15 @@ __global__ void k_count64(GridDesc g, double sr2, int n, const double4_32a* __re
     out[qperm[s]] = cnt;
 }
 
-// Wall record pack (setup): caller order -> slot order.
-template <int ND>
-struct PackWall64 {
-    const double* x;
-    const double* m;
-    double4_32a* pos;
-    __device__ void operator()(int i, int s) const {
-        double y[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < ND; ++d) y[d] = x[(size_t)i * ND + d];
-        pos[s] = make_double4_32a(y[0], y[1], y[2], m[i]);
-    }
-};
-
 // ------------------------------------------------------------------------------------------
 // Host launchers
 // ------------------------------------------------------------------------------------------
 namespace {
 inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
-}
+// FP32 prefilter bound: (2h)^2 widened by 1e-5 so that no FP64 neighbour is dropped.
+inline float filter_sr2(const tp_handle* h) { return (float)(h->phys.sr2 * (1.0 + 1e-5)); }
+inline float cs32f(const tp_handle* h) { return (float)h->grid.cs; }
+}  // namespace
 
 template <int ND>
 static void pack_fluid64(tp_handle* h, const double* u, const double* v, const double* m,
@@ -344,11 +375,14 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
         pk.tu_out = dst->tu;
         pk.tv_out = (double*)dst->tv;
         pk.id_out = dst->id;
+        pk.m_out = (double*)dst->m;
     }
+    pk.test = h->f_test;
     pk.pos = (double4_32a*)h->f_pos;
     pk.vel = (double4_32a*)h->f_vel;
-    // Integrator: the slot-ordered mass array of the next state doubles as the record mass.
-    pk.mass = dst ? (double*)dst->m : (double*)h->f_mass;
+    pk.aux = (double2*)h->f_aux;
+    pk.g = h->grid;
+    pk.cs32 = (double)(float)h->grid.cs;
     pk.P = h->phys;
     const int n = (int)h->cfg.n_fluid;
     k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n, h->f_perm,
@@ -357,24 +391,12 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
 
 void fp64_pack(tp_handle* h, const double* u, const double* v, const double* m,
                const PhysState* src, PhysState* dst) {
+    if (h->cfg.n_fluid == 0) return;
     if (h->cfg.ndims == 2)
         pack_fluid64<2>(h, u, v, m, src, dst);
     else
         pack_fluid64<3>(h, u, v, m, src, dst);
 }
-
-// Positions only (p = 0): neighbour-count diagnostics.
-template <int ND>
-struct PackPos64 {
-    const double* u;
-    double4_32a* pos;
-    __device__ void operator()(int i, int s) const {
-        double x[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
-        pos[s] = make_double4_32a(x[0], x[1], x[2], 0.0);
-    }
-};
 
 void fp64_pack_pos(tp_handle* h, const double* u) {
     const int n = (int)h->cfg.n_fluid;
@@ -390,16 +412,16 @@ void fp64_pack_pos(tp_handle* h, const double* u) {
     }
 }
 
-// Wall records: `out` is h->w_pos (FP64 form) or h->w_pos64 (diagnostic copy).
-void fp64_pack_wall(tp_handle* h, const double* x, const double* m, void* out) {
+void fp64_pack_wall(tp_handle* h, const double* x, const double* m) {
     const int n = (int)h->cfg.n_wall;
     if (n == 0) return;
+    const double cs32 = (double)(float)h->grid.cs;
     if (h->cfg.ndims == 2) {
-        PackWall64<2> pk{x, m, (double4_32a*)out};
+        PackWall64<2> pk{x, m, (double4_32a*)h->w_pos, h->w_test, h->grid, cs32};
         k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
                                                           h->w_perm, h->w_skey, pk);
     } else {
-        PackWall64<3> pk{x, m, (double4_32a*)out};
+        PackWall64<3> pk{x, m, (double4_32a*)h->w_pos, h->w_test, h->grid, cs32};
         k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->w_tmp, h->w_key, h->w_start, n,
                                                           h->w_perm, h->w_skey, pk);
     }
@@ -408,23 +430,26 @@ void fp64_pack_wall(tp_handle* h, const double* x, const double* m, void* out) {
 void fp64_adami(tp_handle* h) {
     const int nw = (int)h->cfg.n_wall;
     if (nw == 0) return;
+    auto run = [&](auto ndc) {
+        constexpr int ND = decltype(ndc)::value;
+        k_adami64<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
+            h->phys, h->grid, cs32f(h), filter_sr2(h), nw, (const double4_32a*)h->w_pos,
+            h->w_test, h->w_skey, (double4_32a*)h->w_state, h->w_vol, h->f_test,
+            (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->f_start);
+    };
     if (h->cfg.ndims == 2)
-        k_adami64<2><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys, h->grid, nw, (const double4_32a*)h->w_pos, h->w_skey, (double2*)h->w_state,
-            h->w_vol, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->f_start);
+        run(std::integral_constant<int, 2>{});
     else
-        k_adami64<3><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys, h->grid, nw, (const double4_32a*)h->w_pos, h->w_skey, (double2*)h->w_state,
-            h->w_vol, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->f_start);
+        run(std::integral_constant<int, 3>{});
 }
 
 template <int ND, bool INTEG>
-static void launch_pair64(tp_handle* h, const double* fmass, const Update64& U) {
+static void launch_pair64(tp_handle* h, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
     k_pair64<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
-        h->phys, h->grid, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, fmass,
-        h->f_start, h->f_skey, (const double4_32a*)h->w_pos, (const double2*)h->w_state,
-        h->w_start, U);
+        h->phys, h->grid, cs32f(h), filter_sr2(h), nf, h->f_test, (const double4_32a*)h->f_pos,
+        (const double4_32a*)h->f_vel, (const double2*)h->f_aux, h->f_start, h->f_skey, h->w_test,
+        (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, h->w_start, U);
 }
 
 void fp64_pair_kick(tp_handle* h, double* dv) {
@@ -433,30 +458,28 @@ void fp64_pair_kick(tp_handle* h, double* dv) {
     U.dv = dv;
     U.perm = h->f_perm;
     if (h->cfg.ndims == 2)
-        launch_pair64<2, false>(h, (const double*)h->f_mass, U);
+        launch_pair64<2, false>(h, U);
     else
-        launch_pair64<3, false>(h, (const double*)h->f_mass, U);
+        launch_pair64<3, false>(h, U);
 }
 
-// Stage update in place on the slot-ordered state `st` written by the pack of this stage.
+// Stage update in place on the slot-ordered state `out` written by the pack of this stage.
 void fp64_pair_stage(tp_handle* h, PhysState& out, double A, double B, double dt, int first) {
     if (h->cfg.n_fluid == 0) return;
     Update64 U{};
     U.perm = h->f_perm;
-    U.tu = out.tu;
-    U.tv = (const double*)out.tv;
     U.u_out = out.u;
     U.v_out = (double*)out.v;
-    U.tu_out = out.tu;
-    U.tv_out = (double*)out.tv;
+    U.tu = out.tu;
+    U.tv = (double*)out.tv;
     U.A = A;
     U.B = B;
     U.dt = dt;
     U.first = first;
     if (h->cfg.ndims == 2)
-        launch_pair64<2, true>(h, (const double*)out.m, U);
+        launch_pair64<2, true>(h, U);
     else
-        launch_pair64<3, true>(h, (const double*)out.m, U);
+        launch_pair64<3, true>(h, U);
 }
 
 void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf) {
@@ -471,10 +494,10 @@ void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf) {
         if (nnb_fw && nf)
             k_count64<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
                 h->grid, sr2, nf, (const double4_32a*)h->f_pos, h->f_skey, h->f_perm,
-                (const double4_32a*)h->w_pos64, h->w_start, nnb_fw);
+                (const double4_32a*)h->w_pos, h->w_start, nnb_fw);
         if (nnb_wf && nw)
             k_count64<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
-                h->grid, sr2, nw, (const double4_32a*)h->w_pos64, h->w_skey, h->w_perm,
+                h->grid, sr2, nw, (const double4_32a*)h->w_pos, h->w_skey, h->w_perm,
                 (const double4_32a*)h->f_pos, h->f_start, nnb_wf);
     };
     if (h->cfg.ndims == 2)

@@ -53,9 +53,10 @@ struct tp_handle {
     int scan_blocks = 0;
 
     // ---- fluid records (slot order) ----
-    void* f_pos = nullptr;   // double4 / float4
-    void* f_vel = nullptr;   // double4 / float4
-    void* f_mass = nullptr;  // double / float
+    float4* f_test = nullptr;  // {ox, oy, oz, cx}: FP32 neighbour filter (both forms)
+    void* f_pos = nullptr;     // FP64 form / diagnostics: double4 {x, y, z, p}
+    void* f_vel = nullptr;     // FP64: double4 {v, rho};  FP32: float4 {v, rho - rho0}
+    void* f_aux = nullptr;     // FP64: double2 {m, 1/rho}; FP32: float2 {p, m}
 
     // ---- fluid masses in caller order (FP64) ----
     double* m_f = nullptr;
@@ -66,9 +67,9 @@ struct tp_handle {
     int* w_perm = nullptr;   // slot -> caller index
     int* w_skey = nullptr;
     int* w_start = nullptr;  // ncells + 1
-    void* w_pos = nullptr;   // double4 / float4 {x.., m}
-    void* w_pos64 = nullptr; // double4 {x, y, z, m} (diagnostics in both forms)
-    void* w_state = nullptr; // double2 / float2 {p, rho}
+    void* w_pos = nullptr;    // double4 {x, y, z, m} (both forms)
+    float4* w_test = nullptr; // {ox, oy, oz, cx}
+    void* w_state = nullptr;  // FP64: double4 {p, rho, 1/rho, 0}; FP32: float4 {p, rho-rho0, m, 0}
     double* w_vol = nullptr;
 
     // ---- integrator ping-pong state ----
