@@ -202,6 +202,30 @@ tp_status tp_enable_timing(tp_handle* h, int32_t enable);
 /* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
 int64_t tp_kernel_launches(const tp_handle* h);
 
+/*
+ * Cell sort without any device allocation.  This entry point has no counterpart in the
+ * reference: it serves callers that must not allocate device memory -- a host that owns all
+ * device memory through its own pool (a Julia process running CUDA.jl) or a fixed-budget
+ * real-time loop -- and gives them the neighbour-search counting sort of this library:
+ * cell[i] and order[k] exactly as tp_nhs_debug returns them, for `n` particles with
+ * coordinates u (ndims, n) on the grid that `cfg` describes (ndims, smoothing_length,
+ * min_corner, max_corner; the other fields are ignored).  u, cell and order are device
+ * pointers; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * All scratch lives in one fixed device array owned by the library (about 10 MB, held by every
+ * GPU that loads the library until the process exits): at most TP_NOALLOC_MAX_PARTICLES
+ * particles and TP_NOALLOC_MAX_CELLS grid cells (padding included), larger requests return
+ * TP_ERR_CAPACITY before any GPU work.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call before any
+ * stream capture.  Calls share the scratch: the call clears what must start at zero, and
+ * calls that overlap on the GPU race, so serialise them.  The call returns after the sort has
+ * finished (it synchronises `stream`) and reports TP_ERR_OUT_OF_GRID / TP_ERR_NONFINITE
+ * directly.  It calls no cudaMalloc, cudaFree or allocating library routine.
+ */
+#define TP_NOALLOC_MAX_PARTICLES 262144
+#define TP_NOALLOC_MAX_CELLS 524288
+tp_status tp_cell_sort_noalloc(const tp_config* cfg, const double* u, int64_t n, int32_t* cell,
+                               int32_t* order, void* stream);
+
 /* Last error message of the handle (or of the last failed tp_create when h is NULL). */
 const char* tp_last_error(const tp_handle* h);
 

@@ -97,8 +97,13 @@ PROTOTYPES = [
     ("tp_phase_times", c_int32, [c_void_p, POINTER(c_double), c_int32]),
     ("tp_enable_timing", c_int32, [c_void_p, c_int32]),
     ("tp_kernel_launches", c_int64, [c_void_p]),
+    ("tp_cell_sort_noalloc", c_int32,
+     [POINTER(TpConfig), c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     ("tp_last_error", c_char_p, [c_void_p]),
 ]
+
+TP_NOALLOC_MAX_PARTICLES = 262144
+TP_NOALLOC_MAX_CELLS = 524288
 
 _LIB = None
 
