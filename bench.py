@@ -117,6 +117,20 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
+def replica_value(dist, ms_local, particles, steps, device="cpu"):
+    """Whole-job particle-steps/s of independent replicas: every rank advanced `particles`
+    particles for `steps` steps; the job time is the slowest rank's (max over ranks)."""
+    import torch
+
+    world = dist.get_world_size() if dist is not None else 1
+    ms = float(ms_local)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return particles * steps * world / (ms / 1e3), ms
+
+
 def make_case(pkg, cfg, precision, device):
     tank, eos = pkg.dam_break(3, cfg["dx"], cfg["fluid"], cfg["tank"], n_layers=cfg["layers"])
     semi = pkg.dam_break_semidiscretization(tank, eos, 1.75 * cfg["dx"], precision=precision,
@@ -350,12 +364,7 @@ def main():
     ph = (ctypes.c_double * 3)()
     lib.tp_phase_times(semi._handle, ph, 3)
     lib.tp_enable_timing(semi._handle, 0)
-    ms_max = ms
-    if dist:
-        t = torch.tensor([ms], device=semi.device, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = ntot * args.steps * world / (ms_max / 1e3)
+    value, ms_max = replica_value(dist, ms, ntot, args.steps, semi.device)
     stages = 5 * args.steps
     bf, bw = BYTES_STAGE["float64"]
     step_bytes = 5 * (nf * bf + nw * bw)
