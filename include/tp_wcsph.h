@@ -199,6 +199,15 @@ tp_status tp_sync(tp_handle* h);
 int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n);
 tp_status tp_enable_timing(tp_handle* h, int32_t enable);
 
+/*
+ * Neighbour-list skin of tp_integrate_ck2n54 (default 0.1): candidate lists are built at radius
+ * 2h (1 + skin) and reused across Runge-Kutta stages until some particle has moved more than
+ * skin * h since the last rebuild (checked on the device every stage); pairs are still decided
+ * exactly with |x_a - x_b|^2 <= (2h)^2 at each stage, so the skin changes speed, not results.
+ * 0 rebuilds the cell list and the lists at every stage, as the reference's update_nhs! does.
+ */
+tp_status tp_set_skin(tp_handle* h, double skin);
+
 /* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
 int64_t tp_kernel_launches(const tp_handle* h);
 

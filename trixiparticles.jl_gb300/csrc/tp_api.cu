@@ -8,7 +8,7 @@
 #include <vector>
 
 #include "tp_api_internal.h"
-#include "tp_nhs.cuh"
+#include "tp_lists.cuh"
 
 using namespace tp;
 
@@ -311,36 +311,116 @@ bool setup_grid(tp_handle* h, std::string& msg) {
     return true;
 }
 
-tp_status scan_cells(tp_handle* h, int* count, int* start, int* cursor) {
-    const int n = h->grid.ncells;
-    const int nb = nblk(n, kScanTile);
-    k_scan_reduce<<<nb, kScanThreads, 0, h->stream>>>(count, n, h->scan_partial);
-    k_scan_partials<<<1, kScanThreads, 0, h->stream>>>(h->scan_partial, nb);
-    k_scan_final<<<nb, kScanThreads, 0, h->stream>>>(count, n, h->scan_partial, start, cursor);
-    TP_LAUNCHED(h, "cell scan");
-    h->launches += 3;
-    return TP_OK;
-}
 
 // Counting sort of `n` particles with coordinates `u` into key/tmp/start (no packing yet).
-tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start) {
+// `gate`: device rebuild gate (null = always).  `maxcell`: if non-null, receives (atomicMax) the
+// largest cell occupancy of this sort.
+tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start,
+                         const unsigned* gate = nullptr, int* maxcell = nullptr) {
     if (n > 0) {
         if (h->cfg.ndims == 2)
             k_cell_keys<2><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
-                                                                 h->d_err);
+                                                                 h->d_err, gate);
         else
             k_cell_keys<3><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
-                                                                 h->d_err);
+                                                                 h->d_err, gate);
         TP_LAUNCHED(h, "cell keys");
         h->launches += 1;
+        if (maxcell) {
+            k_max_count<<<256, 256, 0, h->stream>>>(h->f_count, h->grid.ncells, maxcell);
+            TP_LAUNCHED(h, "max cell count");
+            h->launches += 1;
+        }
     }
-    tp_status st = scan_cells(h, h->f_count, start, h->f_cursor);
-    if (st != TP_OK) return st;
+    const int nc = h->grid.ncells;
+    const int nb = nblk(nc, kScanTile);
+    k_scan_reduce<<<nb, kScanThreads, 0, h->stream>>>(h->f_count, nc, h->scan_partial, gate);
+    k_scan_partials<<<1, kScanThreads, 0, h->stream>>>(h->scan_partial, nb, gate);
+    k_scan_final<<<nb, kScanThreads, 0, h->stream>>>(h->f_count, nc, h->scan_partial, start,
+                                                     h->f_cursor, gate);
+    TP_LAUNCHED(h, "cell scan");
+    h->launches += 3;
     if (n > 0) {
-        k_scatter<<<nblk(n, 256), 256, 0, h->stream>>>(key, n, h->f_cursor, tmp);
+        k_scatter<<<nblk(n, 256), 256, 0, h->stream>>>(key, n, h->f_cursor, tmp, gate);
         TP_LAUNCHED(h, "cell scatter");
         h->launches += 1;
     }
+    return TP_OK;
+}
+
+// List capacity for a radius 2h (1 + skin) from the largest cell occupancy: the neighbour count
+// is at most (ball volume / cell volume) * occupancy; 30 % margin, rounded to 32.
+int list_cap(int nd, double skin, int maxcell) {
+    const double q = 1.0 + skin;
+    const double ball = (nd == 3) ? (4.0 / 3.0) * 3.141592653589793 * q * q * q
+                                  : 3.141592653589793 * q * q;
+    const double c = std::ceil(1.3 * ball * (double)std::max(maxcell, 1)) + 32.0;
+    return ((int)c + 31) / 32 * 32;
+}
+
+// Makes the list buffers large enough for fluid coordinates `u` (one host sync).
+tp_status ensure_lists(tp_handle* h, const double* u) {
+    const int nf = (int)h->cfg.n_fluid, nw = (int)h->cfg.n_wall;
+    TP_CUDA(h, cudaMemsetAsync(h->d_max, 0, sizeof(int), h->stream));
+    int maxcell_f = 0;
+    if (nf > 0) {
+        if (h->cfg.ndims == 2)
+            k_cell_keys<2><<<nblk(nf, 256), 256, 0, h->stream>>>(u, nf, h->grid, h->f_key,
+                                                                  h->f_count, h->d_err);
+        else
+            k_cell_keys<3><<<nblk(nf, 256), 256, 0, h->stream>>>(u, nf, h->grid, h->f_key,
+                                                                  h->f_count, h->d_err);
+        k_max_count<<<256, 256, 0, h->stream>>>(h->f_count, h->grid.ncells, h->d_max);
+        TP_LAUNCHED(h, "list sizing");
+        h->launches += 2;
+        TP_CUDA(h, cudaMemsetAsync(h->f_count, 0, (size_t)h->grid.ncells * sizeof(int), h->stream));
+        TP_CUDA(h, cudaMemcpyAsync(h->h_err + 1, h->d_max, sizeof(int), cudaMemcpyDeviceToHost,
+                                   h->stream));
+        TP_CUDA(h, cudaStreamSynchronize(h->stream));
+        maxcell_f = h->h_err[1];
+    }
+    const int nd = h->cfg.ndims;
+    const int cff = list_cap(nd, h->skin, maxcell_f);
+    const int cfw = list_cap(nd, h->skin, h->maxcell_w);
+    const int cwf = cff;
+    auto grow = [&](unsigned** buf, int* cap, int want, int n) -> cudaError_t {
+        if (*cap >= want && *buf) return cudaSuccess;
+        if (*buf) cudaFree(*buf);
+        *buf = nullptr;
+        *cap = 0;
+        cudaError_t e = dalloc(buf, (size_t)want * (size_t)std::max(n, 1));
+        if (e == cudaSuccess) *cap = want;
+        return e;
+    };
+    TP_CUDA(h, grow(&h->l_ff, &h->cap_ff, cff, nf));
+    TP_CUDA(h, grow(&h->l_fw, &h->cap_fw, cfw, nf));
+    TP_CUDA(h, grow(&h->l_wf, &h->cap_wf, cwf, nw));
+    return TP_OK;
+}
+
+// (Re)builds the fluid-fluid, fluid-wall and wall-fluid lists at radius 2h (1 + skin), gated.
+tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
+    const int nf = (int)h->cfg.n_fluid, nw = (int)h->cfg.n_wall;
+    const double r = 2.0 * h->cfg.smoothing_length * (1.0 + skin);
+    const float r2f = (float)(r * r * (1.0 + 1e-5));
+    const float cs = (float)h->grid.cs;
+    auto run = [&](auto ndc) {
+        constexpr int ND = decltype(ndc)::value;
+        if (nf > 0)
+            k_build_fluid_lists<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
+                h->grid, cs, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_start,
+                h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate);
+        if (nw > 0)
+            k_build_wall_lists<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
+                h->grid, cs, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_start, h->l_wf,
+                h->c_wf, h->cap_wf, h->d_err, gate);
+    };
+    if (h->cfg.ndims == 2)
+        run(std::integral_constant<int, 2>{});
+    else
+        run(std::integral_constant<int, 3>{});
+    TP_LAUNCHED(h, "list build");
+    h->launches += (nf > 0) + (nw > 0);
     return TP_OK;
 }
 
@@ -379,9 +459,14 @@ void finish_timing(tp_handle* h) {
 
 tp_status ensure_state(tp_handle* h) {
     if (h->st[0].u) return TP_OK;
+    if (!h->x_build) TP_CUDA(h, dalloc(&h->x_build, (size_t)h->cfg.n_fluid * h->cfg.ndims));
     const size_t nf = (size_t)h->cfg.n_fluid;
     const int nd = h->cfg.ndims;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
+                    h->d_max};
+    for (void* p : more)
+        if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
         PhysState& s = h->st[k];
         TP_CUDA(h, dalloc(&s.u, nf * nd));
@@ -400,19 +485,25 @@ tp_status ensure_state(tp_handle* h) {
     return TP_OK;
 }
 
-// One RHS evaluation of the cell-sorted pipeline from caller-ordered device arrays.
+// One RHS evaluation of the cell-sorted pipeline from caller-ordered device arrays:
+// sort + pack, exact lists (no skin), Adami.  The pair pass follows in the caller.
 tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
     const int nf = (int)h->cfg.n_fluid;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    tp_status st = ensure_lists(h, u);
+    if (st != TP_OK) return st;
+    if (!h->x_build) TP_CUDA(h, dalloc(&h->x_build, (size_t)std::max(nf, 1) * h->cfg.ndims));
     mark(h, 0);
-    tp_status st = sort_particles(h, u, nf, h->f_key, h->f_tmp, h->f_start);
+    st = sort_particles(h, u, nf, h->f_key, h->f_tmp, h->f_start);
     if (st != TP_OK) return st;
     if (f32)
-        fp32_pack(h, u, v, h->m_f, nullptr, nullptr);
+        fp32_pack(h, u, v, h->m_f, nullptr, nullptr, nullptr);
     else if (nf > 0)
-        fp64_pack(h, u, v, h->m_f, nullptr, nullptr);
+        fp64_pack(h, u, v, h->m_f, nullptr, nullptr, nullptr);
     TP_LAUNCHED(h, "pack");
     h->launches += (nf > 0);
+    st = build_lists(h, 0.0, nullptr);
+    if (st != TP_OK) return st;
     mark(h, 1);
     if (f32)
         fp32_adami(h);
@@ -501,13 +592,22 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->w_test, nw));
     A(dalloc((double4_32a**)&h->w_state, nw));
     A(dalloc(&h->w_vol, nw));
+    A(dalloc(&h->c_ff, nf));
+    A(dalloc(&h->c_fw, nf));
+    A(dalloc(&h->c_wf, nw));
+    A(dalloc(&h->gate, 4));
+    A(dalloc(&h->d_max, 1));
     h->red_blocks = 256;
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
     A(dalloc(&h->d_err, 1));
-    A(cudaMallocHost((void**)&h->h_err, sizeof(int)));
+    A(cudaMallocHost((void**)&h->h_err, 4 * sizeof(int)));
+    A(cudaMallocHost((void**)&h->h_gate, 4 * sizeof(unsigned)));
     if (e == cudaSuccess) e = cudaMemset(h->f_count, 0, nc * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->w_start, 0, (nc + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->c_ff, 0, std::max<size_t>(nf, 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->c_fw, 0, std::max<size_t>(nf, 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->c_wf, 0, std::max<size_t>(nw, 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         g_create_error = std::string("device allocation failed: ") + cudaGetErrorString(e);
@@ -528,6 +628,10 @@ tp_status tp_destroy(tp_handle* h) {
                     h->w_state, h->w_vol,   h->red_partial, h->d_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
+                    h->d_max};
+    for (void* p : more)
+        if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
         PhysState& s = h->st[k];
         void* q[] = {s.u, s.tu, s.v, s.tv, s.m, s.id};
@@ -535,6 +639,7 @@ tp_status tp_destroy(tp_handle* h) {
             if (p) cudaFree(p);
     }
     if (h->h_err) cudaFreeHost(h->h_err);
+    if (h->h_gate) cudaFreeHost(h->h_gate);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
     delete h;
     return TP_OK;
@@ -551,8 +656,14 @@ tp_status tp_set_wall(tp_handle* h, const double* x_wall, const double* m_wall) 
     const int nw = (int)h->cfg.n_wall;
     if (nw > 0 && (!x_wall || !m_wall))
         return fail(h, TP_ERR_ARGUMENT, "tp_set_wall: null coordinates or masses");
-    tp_status st = sort_particles(h, x_wall, nw, h->w_key, h->w_tmp, h->w_start);
+    TP_CUDA(h, cudaMemsetAsync(h->d_max, 0, sizeof(int), h->stream));
+    tp_status st = sort_particles(h, x_wall, nw, h->w_key, h->w_tmp, h->w_start, nullptr,
+                                  h->d_max);
     if (st != TP_OK) return st;
+    TP_CUDA(h, cudaMemcpyAsync(h->h_err + 1, h->d_max, sizeof(int), cudaMemcpyDeviceToHost,
+                               h->stream));
+    TP_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->maxcell_w = nw > 0 ? h->h_err[1] : 0;
     if (nw > 0) {
         fp64_pack_wall(h, x_wall, m_wall);
         if (h->cfg.precision == TP_PRECISION_FP32) fp32_init_wall_state(h);
@@ -669,18 +780,43 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     TP_LAUNCHED(h, "integrator load");
     h->launches += f32 ? 2 : 1;
 
+    st = ensure_lists(h, u_ode);
+    if (st != TP_OK) return st;
+    // Rebuild gate: force the first rebuild of this call; threshold = skin * h.
+    h->h_gate[0] = 1u;
+    h->h_gate[1] = 0u;
+    {
+        const float half = (float)(h->skin * h->cfg.smoothing_length);
+        std::memcpy(&h->h_gate[2], &half, sizeof(float));
+    }
+    TP_CUDA(h, cudaMemcpyAsync(h->gate, h->h_gate, 3 * sizeof(unsigned), cudaMemcpyHostToDevice,
+                               h->stream));
+
     for (int64_t step = 0; step < n_steps; ++step) {
         for (int stage = 0; stage < 5; ++stage) {
             PhysState& src = h->st[h->cur];
             PhysState& dst = h->st[1 - h->cur];
             mark(h, 0);
-            st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start);
+            // displacement since the last rebuild (slot order of src = order of x_build)
+            TP_CUDA(h, cudaMemsetAsync(h->gate + 1, 0, sizeof(unsigned), h->stream));
+            if (nd == 2)
+                k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build, nf,
+                                                                         h->gate);
+            else
+                k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build, nf,
+                                                                         h->gate);
+            h->launches += 1;
+            st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);
             if (st != TP_OK) return st;
             if (f32)
-                fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst);
+                fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst, h->gate);
             else
-                fp64_pack(h, src.u, (const double*)src.v, (const double*)src.m, &src, &dst);
+                fp64_pack(h, src.u, (const double*)src.v, (const double*)src.m, &src, &dst,
+                          h->gate);
             TP_LAUNCHED(h, "pack");
+            h->launches += 1;
+            st = build_lists(h, h->skin, h->gate);
+            if (st != TP_OK) return st;
             mark(h, 1);
             if (f32)
                 fp32_adami(h);
@@ -694,7 +830,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
                 fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
             TP_LAUNCHED(h, "pair stage");
             mark(h, 3);
-            h->launches += 2 + (h->cfg.n_wall > 0);
+            h->launches += 1 + (h->cfg.n_wall > 0);
             h->cur = 1 - h->cur;
         }
     }
@@ -815,6 +951,10 @@ tp_status tp_sync(tp_handle* h) {
         TP_CUDA(h, cudaMemset(h->d_err, 0, sizeof(int)));
         if (bits & TP_ERRBIT_NONFINITE)
             return fail(h, TP_ERR_NONFINITE, "a particle coordinate became NaN or Inf");
+        if (bits & TP_ERRBIT_CAPACITY)
+            return fail(h, TP_ERR_CAPACITY,
+                        "a neighbour list overflowed its capacity (particles were compressed "
+                        "far beyond the densest cell seen when the lists were sized)");
         return fail(h, TP_ERR_OUT_OF_GRID,
                     "a particle left the FullGridCellList bounding box (its cell was clamped)");
     }
@@ -828,6 +968,13 @@ int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n) {
 }
 
 int64_t tp_kernel_launches(const tp_handle* h) { return h ? (int64_t)h->launches : 0; }
+
+tp_status tp_set_skin(tp_handle* h, double skin) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (!(skin >= 0.0 && skin <= 1.0)) return fail(h, TP_ERR_ARGUMENT, "skin must be in [0, 1]");
+    h->skin = skin;
+    return TP_OK;
+}
 
 tp_status tp_enable_timing(tp_handle* h, int32_t enable) {
     if (!h) return TP_ERR_ARGUMENT;

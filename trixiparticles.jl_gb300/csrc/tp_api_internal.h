@@ -9,7 +9,7 @@ namespace tp {
 
 // FP64 drop-in form (tp_fp64.cu)
 void fp64_pack(tp_handle* h, const double* u, const double* v, const double* m,
-               const PhysState* src, PhysState* dst);
+               const PhysState* src, PhysState* dst, const unsigned* gate);
 void fp64_pack_wall(tp_handle* h, const double* x, const double* m);
 void fp64_pack_pos(tp_handle* h, const double* u);
 void fp64_adami(tp_handle* h);
@@ -19,7 +19,7 @@ void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf);
 
 // FP32 precision form (tp_fp32.cu)
 void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
-               const PhysState* src, PhysState* dst);
+               const PhysState* src, PhysState* dst, const unsigned* gate);
 void fp32_init_wall_state(tp_handle* h);
 void fp32_adami(tp_handle* h);
 void fp32_pair_kick(tp_handle* h, double* dv);

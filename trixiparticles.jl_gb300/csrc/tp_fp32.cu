@@ -1,10 +1,11 @@
 // tp_fp32.cu — FP32 precision form of the WCSPH right-hand side (sm_103a).
 //
-// Same passes and neighbour order as the FP64 drop-in, with these precision choices:
-//   * positions enter the pair arithmetic as FP32 offsets inside their cell,
-//     o = x - floor(x / cs) * cs32 (FP64 on input, rounded once to FP32), so a pair difference
-//     is (o_a - o_b) + (cell_a - cell_b) * cs32 and stays accurate to FP32 relative precision of
-//     the smoothing length whatever the domain size;
+// Same passes, lists and neighbour order as the FP64 drop-in, with these precision choices:
+//   * positions enter the pair arithmetic as FP32 offsets inside a reference cell (the cell at
+//     the last list rebuild), o = x - (cmin + c) * cs32 (FP64 on input, rounded once to FP32),
+//     and a pair difference is (o_a - o_b) - (c_b - c_a) * cs32 with the cell offset taken from
+//     the list entry, so it stays accurate to FP32 relative precision of h whatever the domain
+//     size;
 //   * density is stored as the deviation rho - rho0 in FP32, so differences of densities and
 //     the Cole EOS, evaluated as B * expm1(gamma * log1p((rho - rho0) / rho0)), do not cancel;
 //   * per-particle sums (dv, drho, Adami pressure and volume) use Kahan-compensated FP32;
@@ -14,8 +15,7 @@
 //     and density registers are FP32.
 // The neighbour set is the FP32 one: |o_a - o_b + shift|^2 <= (2h)^2 evaluated in FP32.
 #include "tp_api_internal.h"
-#include "tp_nhs.cuh"
-#include "tp_warpnbr.cuh"
+#include "tp_lists.cuh"
 
 namespace tp {
 
@@ -40,18 +40,18 @@ __device__ __forceinline__ float eos32_inverse_dev(float p, const Phys32& P) {
     return P.rho0 * expm1f(log1pf((p - P.p_bg) / P.B) * P.inv_gamma);
 }
 
-// Difference o_a - o_b + shift of a queued candidate, recomputed exactly as the filter did.
+// o_a - o_b + (c_a - c_b) * cs from a list entry (same arithmetic as the list filter).
 template <int ND>
-__device__ __forceinline__ float pair_diff(float4 ta, float cxa, float cs, int e, float4 cb,
-                                           float& pdx, float& pdy, float& pdz) {
-    int dy, dz;
-    row_shift(e >> kSlotBits, dy, dz);
-    pdx = fmaf(cxa - cb.w, cs, ta.x) - cb.x;
-    pdy = (ta.y - (float)dy * cs) - cb.y;
-    float d2 = pdx * pdx + pdy * pdy;
+__device__ __forceinline__ float pair_diff(float4 ta, float cs, unsigned e, float4 cb, float& pdx,
+                                           float& pdy, float& pdz) {
+    int dx, dy, dz;
+    decode_cell_offset(e, dx, dy, dz);
+    pdx = fmaf(-(float)dx, cs, ta.x) - cb.x;
+    pdy = fmaf(-(float)dy, cs, ta.y) - cb.y;
+    float d2 = fmaf(pdy, pdy, pdx * pdx);
     pdz = 0.0f;
     if (ND == 3) {
-        pdz = (ta.z - (float)dz * cs) - cb.z;
+        pdz = fmaf(-(float)dz, cs, ta.z) - cb.z;
         d2 = fmaf(pdz, pdz, d2);
     }
     return d2;
@@ -72,13 +72,14 @@ struct Pack32 {
     float4* tv_out;
     int* id_out;
     float* m_out;
+    double* xb_out;
     float4* test;
     float4* vel;
     float2* aux;
     GridDesc g;
     double cs32, rho0;
     Phys32 P;
-    __device__ void operator()(int i, int s) const {
+    __device__ void operator()(int i, int s, int key, bool rebuild) const {
         double x[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
@@ -95,9 +96,14 @@ struct Pack32 {
             w.w = (float)(vv[ND] - rho0);
             mi = (float)((const double*)m)[i];
         }
-        test[s] = test_record<ND>(x, g, cs32);
+        // offsets against the reference cell `key` (the cell of the last rebuild)
+        test[s] = test_record_in<ND>(x, g, cs32, key);
         vel[s] = w;
         aux[s] = make_float2(eos32(w.w, P, P.fluid_clip), mi);
+        if (rebuild && xb_out) {
+#pragma unroll
+            for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
+        }
         if (u_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) {
@@ -119,29 +125,25 @@ __global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4
 }
 
 template <int ND>
-__global__ void __launch_bounds__(128) k_adami32(Phys32 P, GridDesc g, int nw,
-                                                 const float4* __restrict__ wtest,
-                                                 const int* __restrict__ wskey,
+__global__ void __launch_bounds__(128) k_adami32(Phys32 P, int nw, const float4* __restrict__ wtest,
+                                                 const unsigned* __restrict__ wf,
+                                                 const int* __restrict__ wfc,
                                                  float4* __restrict__ wstate,
                                                  double* __restrict__ wvol,
                                                  const float4* __restrict__ ftest,
                                                  const float4* __restrict__ fvel,
-                                                 const float2* __restrict__ faux,
-                                                 const int* __restrict__ fstart) {
-    __shared__ WarpSmem smw[4];
-    WarpSmem& sm = smw[threadIdx.x >> 5];
+                                                 const float2* __restrict__ faux) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = w < nw;
-    const int wi = active ? w : 0;
-    const float4 tw = wtest[wi];
-    int c[3];
-    key_to_coords(wskey[wi], g, c);
-    const float cxw = (float)c[0];
+    if (w >= nw) return;
+    const float4 tw = wtest[w];
     Kahan Ps, V;
-    auto gather = [&](int e) {
-        const int b = e & kSlotMask;
+    const int n = wfc[w];
+    for (int k = 0; k < n; ++k) {
+        const unsigned e = wf[(size_t)k * nw + w];
+        const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(tw, cxw, P.cs, e, ftest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(tw, P.cs, e, ftest[b], pd0, pd1, pd2);
+        if (d2 > P.sr2) continue;
         const float r = sqrtf(d2);
         const float rho_f = P.rho0 + fvel[b].w;
         float hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
@@ -156,9 +158,7 @@ __global__ void __launch_bounds__(128) k_adami32(Phys32 P, GridDesc g, int nw,
         }
         Ps.add(sum * W);
         V.add(W);
-    };
-    warp_neighbors<ND>(g, P.cs, active, c, tw, fstart, ftest, P.sr2, sm, gather);
-    if (!active) return;
+    }
     float pw = Ps.s - Ps.c;
     const float vw = V.s - V.c;
     if ((double)vw > 2.220446049250313e-16) pw = pw / vw;
@@ -183,36 +183,35 @@ struct Update32 {
 };
 
 template <int ND, bool INTEGRATE>
-__global__ void __launch_bounds__(128, 4) k_pair32(Phys32 P, GridDesc g, int nf,
-                                                const float4* __restrict__ ftest,
+__global__ void __launch_bounds__(128) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float2* __restrict__ faux,
-                                                const int* __restrict__ fstart,
-                                                const int* __restrict__ fskey,
+                                                const unsigned* __restrict__ ff,
+                                                const int* __restrict__ ffc,
+                                                const unsigned* __restrict__ fw,
+                                                const int* __restrict__ fwc,
                                                 const float4* __restrict__ wtest,
                                                 const float4* __restrict__ wstate,
-                                                const int* __restrict__ wstart, Update32 U) {
-    __shared__ WarpSmem smw[4];
-    WarpSmem& sm = smw[threadIdx.x >> 5];
+                                                unsigned* __restrict__ gate, Update32 U) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = s < nf;
-    const int si = active ? s : 0;
-    const float4 ta = ftest[si];
-    const float4 va = fvel[si];
-    const float p_a = faux[si].x;
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
+    if (s >= nf) return;
+    const float4 ta = ftest[s];
+    const float4 va = fvel[s];
+    const float p_a = faux[s].x;
     const float drho_a = va.w;
     const float rho_a = P.rho0 + drho_a;
-    int c[3];
-    key_to_coords(fskey[si], g, c);
-    const float cxa = (float)c[0];
 
     Kahan a0, a1, a2, ar;
-    auto ff = [&](int e) {
-        const int b = e & kSlotMask;
+    const int nff = ffc[s];
+    for (int k = 0; k < nff; ++k) {
+        const unsigned e = ff[(size_t)k * nf + s];
+        const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, cxa, P.cs, e, ftest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(ta, P.cs, e, ftest[b], pd0, pd1, pd2);
+        if (d2 > P.sr2) continue;
         const float r = sqrtf(d2);
-        if (r < P.almostzero) return;
+        if (r < P.almostzero) continue;
         const float4 vb = fvel[b];
         const float2 ab = faux[b];  // {p_b, m_b}
         const float m_b = ab.y;
@@ -252,16 +251,18 @@ __global__ void __launch_bounds__(128, 4) k_pair32(Phys32 P, GridDesc g, int nf,
             er += P.diff_coef * (vol_b * (pc * pg));
         }
         ar.add(er);
-    };
-    warp_neighbors<ND>(g, P.cs, active, c, ta, fstart, ftest, P.sr2, sm, ff);
+    }
 
     Kahan w0, w1, w2, wr;
-    auto fw = [&](int e) {
-        const int b = e & kSlotMask;
+    const int nfw = fwc[s];
+    for (int k = 0; k < nfw; ++k) {
+        const unsigned e = fw[(size_t)k * nf + s];
+        const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, cxa, P.cs, e, wtest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(ta, P.cs, e, wtest[b], pd0, pd1, pd2);
+        if (d2 > P.sr2) continue;
         const float r = sqrtf(d2);
-        if (r < P.almostzero) return;
+        if (r < P.almostzero) continue;
         const float4 sb = wstate[b];  // {p, rho - rho0, m, 0}
         const float m_b = sb.z, p_b = sb.x, rho_b = P.rho0 + sb.y;
         const float q = r * P.h_inv;
@@ -275,9 +276,7 @@ __global__ void __launch_bounds__(128, 4) k_pair32(Phys32 P, GridDesc g, int nf,
         float vg = va.x * g0 + va.y * g1;
         if (ND == 3) vg += va.z * g2;
         wr.add((__fdividef(rho_a, rho_b) * m_b) * vg);
-    };
-    warp_neighbors<ND>(g, P.cs, active, c, ta, wstart, wtest, P.sr2, sm, fw);
-    if (!active) return;
+    }
 
     double k[4];
     k[0] = (a0.value() + w0.value()) + U.g[0];
@@ -324,7 +323,7 @@ inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 }
 
 void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
-               const PhysState* src, PhysState* dst) {
+               const PhysState* src, PhysState* dst, const unsigned* gate) {
     const int n = (int)h->cfg.n_fluid;
     if (n == 0) return;
     const double cs32 = (double)(float)h->grid.cs;
@@ -345,6 +344,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
             pk.id_out = dst->id;
             pk.m_out = (float*)dst->m;
         }
+        pk.xb_out = h->x_build;
         pk.test = h->f_test;
         pk.vel = (float4*)h->f_vel;
         pk.aux = (float2*)h->f_aux;
@@ -353,7 +353,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         pk.rho0 = h->cfg.reference_density;
         pk.P = h->phys32;
         k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n,
-                                                          h->f_perm, h->f_skey, pk);
+                                                          h->f_perm, h->f_skey, pk, gate);
     };
     const bool s32 = src != nullptr;
     if (h->cfg.ndims == 2) {
@@ -379,20 +379,20 @@ void fp32_adami(tp_handle* h) {
     if (nw == 0) return;
     if (h->cfg.ndims == 2)
         k_adami32<2><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys32, h->grid, nw, h->w_test, h->w_skey, (float4*)h->w_state, h->w_vol,
-            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->f_start);
+            h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
+            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux);
     else
         k_adami32<3><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys32, h->grid, nw, h->w_test, h->w_skey, (float4*)h->w_state, h->w_vol,
-            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->f_start);
+            h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
+            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux);
 }
 
 template <int ND, bool INTEG>
-static void launch_pair32(tp_handle* h, const Update32& U) {
+static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
     const int nf = (int)h->cfg.n_fluid;
     k_pair32<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
-        h->phys32, h->grid, nf, h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux,
-        h->f_start, h->f_skey, h->w_test, (const float4*)h->w_state, h->w_start, U);
+        h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->l_ff,
+        h->c_ff, h->l_fw, h->c_fw, h->w_test, (const float4*)h->w_state, gate, U);
 }
 
 void fp32_pair_kick(tp_handle* h, double* dv) {
@@ -402,9 +402,9 @@ void fp32_pair_kick(tp_handle* h, double* dv) {
     U.perm = h->f_perm;
     for (int d = 0; d < 3; ++d) U.g[d] = h->cfg.acceleration[d];
     if (h->cfg.ndims == 2)
-        launch_pair32<2, false>(h, U);
+        launch_pair32<2, false>(h, nullptr, U);
     else
-        launch_pair32<3, false>(h, U);
+        launch_pair32<3, false>(h, nullptr, U);
 }
 
 void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first) {
@@ -424,9 +424,9 @@ void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt,
     U.dtf = (float)dt;
     U.first = first;
     if (h->cfg.ndims == 2)
-        launch_pair32<2, true>(h, U);
+        launch_pair32<2, true>(h, h->gate, U);
     else
-        launch_pair32<3, true>(h, U);
+        launch_pair32<3, true>(h, h->gate, U);
 }
 
 }  // namespace tp

@@ -8,13 +8,13 @@
 // and reused for rho_a / rho_b and m_b / rho_b, which is bitwise the same as evaluating it per
 // pair.  Plain `/` in the reference stays IEEE division here.
 //
-// Neighbour candidates are filtered with an FP32 distance on cell-relative offsets whose bound
-// is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative), then every surviving pair is
-// decided exactly in FP64 with explicitly rounded products and sums (no FMA contraction), so the
-// neighbour set {b : |x_a - x_b|^2 <= (2h)^2} is the one the CPU computes.
+// Neighbour lists (tp_lists.cuh) are built with an FP32 distance on cell-relative offsets whose
+// bound is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative); the pair and Adami
+// kernels then decide every listed pair exactly in FP64 with explicitly rounded products and sums
+// (no FMA contraction), so the neighbour set {b : |x_a - x_b|^2 <= (2h)^2} is the one the CPU
+// computes, visited in the CPU's order.
 #include "tp_api_internal.h"
-#include "tp_nhs.cuh"
-#include "tp_warpnbr.cuh"
+#include "tp_lists.cuh"
 
 namespace tp {
 
@@ -51,6 +51,7 @@ struct Pack64 {
     double* tv_out;
     int* id_out;
     double* m_out;
+    double* xb_out;  // positions at the last rebuild (slot order), written on rebuild only
     float4* test;
     double4_32a* pos;
     double4_32a* vel;
@@ -58,7 +59,7 @@ struct Pack64 {
     GridDesc g;
     double cs32;
     Phys P;
-    __device__ void operator()(int i, int s) const {
+    __device__ void operator()(int i, int s, int key, bool rebuild) const {
         double x[3] = {0, 0, 0}, w[4] = {0, 0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
@@ -67,10 +68,14 @@ struct Pack64 {
         const double rho = w[ND];
         const double p = eos_pressure(rho, P, P.fluid_clip);
         const double mi = m[i];
-        test[s] = test_record<ND>(x, g, cs32);
+        if (rebuild) test[s] = test_record_in<ND>(x, g, cs32, key);
         pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
         vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
         aux[s] = make_double2(mi, fast_inv(rho));
+        if (rebuild && xb_out) {
+#pragma unroll
+            for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
+        }
         if (tu_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) tu_out[(size_t)s * ND + d] = tu[(size_t)i * ND + d];
@@ -88,7 +93,7 @@ template <int ND>
 struct PackPos64 {
     const double* u;
     double4_32a* pos;
-    __device__ void operator()(int i, int s) const {
+    __device__ void operator()(int i, int s, int, bool) const {
         double x[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
@@ -105,12 +110,12 @@ struct PackWall64 {
     float4* test;
     GridDesc g;
     double cs32;
-    __device__ void operator()(int i, int s) const {
+    __device__ void operator()(int i, int s, int key, bool) const {
         double y[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) y[d] = x[(size_t)i * ND + d];
         pos[s] = make_double4_32a(y[0], y[1], y[2], m[i]);
-        test[s] = test_record<ND>(y, g, cs32);
+        test[s] = test_record_in<ND>(y, g, cs32, key);
     }
 };
 
@@ -119,33 +124,25 @@ struct PackWall64 {
 // wall slot gathers its fluid neighbours in PointNeighbors order.
 // ------------------------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(128) k_adami64(Phys P, GridDesc g, float cs32f, float sr2f,
-                                                 int nw, const double4_32a* __restrict__ wpos,
-                                                 const float4* __restrict__ wtest,
-                                                 const int* __restrict__ wskey,
+__global__ void __launch_bounds__(128, 4) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
+                                                 const unsigned* __restrict__ wf,
+                                                 const int* __restrict__ wfc,
                                                  double4_32a* __restrict__ wstate,
                                                  double* __restrict__ wvol,
-                                                 const float4* __restrict__ ftest,
                                                  const double4_32a* __restrict__ fpos,
-                                                 const double4_32a* __restrict__ fvel,
-                                                 const int* __restrict__ fstart) {
-    __shared__ WarpSmem smw[4];
-    WarpSmem& sm = smw[threadIdx.x >> 5];
+                                                 const double4_32a* __restrict__ fvel) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = w < nw;
-    const int wi = active ? w : 0;
-    const double4_32a xw = wpos[wi];
-    const float4 tw = wtest[wi];
-    int c[3];
-    key_to_coords(wskey[wi], g, c);
+    if (w >= nw) return;
+    const double4_32a xw = wpos[w];
     double Ps = 0.0, V = 0.0;
-    auto gather = [&](int e) {
-        const int b = e & kSlotMask;
+    const int n = wfc[w];
+    for (int k = 0; k < n; ++k) {
+        const int b = (int)(wf[(size_t)k * nw + w] & kSlotMask);
         const double4_32a xb = fpos[b];
         const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
         const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
         const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-        if (d2 > P.sr2) return;
+        if (d2 > P.sr2) continue;
         const double r = sqrt(d2);
         const double rho_f = fvel[b].w;
         double hp = __dadd_rn(__dmul_rn(P.g[0], __dmul_rn(rho_f, pd0)),
@@ -162,9 +159,7 @@ __global__ void __launch_bounds__(128) k_adami64(Phys P, GridDesc g, float cs32f
         }
         Ps = __dadd_rn(Ps, __dmul_rn(sum, W));
         V = __dadd_rn(V, W);
-    };
-    warp_neighbors<ND>(g, cs32f, active, c, tw, fstart, ftest, sr2f, sm, gather);
-    if (!active) return;
+    }
     if (V > 2.220446049250313e-16) Ps = Ps / V;
     if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
     const double rho_w = eos_inverse(Ps, P);
@@ -190,40 +185,36 @@ struct Update64 {
 };
 
 template <int ND, bool INTEGRATE>
-__global__ void __launch_bounds__(128, 4) k_pair64(Phys P, GridDesc g, float cs32f, float sr2f,
-                                                int nf, const float4* __restrict__ ftest,
+__global__ void __launch_bounds__(128) k_pair64(Phys P, int nf,
                                                 const double4_32a* __restrict__ fpos,
                                                 const double4_32a* __restrict__ fvel,
                                                 const double2* __restrict__ faux,
-                                                const int* __restrict__ fstart,
-                                                const int* __restrict__ fskey,
-                                                const float4* __restrict__ wtest,
+                                                const unsigned* __restrict__ ff,
+                                                const int* __restrict__ ffc,
+                                                const unsigned* __restrict__ fw,
+                                                const int* __restrict__ fwc,
                                                 const double4_32a* __restrict__ wpos,
                                                 const double4_32a* __restrict__ wstate,
-                                                const int* __restrict__ wstart, Update64 U) {
-    __shared__ WarpSmem smw[4];
-    WarpSmem& sm = smw[threadIdx.x >> 5];
+                                                unsigned* __restrict__ gate, Update64 U) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = s < nf;
-    const int si = active ? s : 0;
-    const double4_32a pa = fpos[si];
-    const double4_32a va = fvel[si];
-    const float4 ta = ftest[si];
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
+    if (s >= nf) return;
+    const double4_32a pa = fpos[s];
+    const double4_32a va = fvel[s];
     const double p_a = pa.w, rho_a = va.w;
-    int c[3];
-    key_to_coords(fskey[si], g, c);
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
-    auto ff = [&](int e) {
-        const int b = e & kSlotMask;
+    const int nff = ffc[s];
+    for (int k = 0; k < nff; ++k) {
+        const int b = (int)(ff[(size_t)k * nf + s] & kSlotMask);
         const double4_32a pb = fpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-        if (d2 > P.sr2) return;
+        if (d2 > P.sr2) continue;
         const double r = sqrt(d2);
-        if (r < P.almostzero) return;
+        if (r < P.almostzero) continue;
         const double4_32a vb = fvel[b];
         const double2 ab = faux[b];  // {m_b, fast_inv(rho_b)}
         const double m_b = ab.x, rho_b = vb.w;
@@ -262,20 +253,20 @@ __global__ void __launch_bounds__(128, 4) k_pair64(Phys P, GridDesc g, float cs3
             if (ND == 3) pg += (pc * pd2) * g2;
             drho += P.diff_coef * (vol_b * pg);
         }
-    };
-    warp_neighbors<ND>(g, cs32f, active, c, ta, fstart, ftest, sr2f, sm, ff);
+    }
 
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion) ----
     double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
-    auto fw = [&](int e) {
-        const int b = e & kSlotMask;
+    const int nfw = fwc[s];
+    for (int k = 0; k < nfw; ++k) {
+        const int b = (int)(fw[(size_t)k * nf + s] & kSlotMask);
         const double4_32a pb = wpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-        if (d2 > P.sr2) return;
+        if (d2 > P.sr2) continue;
         const double r = sqrt(d2);
-        if (r < P.almostzero) return;
+        if (r < P.almostzero) continue;
         const double4_32a sb = wstate[b];  // {p, rho, fast_inv(rho), 0}
         const double m_b = pb.w, p_b = sb.x, rho_b = sb.y;
         const double q = r * P.h_inv;
@@ -289,9 +280,7 @@ __global__ void __launch_bounds__(128, 4) k_pair64(Phys P, GridDesc g, float cs3
         double vg = va.x * g0 + va.y * g1;
         if (ND == 3) vg += va.z * g2;
         erho += ((rho_a * sb.z) * m_b) * vg;
-    };
-    warp_neighbors<ND>(g, cs32f, active, c, ta, wstart, wtest, sr2f, sm, fw);
-    if (!active) return;
+    }
 
     // dv = ((0 + S_ff) + S_fw) + g ;  drho = S_ff + S_fw
     double k[4];
@@ -356,14 +345,11 @@ __global__ void k_count64(GridDesc g, double sr2, int n, const double4_32a* __re
 // ------------------------------------------------------------------------------------------
 namespace {
 inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
-// FP32 prefilter bound: (2h)^2 widened by 1e-5 so that no FP64 neighbour is dropped.
-inline float filter_sr2(const tp_handle* h) { return (float)(h->phys.sr2 * (1.0 + 1e-5)); }
-inline float cs32f(const tp_handle* h) { return (float)h->grid.cs; }
 }  // namespace
 
 template <int ND>
 static void pack_fluid64(tp_handle* h, const double* u, const double* v, const double* m,
-                         const PhysState* src, PhysState* dst) {
+                         const PhysState* src, PhysState* dst, const unsigned* gate) {
     Pack64<ND> pk{};
     pk.u = u;
     pk.v = v;
@@ -377,6 +363,7 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
         pk.id_out = dst->id;
         pk.m_out = (double*)dst->m;
     }
+    pk.xb_out = h->x_build;
     pk.test = h->f_test;
     pk.pos = (double4_32a*)h->f_pos;
     pk.vel = (double4_32a*)h->f_vel;
@@ -386,16 +373,16 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
     pk.P = h->phys;
     const int n = (int)h->cfg.n_fluid;
     k_rank_pack<<<nblk(n, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, n, h->f_perm,
-                                                      h->f_skey, pk);
+                                                      h->f_skey, pk, gate);
 }
 
 void fp64_pack(tp_handle* h, const double* u, const double* v, const double* m,
-               const PhysState* src, PhysState* dst) {
+               const PhysState* src, PhysState* dst, const unsigned* gate) {
     if (h->cfg.n_fluid == 0) return;
     if (h->cfg.ndims == 2)
-        pack_fluid64<2>(h, u, v, m, src, dst);
+        pack_fluid64<2>(h, u, v, m, src, dst, gate);
     else
-        pack_fluid64<3>(h, u, v, m, src, dst);
+        pack_fluid64<3>(h, u, v, m, src, dst, gate);
 }
 
 void fp64_pack_pos(tp_handle* h, const double* u) {
@@ -433,9 +420,9 @@ void fp64_adami(tp_handle* h) {
     auto run = [&](auto ndc) {
         constexpr int ND = decltype(ndc)::value;
         k_adami64<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
-            h->phys, h->grid, cs32f(h), filter_sr2(h), nw, (const double4_32a*)h->w_pos,
-            h->w_test, h->w_skey, (double4_32a*)h->w_state, h->w_vol, h->f_test,
-            (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->f_start);
+            h->phys, nw, (const double4_32a*)h->w_pos, h->l_wf, h->c_wf,
+            (double4_32a*)h->w_state, h->w_vol, (const double4_32a*)h->f_pos,
+            (const double4_32a*)h->f_vel);
     };
     if (h->cfg.ndims == 2)
         run(std::integral_constant<int, 2>{});
@@ -444,12 +431,12 @@ void fp64_adami(tp_handle* h) {
 }
 
 template <int ND, bool INTEG>
-static void launch_pair64(tp_handle* h, const Update64& U) {
+static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
     k_pair64<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
-        h->phys, h->grid, cs32f(h), filter_sr2(h), nf, h->f_test, (const double4_32a*)h->f_pos,
-        (const double4_32a*)h->f_vel, (const double2*)h->f_aux, h->f_start, h->f_skey, h->w_test,
-        (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, h->w_start, U);
+        h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
+        (const double2*)h->f_aux, h->l_ff, h->c_ff, h->l_fw, h->c_fw,
+        (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);
 }
 
 void fp64_pair_kick(tp_handle* h, double* dv) {
@@ -458,9 +445,9 @@ void fp64_pair_kick(tp_handle* h, double* dv) {
     U.dv = dv;
     U.perm = h->f_perm;
     if (h->cfg.ndims == 2)
-        launch_pair64<2, false>(h, U);
+        launch_pair64<2, false>(h, nullptr, U);
     else
-        launch_pair64<3, false>(h, U);
+        launch_pair64<3, false>(h, nullptr, U);
 }
 
 // Stage update in place on the slot-ordered state `out` written by the pack of this stage.
@@ -477,9 +464,9 @@ void fp64_pair_stage(tp_handle* h, PhysState& out, double A, double B, double dt
     U.dt = dt;
     U.first = first;
     if (h->cfg.ndims == 2)
-        launch_pair64<2, true>(h, U);
+        launch_pair64<2, true>(h, h->gate, U);
     else
-        launch_pair64<3, true>(h, U);
+        launch_pair64<3, true>(h, h->gate, U);
 }
 
 void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf) {

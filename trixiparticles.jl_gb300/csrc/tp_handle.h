@@ -72,6 +72,20 @@ struct tp_handle {
     void* w_state = nullptr;  // FP64: double4 {p, rho, 1/rho, 0}; FP32: float4 {p, rho-rho0, m, 0}
     double* w_vol = nullptr;
 
+    // ---- neighbour lists (tp_lists.cuh): entry k of slot s at list[k * n + s] ----
+    unsigned* l_ff = nullptr;  // fluid -> fluid candidates
+    unsigned* l_fw = nullptr;  // fluid -> wall
+    unsigned* l_wf = nullptr;  // wall -> fluid (Adami)
+    int* c_ff = nullptr;
+    int* c_fw = nullptr;
+    int* c_wf = nullptr;
+    int cap_ff = 0, cap_fw = 0, cap_wf = 0;
+    double skin = 0.1;          // list radius 2h (1 + skin); rebuild after skin * h displacement
+    double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
+    unsigned* gate = nullptr;   // {force, max displacement bits, half-skin bits}
+    int* d_max = nullptr;       // scratch for the largest cell occupancy
+    int maxcell_w = 0;          // largest wall cell occupancy (walls are static)
+
     // ---- integrator ping-pong state ----
     tp::PhysState st[2];
     int cur = 0;
@@ -83,6 +97,7 @@ struct tp_handle {
     // ---- device error word ----
     int* d_err = nullptr;
     int* h_err = nullptr;  // pinned
+    unsigned* h_gate = nullptr;  // pinned gate initialiser
 
     // Phase timing: kNumPhases + 1 events per RHS evaluation from a pool, read back once at
     // the end of the call (no synchronisation inside the stage loop).

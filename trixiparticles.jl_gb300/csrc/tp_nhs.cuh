@@ -13,11 +13,22 @@
 //                 order (cell, index) whatever order the atomics ran in; the same pass packs
 //                 the particle's record into its slot (SoA reorder).
 // The scan also re-zeroes the histogram, so no memset is needed between rebuilds.
+//
+// Gate: inside the integrator the cell list is rebuilt only when some particle has moved more
+// than half the neighbour-list skin since the last rebuild (or a rebuild is forced).  The
+// decision is taken on the device: gate[0] = force flag, gate[1] = largest displacement since
+// the last rebuild (non-negative float bits, so unsigned order = float order), gate[2] = half
+// skin (float bits).  A null gate means "always rebuild".  When the gate is closed the kernels
+// return at once and the rank pass packs every slot in place.
 #pragma once
 
 #include "tp_internal.cuh"
 
 namespace tp {
+
+__device__ __forceinline__ bool gate_open(const unsigned* gate) {
+    return gate == nullptr || gate[0] != 0u || gate[1] > gate[2];
+}
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
@@ -26,7 +37,9 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 template <int ND>
 __global__ void __launch_bounds__(256) k_cell_keys(const double* __restrict__ u, int n,
                                                    GridDesc g, int* __restrict__ key,
-                                                   int* __restrict__ count, int* __restrict__ err) {
+                                                   int* __restrict__ count, int* __restrict__ err,
+                                                   const unsigned* __restrict__ gate = nullptr) {
+    if (!gate_open(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
@@ -82,7 +95,9 @@ __device__ __forceinline__ int block_exclusive_scan(int (&v)[kScanItems], int* w
 }
 
 static __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int* __restrict__ count, int n,
-                                                             int* __restrict__ partial) {
+                                                             int* __restrict__ partial,
+                                                             const unsigned* __restrict__ gate = nullptr) {
+    if (!gate_open(gate)) return;
     __shared__ int sm[33];
     const int base = blockIdx.x * kScanTile;
     int s = 0;
@@ -104,7 +119,9 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int* 
 }
 
 // Single block: exclusive scan of the per-tile partial sums, in chunks of kScanTile.
-static __global__ void __launch_bounds__(kScanThreads) k_scan_partials(int* __restrict__ partial, int nb) {
+static __global__ void __launch_bounds__(kScanThreads) k_scan_partials(int* __restrict__ partial, int nb,
+                                                               const unsigned* __restrict__ gate = nullptr) {
+    if (!gate_open(gate)) return;
     __shared__ int ws[33];
     int carry = 0;
     for (int base = 0; base < nb; base += kScanTile) {
@@ -129,7 +146,9 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_partials(int* __re
 static __global__ void __launch_bounds__(kScanThreads) k_scan_final(int* __restrict__ count, int n,
                                                             const int* __restrict__ partial,
                                                             int* __restrict__ start,
-                                                            int* __restrict__ cursor) {
+                                                            int* __restrict__ cursor,
+                                                            const unsigned* __restrict__ gate = nullptr) {
+    if (!gate_open(gate)) return;
     __shared__ int ws[33];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -150,7 +169,9 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_final(int* __restr
 }
 
 static __global__ void __launch_bounds__(256) k_scatter(const int* __restrict__ key, int n,
-                                                 int* __restrict__ cursor, int* __restrict__ tmp) {
+                                                 int* __restrict__ cursor, int* __restrict__ tmp,
+                                                 const unsigned* __restrict__ gate = nullptr) {
+    if (!gate_open(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
@@ -165,15 +186,21 @@ static __global__ void __launch_bounds__(256) k_scatter(const int* __restrict__ 
 }
 
 // Final slot = cell start + rank of the source index among the cell's particles.  The packer
-// functor copies source particle i into slot dst (records, masses, state).
+// functor copies source particle i into slot dst of cell `key` (records, masses, state).  With
+// a closed gate every slot is packed in place: pack(s, s, skey[s]).
 template <class Packer>
 __global__ void __launch_bounds__(256) k_rank_pack(const int* __restrict__ tmp,
                                                    const int* __restrict__ key,
                                                    const int* __restrict__ start, int n,
                                                    int* __restrict__ perm, int* __restrict__ skey,
-                                                   Packer pack) {
+                                                   Packer pack,
+                                                   const unsigned* __restrict__ gate = nullptr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
+    if (!gate_open(gate)) {
+        pack(s, s, skey[s], false);
+        return;
+    }
     const int i = tmp[s];
     const int k = key[i];
     const int lo = start[k], hi = start[k + 1];
@@ -182,12 +209,12 @@ __global__ void __launch_bounds__(256) k_rank_pack(const int* __restrict__ tmp,
     const int dst = lo + r;
     perm[dst] = i;
     skey[dst] = k;
-    pack(i, dst);
+    pack(i, dst, k, true);
 }
 
 // Rank pass without packing (wall setup and diagnostics).
 struct NoPack {
-    __device__ void operator()(int, int) const {}
+    __device__ void operator()(int, int, int, bool) const {}
 };
 
 }  // namespace tp
