@@ -1,0 +1,64 @@
+// Drives every C ABI entry point through create -> wall -> masses -> kick/drift/integrate ->
+// diagnostics -> destroy, in both precision forms and in 2D and 3D (host logic only).
+#include <cstdio>
+#include <vector>
+
+#include "tp_wcsph.h"
+
+static int run(int nd, int precision) {
+    tp_config c;
+    tp_config_default(&c);
+    c.ndims = nd;
+    c.precision = precision;
+    c.n_fluid = 3000;
+    c.n_wall = 1500;
+    c.smoothing_length = 0.035;
+    c.sound_speed = 62.6;
+    for (int d = 0; d < nd; ++d) {
+        c.min_corner[d] = -0.05;
+        c.max_corner[d] = 1.0;
+    }
+    c.acceleration[1] = -9.81;
+    c.wall_clip_negative_pressure = 1;
+    tp_handle* h = nullptr;
+    int bad = 0;
+    bad |= tp_create(&c, &h) != TP_OK;
+    if (!h) return 1;
+    std::vector<double> xw(c.n_wall * nd, 0.1), mw(c.n_wall, 0.4), mf(c.n_fluid, 0.4);
+    std::vector<double> v(c.n_fluid * (nd + 1), 1000.0), u(c.n_fluid * nd, 0.5);
+    std::vector<double> dv(v.size()), du(u.size()), pf(c.n_fluid), pw(c.n_wall);
+    std::vector<int> cell(c.n_fluid), order(c.n_fluid), nff(c.n_fluid), nfw(c.n_fluid),
+        nwf(c.n_wall);
+    bad |= tp_kick(h, dv.data(), v.data(), u.data(), 0.0) != TP_ERR_NOT_READY;
+    bad |= tp_set_wall(h, xw.data(), mw.data()) != TP_OK;
+    bad |= tp_set_fluid_mass(h, mf.data()) != TP_OK;
+    bad |= tp_enable_timing(h, 1) != TP_OK;
+    bad |= tp_kick(h, dv.data(), v.data(), u.data(), 0.0) != TP_OK;
+    bad |= tp_drift(h, du.data(), v.data(), u.data(), 0.0) != TP_OK;
+    bad |= tp_set_skin(h, 0.2) != TP_OK;
+    bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 2) != TP_OK;
+    bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 1) != TP_OK;
+    bad |= tp_kick(h, dv.data(), v.data(), u.data(), 0.0) != TP_OK;
+    bad |= tp_fluid_pressure(h, pf.data()) != TP_OK;
+    bad |= tp_wall_state(h, pw.data(), nullptr, nullptr) != TP_OK;
+    bad |= tp_nhs_debug(h, u.data(), cell.data(), order.data(), nff.data(), nfw.data(),
+                        nwf.data()) != TP_OK;
+    double cons[5];
+    bad |= tp_conservation(h, v.data(), cons) != TP_OK;
+    double ms[8];
+    bad |= tp_phase_times(h, ms, 8) != 3;
+    bad |= tp_sync(h) != TP_OK;
+    bad |= tp_cell_sort_noalloc(&c, u.data(), c.n_fluid, cell.data(), order.data(), nullptr) !=
+           TP_OK;
+    bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, -1) != TP_ERR_ARGUMENT;
+    bad |= tp_destroy(h) != TP_OK;
+    std::printf("nd=%d precision=%d bad=%d\n", nd, precision, bad);
+    return bad;
+}
+
+int main() {
+    int bad = 0;
+    for (int nd = 2; nd <= 3; ++nd)
+        for (int p = 0; p <= 1; ++p) bad |= run(nd, p);
+    return bad;
+}

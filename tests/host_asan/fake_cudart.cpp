@@ -1,0 +1,44 @@
+// Host-only stand-in of the CUDA runtime: device memory is host memory, copies are memmove,
+// kernel launches do nothing.  Linking the library's objects against it runs every host code
+// path of the C ABI (allocation, sizing, orchestration, error handling, teardown) on a machine
+// without a GPU, under AddressSanitizer.
+#include <cuda_runtime_api.h>
+#include <cstdlib>
+#include <cstring>
+#include <cstdio>
+extern "C" {
+cudaError_t cudaMalloc(void** p, size_t n) { *p = calloc(1, n); return *p ? cudaSuccess : cudaErrorMemoryAllocation; }
+cudaError_t cudaFree(void* p) { free(p); return cudaSuccess; }
+cudaError_t cudaMallocHost(void** p, size_t n) { *p = calloc(1, n); return cudaSuccess; }
+cudaError_t cudaFreeHost(void* p) { free(p); return cudaSuccess; }
+cudaError_t cudaMemset(void* p, int v, size_t n) { memset(p, v, n); return cudaSuccess; }
+cudaError_t cudaMemsetAsync(void* p, int v, size_t n, cudaStream_t) { memset(p, v, n); return cudaSuccess; }
+cudaError_t cudaMemcpy(void* d, const void* s, size_t n, cudaMemcpyKind) { memmove(d, s, n); return cudaSuccess; }
+cudaError_t cudaMemcpyAsync(void* d, const void* s, size_t n, cudaMemcpyKind, cudaStream_t) { memmove(d, s, n); return cudaSuccess; }
+cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaDeviceSynchronize() { return cudaSuccess; }
+cudaError_t cudaGetLastError() { return cudaSuccess; }
+const char* cudaGetErrorString(cudaError_t) { return "stub"; }
+cudaError_t cudaEventCreate(cudaEvent_t* e) { *e = (cudaEvent_t)malloc(8); return cudaSuccess; }
+cudaError_t cudaEventDestroy(cudaEvent_t e) { free(e); return cudaSuccess; }
+cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaEventSynchronize(cudaEvent_t) { return cudaSuccess; }
+cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t, cudaEvent_t) { *ms = 0; return cudaSuccess; }
+cudaError_t cudaGetDevice(int* d) { *d = 0; return cudaSuccess; }
+cudaError_t cudaGetSymbolAddress(void** p, const void* s) { *p = (void*)s; return cudaSuccess; }
+cudaError_t cudaLaunchKernel(const void*, dim3, dim3, void**, size_t, cudaStream_t) { return cudaSuccess; }
+unsigned __cudaPushCallConfiguration(dim3, dim3, size_t, void*) { return 0; }
+cudaError_t __cudaPopCallConfiguration(dim3*, dim3*, size_t*, void*) { return cudaSuccess; }
+void** __cudaRegisterFatBinary(void*) { static void* h[4]; return h; }
+void __cudaRegisterFatBinaryEnd(void**) {}
+void __cudaUnregisterFatBinary(void**) {}
+void __cudaRegisterFunction(void**, const char*, char*, const char*, int, void*, void*, void*, void*, int*) {}
+void __cudaRegisterVar(void**, char*, char*, const char*, int, size_t, int, int) {}
+void __cudaRegisterManagedVar(void**, void**, char*, const char*, int, size_t, int, int) {}
+char __cudaInitModule(void**) { return 0; }
+}
+extern "C" {
+cudaError_t __cudaGetKernel(void** k, const void* f) { *k = (void*)f; return cudaSuccess; }
+cudaError_t __cudaLaunchKernel(const void*, dim3, dim3, void**, size_t, cudaStream_t) { return cudaSuccess; }
+cudaError_t __cudaLaunchKernel_ptsz(const void*, dim3, dim3, void**, size_t, cudaStream_t) { return cudaSuccess; }
+}

@@ -2,6 +2,7 @@
 // kick!/drift! and the fused CarpenterKennedy2N54 integrator.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -38,6 +39,34 @@ tp_status cuda_fail(tp_handle* h, cudaError_t e, const char* where) {
     do {                                                   \
         cudaError_t e_ = cudaGetLastError();               \
         if (e_ != cudaSuccess) return cuda_fail(h, e_, where); \
+    } while (0)
+
+// TP_DEBUG_SYNC=1: synchronise and check after every launch group and print a progress line to
+// stderr (diagnostics of a failing launch; never set in production runs).
+bool debug_sync_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("TP_DEBUG_SYNC");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
+tp_status dbg(tp_handle* h, const char* what) {
+    if (!debug_sync_enabled()) return TP_OK;
+    std::fprintf(stderr, "tp: %s ...", what);
+    std::fflush(stderr);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    std::fprintf(stderr, " %s\n", e == cudaSuccess ? "ok" : cudaGetErrorString(e));
+    std::fflush(stderr);
+    if (e != cudaSuccess) return cuda_fail(h, e, what);
+    return TP_OK;
+}
+
+#define TP_DBG(h, what)                      \
+    do {                                     \
+        tp_status s_ = dbg((h), (what));     \
+        if (s_ != TP_OK) return s_;          \
     } while (0)
 
 template <class T>
@@ -326,6 +355,7 @@ tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tm
                                                                  h->d_err, gate);
         TP_LAUNCHED(h, "cell keys");
         h->launches += 1;
+        TP_DBG(h, "cell keys");
         if (maxcell) {
             k_max_count<<<256, 256, 0, h->stream>>>(h->f_count, h->grid.ncells, maxcell);
             TP_LAUNCHED(h, "max cell count");
@@ -340,10 +370,12 @@ tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tm
                                                      h->f_cursor, gate);
     TP_LAUNCHED(h, "cell scan");
     h->launches += 3;
+    TP_DBG(h, "cell scan");
     if (n > 0) {
         k_scatter<<<nblk(n, 256), 256, 0, h->stream>>>(key, n, h->f_cursor, tmp, gate);
         TP_LAUNCHED(h, "cell scatter");
         h->launches += 1;
+        TP_DBG(h, "cell scatter");
     }
     return TP_OK;
 }
@@ -373,6 +405,7 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
         k_max_count<<<256, 256, 0, h->stream>>>(h->f_count, h->grid.ncells, h->d_max);
         TP_LAUNCHED(h, "list sizing");
         h->launches += 2;
+        TP_DBG(h, "list sizing");
         TP_CUDA(h, cudaMemsetAsync(h->f_count, 0, (size_t)h->grid.ncells * sizeof(int), h->stream));
         TP_CUDA(h, cudaMemcpyAsync(h->h_err + 1, h->d_max, sizeof(int), cudaMemcpyDeviceToHost,
                                    h->stream));
@@ -395,6 +428,9 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
     TP_CUDA(h, grow(&h->l_ff, &h->cap_ff, cff, nf));
     TP_CUDA(h, grow(&h->l_fw, &h->cap_fw, cfw, nf));
     TP_CUDA(h, grow(&h->l_wf, &h->cap_wf, cwf, nw));
+    if (debug_sync_enabled())
+        std::fprintf(stderr, "tp: lists maxcell_f=%d maxcell_w=%d cap ff=%d fw=%d wf=%d nf=%d nw=%d\n",
+                     maxcell_f, h->maxcell_w, h->cap_ff, h->cap_fw, h->cap_wf, nf, nw);
     return TP_OK;
 }
 
@@ -421,6 +457,7 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
         run(std::integral_constant<int, 3>{});
     TP_LAUNCHED(h, "list build");
     h->launches += (nf > 0) + (nw > 0);
+    TP_DBG(h, "list build");
     return TP_OK;
 }
 
@@ -463,10 +500,6 @@ tp_status ensure_state(tp_handle* h) {
     const size_t nf = (size_t)h->cfg.n_fluid;
     const int nd = h->cfg.ndims;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
-    void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
-                    h->d_max};
-    for (void* p : more)
-        if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
         PhysState& s = h->st[k];
         TP_CUDA(h, dalloc(&s.u, nf * nd));
@@ -778,6 +811,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     }
     k_iota<<<nblk(nf, 256), 256, 0, h->stream>>>(s0.id, nf);
     TP_LAUNCHED(h, "integrator load");
+    TP_DBG(h, "integrator load");
     h->launches += f32 ? 2 : 1;
 
     st = ensure_lists(h, u_ode);
@@ -806,6 +840,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
                 k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build, nf,
                                                                          h->gate);
             h->launches += 1;
+            TP_DBG(h, "displacement");
             st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);
             if (st != TP_OK) return st;
             if (f32)
@@ -815,6 +850,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
                           h->gate);
             TP_LAUNCHED(h, "pack");
             h->launches += 1;
+            TP_DBG(h, "pack");
             st = build_lists(h, h->skin, h->gate);
             if (st != TP_OK) return st;
             mark(h, 1);
@@ -823,12 +859,14 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
             else
                 fp64_adami(h);
             TP_LAUNCHED(h, "adami");
+            TP_DBG(h, "adami");
             mark(h, 2);
             if (f32)
                 fp32_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
             else
                 fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
             TP_LAUNCHED(h, "pair stage");
+            TP_DBG(h, "pair stage");
             mark(h, 3);
             h->launches += 1 + (h->cfg.n_wall > 0);
             h->cur = 1 - h->cur;
@@ -853,6 +891,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
                                                                      u_ode, v_ode, nf);
     }
     TP_LAUNCHED(h, "integrator store");
+    TP_DBG(h, "integrator store");
     h->launches += 1;
     finish_timing(h);
     return TP_OK;
