@@ -225,6 +225,67 @@ def cpu_baseline(semi, tank, cfg, threads=None):
                       f"({n} particles) with the FP64 C++ oracle, OpenMP, {el:.1f} s"}
 
 
+def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
+    """Batching form: 512 seeded 2D dam breaks (FP32), three spacing groups as the branches of
+    one CUDA graph of `steps_per_replay` CK2N54 steps; autotuned launch shape and skin.
+    Aggregate particle-steps/s over all instances, plus the agreement of one instance per group
+    with the same instance run alone."""
+    e = pkg.ensemble
+    t0 = time.perf_counter()
+    specs = e.ensemble_specs(n_instances, seed)
+    groups = e.build_ensemble(specs)
+    setup_s = time.perf_counter() - t0
+    tuned = e.autotune(groups, trial_steps=2)
+    eg = e.EnsembleGraph(groups, steps_per_replay)
+    eg.reset()
+    eg.replay()  # warm-up replay
+    torch.cuda.synchronize()
+    reps = max(1, min(args.steps, 4))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(eg.stream)
+    for _ in range(reps):
+        eg.replay()
+    ev1.record(eg.stream)
+    torch.cuda.synchronize()
+    eg.check()
+    ms = ev0.elapsed_time(ev1)
+    steps = reps * steps_per_replay
+    n = eg.n_particles
+    # agreement with the single-instance path after one replay from the initial state
+    eg.reset()
+    eg.replay()
+    torch.cuda.synchronize()
+    agree = {}
+    for g in groups:
+        one = e.single_instance(specs[g.instances[0]])
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            e.prepare(one, s)
+            one.semi._call("tp_set_skin", ctypes.c_double(g.tuned["skin"]))
+            e.prepare(one, s)
+            e._integrate(one, steps_per_replay)
+        s.synchronize()
+        (xa, va, ra), (xb, vb, rb) = e.instance_state(g, 0), e.instance_state(one, 0)
+
+        def rl2(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+        agree[str(g.dx)] = {"rel_l2_x": rl2(xa, xb), "rel_l2_v": rl2(va, vb),
+                            "rel_l2_rho": rl2(ra, rb), "after_steps": steps_per_replay}
+        one.semi.close()
+    out = {"workload": f"{n_instances} seeded 2D dam breaks (width U[0.5,2], height U[0.25,1], "
+                       f"dx in {{0.005,0.01,0.02}}, 5.366x4.0 tank, 3 layers), FP32 form, "
+                       f"dt = 5e-3 dx",
+           "value": n * steps / (ms / 1e3), "unit": UNIT, "particles": n,
+           "n_fluid": eg.n_fluid, "steps": steps, "ms_per_step": ms / steps,
+           "graph": f"{len(groups)} concurrent branches x {steps_per_replay} steps per replay",
+           "autotuned": {str(k): v for k, v in tuned.items()},
+           "per_instance_agreement": agree, "host_setup_s": round(setup_s, 2)}
+    for g in groups:
+        g.semi.close()
+    return out
+
+
 def run_reference(args):
     """--impl reference: the oracle (C++ FP64 restatement of the reference) on host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -299,6 +360,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-forms", action="store_true", help="skip the dx=0.0064 form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the 512-instance 2D ensemble (batching form)")
     ap.add_argument("--profile-form", default=None, metavar="PRECISION:WORKLOAD",
                     help="profiling mode (e.g. float32:cfg2): only warm-up + timed steps of that "
                          "form, one summary line; used under ncu")
@@ -438,6 +501,9 @@ def main():
             "rel_l2_x": rl2(u32, u64)}
         forms["workload"] = CFG2["name"]
         out["forms"] = forms
+
+    if rank == 0 and not args.no_ensemble:
+        out.setdefault("forms", {})["batching"] = run_ensemble(pkg, torch, args)
 
     if rank == 0 and not args.no_cpu:
         semi_c, tank_c = make_case(pkg, CFG1, "float64", local)

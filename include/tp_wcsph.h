@@ -208,6 +208,22 @@ tp_status tp_enable_timing(tp_handle* h, int32_t enable);
  */
 tp_status tp_set_skin(tp_handle* h, double skin);
 
+/*
+ * Sizes the neighbour lists once for coordinates u_ode (device pointer) with room for `growth`
+ * times the densest cell seen now (>= 1), allocates the integrator state, and fixes both: later
+ * tp_kick / tp_integrate_ck2n54 calls then issue no host synchronisation and no allocation, so
+ * they can be recorded into a CUDA graph (a list that still overflows is reported as
+ * TP_ERR_CAPACITY by tp_sync).  Without this call the lists are re-sized at every call; a later
+ * tp_set_skin with a different skin also returns to that mode.  While a stream capture is
+ * active on the handle's stream, tp_integrate_ck2n54 requires this call first (and timing off)
+ * and fails with TP_ERR_ARGUMENT otherwise.  A captured graph refers to the handle's device
+ * buffers: a later call that grows them (a larger growth or skin) requires a new capture.
+ */
+tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth);
+
+/* Threads per block of the pair and Adami kernels: 64, 128 (default) or 256 (autotuning). */
+tp_status tp_set_launch(tp_handle* h, int32_t pair_block);
+
 /* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
 int64_t tp_kernel_launches(const tp_handle* h);
 

@@ -36,6 +36,9 @@ static int run(int nd, int precision) {
     bad |= tp_kick(h, dv.data(), v.data(), u.data(), 0.0) != TP_OK;
     bad |= tp_drift(h, du.data(), v.data(), u.data(), 0.0) != TP_OK;
     bad |= tp_set_skin(h, 0.2) != TP_OK;
+    bad |= tp_set_launch(h, 256) != TP_OK;
+    bad |= tp_set_launch(h, 100) != TP_ERR_ARGUMENT;
+    bad |= tp_prepare_lists(h, u.data(), 1.5) != TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 2) != TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 1) != TP_OK;
     bad |= tp_kick(h, dv.data(), v.data(), u.data(), 0.0) != TP_OK;

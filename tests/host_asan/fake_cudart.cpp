@@ -18,6 +18,7 @@ cudaError_t cudaMemcpyAsync(void* d, const void* s, size_t n, cudaMemcpyKind, cu
 cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
 cudaError_t cudaDeviceSynchronize() { return cudaSuccess; }
 cudaError_t cudaGetLastError() { return cudaSuccess; }
+cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus* s) { *s = cudaStreamCaptureStatusNone; return cudaSuccess; }
 const char* cudaGetErrorString(cudaError_t) { return "stub"; }
 cudaError_t cudaEventCreate(cudaEvent_t* e) { *e = (cudaEvent_t)malloc(8); return cudaSuccess; }
 cudaError_t cudaEventDestroy(cudaEvent_t e) { free(e); return cudaSuccess; }

@@ -28,6 +28,7 @@ from .semidiscretization import (
     solve,
 )
 from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
+from . import ensemble
 
 __all__ = [
     "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
@@ -35,6 +36,6 @@ __all__ = [
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
     "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
-    "build", "dam_break", "dam_break_semidiscretization", "default_config", "drift", "kick",
+    "build", "dam_break", "ensemble", "dam_break_semidiscretization", "default_config", "drift", "kick",
     "load_library", "semidiscretize", "solve",
 ]

@@ -96,6 +96,8 @@ PROTOTYPES = [
     ("tp_sync", c_int32, [c_void_p]),
     ("tp_phase_times", c_int32, [c_void_p, POINTER(c_double), c_int32]),
     ("tp_enable_timing", c_int32, [c_void_p, c_int32]),
+    ("tp_prepare_lists", c_int32, [c_void_p, c_void_p, c_double]),
+    ("tp_set_launch", c_int32, [c_void_p, c_int32]),
     ("tp_set_skin", c_int32, [c_void_p, c_double]),
     ("tp_kernel_launches", c_int64, [c_void_p]),
     ("tp_cell_sort_noalloc", c_int32,

@@ -99,6 +99,14 @@ __global__ void k_drift(double* __restrict__ du, const double* __restrict__ v, i
     for (int d = 0; d < ND; ++d) du[(size_t)i * ND + d] = v[(size_t)i * (ND + 1) + d];
 }
 
+__global__ void k_gate_init(unsigned* __restrict__ gate, float threshold) {
+    if (threadIdx.x == 0) {
+        gate[0] = 1u;
+        gate[1] = 0u;
+        gate[2] = __float_as_uint(threshold);
+    }
+}
+
 __global__ void k_iota(int* __restrict__ id, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) id[i] = i;
@@ -523,7 +531,7 @@ tp_status ensure_state(tp_handle* h) {
 tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
     const int nf = (int)h->cfg.n_fluid;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
-    tp_status st = ensure_lists(h, u);
+    tp_status st = h->lists_fixed ? TP_OK : ensure_lists(h, u);
     if (st != TP_OK) return st;
     if (!h->x_build) TP_CUDA(h, dalloc(&h->x_build, (size_t)std::max(nf, 1) * h->cfg.ndims));
     mark(h, 0);
@@ -634,7 +642,6 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
     A(dalloc(&h->d_err, 1));
     A(cudaMallocHost((void**)&h->h_err, 4 * sizeof(int)));
-    A(cudaMallocHost((void**)&h->h_gate, 4 * sizeof(unsigned)));
     if (e == cudaSuccess) e = cudaMemset(h->f_count, 0, nc * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->w_start, 0, (nc + 1) * sizeof(int));
@@ -672,7 +679,6 @@ tp_status tp_destroy(tp_handle* h) {
             if (p) cudaFree(p);
     }
     if (h->h_err) cudaFreeHost(h->h_err);
-    if (h->h_gate) cudaFreeHost(h->h_gate);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
     delete h;
     return TP_OK;
@@ -785,6 +791,15 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
     if (nf == 0 || n_steps == 0) return TP_OK;
     if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: null array");
+    {
+        // Under stream capture nothing may synchronise or allocate: list capacities and the
+        // integrator state must have been set up by tp_prepare_lists, and timing must be off.
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        TP_CUDA(h, cudaStreamIsCapturing(h->stream, &cap));
+        if (cap != cudaStreamCaptureStatusNone && (!h->lists_fixed || !h->st[0].u || h->timing))
+            return fail(h, TP_ERR_ARGUMENT,
+                        "tp_integrate_ck2n54: capturing needs tp_prepare_lists first and timing off");
+    }
     st = ensure_state(h);
     if (st != TP_OK) return st;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
@@ -814,17 +829,15 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     TP_DBG(h, "integrator load");
     h->launches += f32 ? 2 : 1;
 
-    st = ensure_lists(h, u_ode);
-    if (st != TP_OK) return st;
-    // Rebuild gate: force the first rebuild of this call; threshold = skin * h.
-    h->h_gate[0] = 1u;
-    h->h_gate[1] = 0u;
-    {
-        const float half = (float)(h->skin * h->cfg.smoothing_length);
-        std::memcpy(&h->h_gate[2], &half, sizeof(float));
+    if (!h->lists_fixed) {
+        st = ensure_lists(h, u_ode);
+        if (st != TP_OK) return st;
     }
-    TP_CUDA(h, cudaMemcpyAsync(h->gate, h->h_gate, 3 * sizeof(unsigned), cudaMemcpyHostToDevice,
-                               h->stream));
+    // Rebuild gate: force the first rebuild of this call; threshold = skin * h.  Written by a
+    // kernel (not a host copy) so that a captured graph carries the values of capture time.
+    k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length));
+    TP_LAUNCHED(h, "gate init");
+    h->launches += 1;
 
     for (int64_t step = 0; step < n_steps; ++step) {
         for (int stage = 0; stage < 5; ++stage) {
@@ -1008,9 +1021,36 @@ int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n) {
 
 int64_t tp_kernel_launches(const tp_handle* h) { return h ? (int64_t)h->launches : 0; }
 
+tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth) {
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    if (!(growth >= 1.0 && growth <= 16.0))
+        return fail(h, TP_ERR_ARGUMENT, "tp_prepare_lists: growth must be in [1, 16]");
+    if (h->cfg.n_fluid > 0 && !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_prepare_lists: null u");
+    const double skin = h->skin;
+    h->skin = (1.0 + skin) * std::cbrt(growth) - 1.0;  // size for `growth` x the densest cell
+    h->lists_fixed = false;
+    st = ensure_lists(h, u_ode);
+    h->skin = skin;
+    if (st != TP_OK) return st;
+    st = ensure_state(h);
+    if (st != TP_OK) return st;
+    h->lists_fixed = true;
+    return TP_OK;
+}
+
+tp_status tp_set_launch(tp_handle* h, int32_t pair_block) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (pair_block != 64 && pair_block != 128 && pair_block != 256)
+        return fail(h, TP_ERR_ARGUMENT, "pair_block must be 64, 128 or 256");
+    h->pair_block = pair_block;
+    return TP_OK;
+}
+
 tp_status tp_set_skin(tp_handle* h, double skin) {
     if (!h) return TP_ERR_ARGUMENT;
     if (!(skin >= 0.0 && skin <= 1.0)) return fail(h, TP_ERR_ARGUMENT, "skin must be in [0, 1]");
+    if (skin != h->skin) h->lists_fixed = false;  // capacities were sized for the old skin
     h->skin = skin;
     return TP_OK;
 }

@@ -125,7 +125,7 @@ __global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4
 }
 
 template <int ND>
-__global__ void __launch_bounds__(128) k_adami32(Phys32 P, int nw, const float4* __restrict__ wtest,
+__global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4* __restrict__ wtest,
                                                  const unsigned* __restrict__ wf,
                                                  const int* __restrict__ wfc,
                                                  float4* __restrict__ wstate,
@@ -183,7 +183,7 @@ struct Update32 {
 };
 
 template <int ND, bool INTEGRATE>
-__global__ void __launch_bounds__(128) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
+__global__ void __launch_bounds__(256) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float2* __restrict__ faux,
                                                 const unsigned* __restrict__ ff,
@@ -378,11 +378,11 @@ void fp32_adami(tp_handle* h) {
     const int nw = (int)h->cfg.n_wall;
     if (nw == 0) return;
     if (h->cfg.ndims == 2)
-        k_adami32<2><<<nblk(nw, 128), 128, 0, h->stream>>>(
+        k_adami32<2><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
             h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux);
     else
-        k_adami32<3><<<nblk(nw, 128), 128, 0, h->stream>>>(
+        k_adami32<3><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
             h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux);
 }
@@ -390,7 +390,7 @@ void fp32_adami(tp_handle* h) {
 template <int ND, bool INTEG>
 static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
     const int nf = (int)h->cfg.n_fluid;
-    k_pair32<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
+    k_pair32<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
         h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->l_ff,
         h->c_ff, h->l_fw, h->c_fw, h->w_test, (const float4*)h->w_state, gate, U);
 }

@@ -124,7 +124,7 @@ struct PackWall64 {
 // wall slot gathers its fluid neighbours in PointNeighbors order.
 // ------------------------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(128, 4) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
+__global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
                                                  const unsigned* __restrict__ wf,
                                                  const int* __restrict__ wfc,
                                                  double4_32a* __restrict__ wstate,
@@ -185,7 +185,7 @@ struct Update64 {
 };
 
 template <int ND, bool INTEGRATE>
-__global__ void __launch_bounds__(128) k_pair64(Phys P, int nf,
+__global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
                                                 const double4_32a* __restrict__ fpos,
                                                 const double4_32a* __restrict__ fvel,
                                                 const double2* __restrict__ faux,
@@ -419,7 +419,7 @@ void fp64_adami(tp_handle* h) {
     if (nw == 0) return;
     auto run = [&](auto ndc) {
         constexpr int ND = decltype(ndc)::value;
-        k_adami64<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
+        k_adami64<ND><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nw, (const double4_32a*)h->w_pos, h->l_wf, h->c_wf,
             (double4_32a*)h->w_state, h->w_vol, (const double4_32a*)h->f_pos,
             (const double4_32a*)h->f_vel);
@@ -433,7 +433,7 @@ void fp64_adami(tp_handle* h) {
 template <int ND, bool INTEG>
 static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
-    k_pair64<ND, INTEG><<<nblk(nf, 128), 128, 0, h->stream>>>(
+    k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
         h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
         (const double2*)h->f_aux, h->l_ff, h->c_ff, h->l_fw, h->c_fw,
         (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);

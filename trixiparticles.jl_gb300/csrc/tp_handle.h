@@ -85,6 +85,8 @@ struct tp_handle {
     unsigned* gate = nullptr;   // {force, max displacement bits, half-skin bits}
     int* d_max = nullptr;       // scratch for the largest cell occupancy
     int maxcell_w = 0;          // largest wall cell occupancy (walls are static)
+    bool lists_fixed = false;   // capacity fixed by tp_prepare_lists (no sizing sync per call)
+    int pair_block = 128;       // threads per block of the pair / Adami kernels (autotuned)
 
     // ---- integrator ping-pong state ----
     tp::PhysState st[2];
@@ -97,7 +99,6 @@ struct tp_handle {
     // ---- device error word ----
     int* d_err = nullptr;
     int* h_err = nullptr;  // pinned
-    unsigned* h_gate = nullptr;  // pinned gate initialiser
 
     // Phase timing: kNumPhases + 1 events per RHS evaluation from a pool, read back once at
     // the end of the call (no synchronisation inside the stage loop).
