@@ -242,10 +242,11 @@ def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
     torch.cuda.synchronize()
     reps = max(1, min(args.steps, 4))
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(eg.stream)
+    launch = torch.cuda.current_stream()  # CUDAGraph.replay launches on the current stream
+    ev0.record(launch)
     for _ in range(reps):
         eg.replay()
-    ev1.record(eg.stream)
+    ev1.record(launch)
     torch.cuda.synchronize()
     eg.check()
     ms = ev0.elapsed_time(ev1)

@@ -55,7 +55,7 @@ def test_graph_replay_equals_eager(pkg, cuda):
     eg = e.EnsembleGraph(groups, K)
     eg.reset()
     eg.replay()
-    cuda.synchronize()
+    cuda.cuda.synchronize()
     eg.check()
     got = [(g.v.cpu().numpy(), g.u.cpu().numpy()) for g in groups]
     for g, (v, u) in zip(e.build_ensemble(specs), got):  # fresh handles, eager launches
@@ -66,7 +66,7 @@ def test_graph_replay_equals_eager(pkg, cuda):
     # a second replay from the reset state reproduces the first
     eg.reset()
     eg.replay()
-    cuda.synchronize()
+    cuda.cuda.synchronize()
     for g, (v, u) in zip(groups, got):
         assert np.array_equal(g.v.cpu().numpy(), v)
     for g in groups:
@@ -80,7 +80,7 @@ def test_instances_match_single_instance_path(pkg, orc, cuda):
     eg = e.EnsembleGraph(groups, K)
     eg.reset()
     eg.replay()
-    cuda.synchronize()
+    cuda.cuda.synchronize()
     eg.check()
     for g in groups:
         for j in (0, len(g.instances) - 1):

@@ -234,6 +234,7 @@ class EnsembleGraph:
             g.u.copy_(g.ode.u0)
 
     def replay(self):
+        """Launches the graph on the current torch stream (asynchronous)."""
         self.graph.replay()
 
     def check(self):
