@@ -251,6 +251,33 @@ int64_t tp_kernel_launches(const tp_handle* h);
 tp_status tp_cell_sort_noalloc(const tp_config* cfg, const double* u, int64_t n, int32_t* cell,
                                int32_t* order, void* stream);
 
+/*
+ * Differentiation form: reverse-mode gradients of a CarpenterKennedy2N54 trajectory.  Stands
+ * where the reference would take gradients through `solve` with ChainRulesCore rules (the
+ * Julia shim defines an rrule over these two calls); the reference itself ships no adjoint.
+ *
+ * tp_adjoint_forward advances (v_ode, u_ode) in place by n_steps steps of size dt, exactly
+ * like tp_integrate_ck2n54 but in caller order with neighbour lists rebuilt at the start of
+ * every step and held fixed for its five stages, and records a checkpoint of the state every
+ * `checkpoint_every` steps on the device.  Arithmetic follows the handle's precision (FP32
+ * form: FP32 pair arithmetic and adjoint; FP64: everything in FP64).  Synchronises once at the
+ * end (error check).
+ *
+ * tp_adjoint_backward takes the cotangents of the final state -- v_bar (ndims+1, n_fluid:
+ * velocity rows, then the density row) and u_bar (ndims, n_fluid), device arrays in the
+ * reference layout -- and overwrites them with the cotangents of the initial state (the
+ * gradient with respect to v0 / rho0 and u0).  params_bar (host, 3 doubles) receives the
+ * gradient with respect to (Monaghan alpha, Molteni-Colagrossi delta, gravity magnitude along
+ * the configured acceleration), reduced in FP64.  Each k-step segment is recomputed from its
+ * checkpoint and reversed stage by stage.  Needs a preceding tp_adjoint_forward on the handle;
+ * may be called again with other cotangents.
+ */
+tp_status tp_adjoint_forward(tp_handle* h, double* v_ode, double* u_ode, double dt,
+                             int64_t n_steps, int64_t checkpoint_every);
+tp_status tp_adjoint_backward(tp_handle* h, double* v_bar, double* u_bar, double params_bar[3]);
+/* Kernel launches issued by the differentiation form on this handle (diagnostics). */
+int64_t tp_adjoint_kernel_launches(const tp_handle* h);
+
 /* Last error message of the handle (or of the last failed tp_create when h is NULL). */
 const char* tp_last_error(const tp_handle* h);
 

@@ -54,6 +54,18 @@ static int run(int nd, int precision) {
     bad |= tp_cell_sort_noalloc(&c, u.data(), c.n_fluid, cell.data(), order.data(), nullptr) !=
            TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, -1) != TP_ERR_ARGUMENT;
+    // differentiation form: forward with checkpoints, two backward sweeps, argument checks
+    double pbar[3];
+    std::vector<double> vbar(v.size(), 0.5), ubar(u.size(), 0.25);
+    bad |= tp_adjoint_backward(h, vbar.data(), ubar.data(), pbar) != TP_ERR_NOT_READY;
+    bad |= tp_adjoint_forward(h, v.data(), u.data(), 1e-4, 7, 3) != TP_OK;
+    bad |= tp_adjoint_backward(h, vbar.data(), ubar.data(), pbar) != TP_OK;
+    bad |= tp_adjoint_backward(h, vbar.data(), ubar.data(), pbar) != TP_OK;
+    bad |= tp_adjoint_forward(h, v.data(), u.data(), 1e-4, 2, 5) != TP_OK;
+    bad |= tp_adjoint_backward(h, vbar.data(), ubar.data(), pbar) != TP_OK;
+    bad |= tp_adjoint_forward(h, v.data(), u.data(), 1e-4, 0, 5) != TP_ERR_ARGUMENT;
+    bad |= tp_adjoint_forward(h, v.data(), u.data(), -1e-4, 3, 5) != TP_ERR_ARGUMENT;
+    bad |= tp_adjoint_kernel_launches(h) <= 0;
     bad |= tp_destroy(h) != TP_OK;
     std::printf("nd=%d precision=%d bad=%d\n", nd, precision, bad);
     return bad;

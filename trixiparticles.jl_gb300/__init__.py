@@ -28,7 +28,7 @@ from .semidiscretization import (
     solve,
 )
 from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
-from . import ensemble
+from . import adjoint, ensemble
 
 __all__ = [
     "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
@@ -36,6 +36,6 @@ __all__ = [
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
     "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
-    "build", "dam_break", "ensemble", "dam_break_semidiscretization", "default_config", "drift", "kick",
+    "adjoint", "build", "dam_break", "ensemble", "dam_break_semidiscretization", "default_config", "drift", "kick",
     "load_library", "semidiscretize", "solve",
 ]

@@ -102,6 +102,10 @@ PROTOTYPES = [
     ("tp_kernel_launches", c_int64, [c_void_p]),
     ("tp_cell_sort_noalloc", c_int32,
      [POINTER(TpConfig), c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    ("tp_adjoint_forward", c_int32,
+     [c_void_p, c_void_p, c_void_p, c_double, c_int64, c_int64]),
+    ("tp_adjoint_backward", c_int32, [c_void_p, c_void_p, c_void_p, POINTER(c_double)]),
+    ("tp_adjoint_kernel_launches", c_int64, [c_void_p]),
     ("tp_last_error", c_char_p, [c_void_p]),
 ]
 

@@ -558,6 +558,30 @@ tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
 
 }  // namespace
 
+namespace tp {
+const double kCK2N54_A[5] = {kA[0], kA[1], kA[2], kA[3], kA[4]};
+const double kCK2N54_B[5] = {kB[0], kB[1], kB[2], kB[3], kB[4]};
+
+tp_status api_fail(tp_handle* h, tp_status st, const std::string& msg) { return fail(h, st, msg); }
+tp_status api_cuda_fail(tp_handle* h, cudaError_t e, const char* where) {
+    return cuda_fail(h, e, where);
+}
+
+tp_status sort_fluid_cells(tp_handle* h, const double* u, int* maxcell) {
+    const int nf = (int)h->cfg.n_fluid;
+    tp_status st = sort_particles(h, u, nf, h->f_key, h->f_tmp, h->f_start, nullptr, maxcell);
+    if (st != TP_OK) return st;
+    if (nf > 0) {
+        k_rank_pack<<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, nf,
+                                                           h->f_perm, h->f_skey, NoPack{},
+                                                           nullptr);
+        TP_LAUNCHED(h, "rank");
+        h->launches += 1;
+    }
+    return TP_OK;
+}
+}  // namespace tp
+
 // =========================================================================================
 // C ABI
 // =========================================================================================
@@ -661,6 +685,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
 tp_status tp_destroy(tp_handle* h) {
     if (!h) return TP_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    adjoint_release(h);
     void* ptrs[] = {h->f_key,   h->f_tmp,   h->f_perm,  h->f_skey,        h->f_count,
                     h->f_start, h->f_cursor, h->scan_partial, h->f_test, h->f_pos,
                     h->f_vel,   h->f_aux,   h->m_f,     h->w_key,         h->w_tmp,

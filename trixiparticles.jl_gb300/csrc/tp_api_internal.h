@@ -25,4 +25,16 @@ void fp32_adami(tp_handle* h);
 void fp32_pair_kick(tp_handle* h, double* dv);
 void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first);
 
+// API layer services used by the differentiation form (tp_api.cu)
+tp_status api_fail(tp_handle* h, tp_status st, const std::string& msg);
+tp_status api_cuda_fail(tp_handle* h, cudaError_t e, const char* where);
+// Cell sort of fluid coordinates u (caller order): f_key (caller order), f_start, f_perm
+// (slot -> caller index), f_skey; `maxcell` (optional, device) receives the largest occupancy.
+tp_status sort_fluid_cells(tp_handle* h, const double* u, int* maxcell);
+extern const double kCK2N54_A[5];
+extern const double kCK2N54_B[5];
+
+// Differentiation form (tp_adjoint.cu)
+void adjoint_release(tp_handle* h);
+
 }  // namespace tp

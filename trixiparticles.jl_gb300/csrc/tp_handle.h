@@ -10,6 +10,8 @@
 
 namespace tp {
 
+struct AdjointState;  // differentiation form (tp_adjoint.cu)
+
 // Timed phases of one RHS evaluation (labels of the reference's TimerOutputs sections):
 //   0 "update nhs" (cell keys, scan, scatter, rank + pack incl. the fluid EOS),
 //   1 "compute boundary pressure" (Adami), 2 "system interaction" (pair kernel + fused update).
@@ -106,4 +108,7 @@ struct tp_handle {
     size_t ev_used = 0;
     double phase_ms[tp::kNumPhases] = {};
     long long launches = 0;  // kernel launches issued on this handle
+
+    // ---- differentiation form: checkpoints, tape and adjoint buffers (tp_adjoint.cu) ----
+    tp::AdjointState* adj = nullptr;
 };
