@@ -287,6 +287,99 @@ def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
     return out
 
 
+def run_adjoint(pkg, torch, dx=0.01, n_steps=500, every=25, fd_h=1e-4, seed=7):
+    """Differentiation form: 2D dam break at dx = 0.01 (20 000 fluid), v0 ~ N(0, 0.1^2) m/s,
+    FP32 forward + adjoint over 500 CK2N54 steps with checkpoints every 25; objective = mean
+    final height of the initial top layer.  Gradients w.r.t. alpha, delta, |g| and v0 (seeded
+    direction) against central differences (h = 1e-4) through the fused FP64 integrator, and
+    the cost of the backward pass per step relative to one forward step."""
+    dt = 5e-3 * dx
+    tank, eos = pkg.dam_break(2, dx, (2.0, 1.0), (5.366, 4.0), n_layers=3)
+    n = tank.fluid.n_particles
+    rng = np.random.default_rng(seed)
+    v0 = np.zeros((n, 3))
+    v0[:, :2] = rng.normal(0.0, 0.1, (n, 2))
+    v0[:, 2] = tank.fluid.density
+    u0 = tank.fluid.coordinates.copy()
+    w = np.random.default_rng(11).normal(size=(n, 2))
+    idx = pkg.adjoint.top_layer_indices(tank)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device="cuda")
+
+    def semi_of(precision, **kw):
+        p = dict(alpha=0.02, delta=0.1, gravity=9.81)
+        p.update(kw)
+        s = pkg.dam_break_semidiscretization(tank, eos, 1.75 * dx, precision=precision, **p)
+        pkg.semidiscretize(s, (0.0, 1.0))
+        return s
+
+    semi = semi_of("float32")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stream = torch.cuda.current_stream()
+    pkg.adjoint.Trajectory(semi, dev(v0), dev(u0), dt=dt, n_steps=every, checkpoint_every=every)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    traj = pkg.adjoint.Trajectory(semi, dev(v0), dev(u0), dt=dt, n_steps=n_steps,
+                                  checkpoint_every=every)
+    ev[1].record(stream)
+    loss, ubar = pkg.adjoint.surface_height_loss(traj.u, idx, 2)
+    vbar = torch.zeros_like(traj.v)
+    torch.cuda.synchronize()
+    ev[2].record(stream)
+    vb, ub, pbar = traj.pullback(vbar, ubar)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    fwd_ms, bwd_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+    # the fused FP32 integrator step (product forward) for the cost ratio
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    vi, ui = dev(v0), dev(u0)
+    semi._set_stream()
+    semi._call("tp_integrate_ck2n54", vi.data_ptr(), ui.data_ptr(), ctypes.c_double(0.0),
+               ctypes.c_double(dt), ctypes.c_int64(10))
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    semi._call("tp_integrate_ck2n54", vi.data_ptr(), ui.data_ptr(), ctypes.c_double(0.0),
+               ctypes.c_double(dt), ctypes.c_int64(100))
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    integ_ms = ev[0].elapsed_time(ev[1]) / 100
+    del ode
+    grad = dict(pbar, v0=float((vb.view(-1, 3)[:, :2].cpu().numpy() * w).sum()))
+    semi.close()
+
+    def fd_loss(v, **kw):
+        s = semi_of("float64", **kw)
+        vv, uu = dev(v), dev(u0)
+        s._set_stream()
+        s._call("tp_integrate_ck2n54", vv.data_ptr(), uu.data_ptr(), ctypes.c_double(0.0),
+                ctypes.c_double(dt), ctypes.c_int64(n_steps))
+        s.sync()
+        val = float(uu.view(-1, 2)[torch.as_tensor(idx, device="cuda"), 1].mean())
+        s.close()
+        return val
+
+    base = dict(alpha=0.02, delta=0.1, gravity=9.81)
+    fd = {}
+    for name in ("alpha", "delta", "gravity"):
+        fd[name] = (fd_loss(v0, **{name: base[name] + fd_h})
+                    - fd_loss(v0, **{name: base[name] - fd_h})) / (2 * fd_h)
+    vp, vm = v0.copy(), v0.copy()
+    vp[:, :2] += fd_h * w
+    vm[:, :2] -= fd_h * w
+    fd["v0"] = (fd_loss(vp) - fd_loss(vm)) / (2 * fd_h)
+    fwd_step = fwd_ms / n_steps
+    bwd_step = bwd_ms / n_steps
+    return {"workload": f"2D dam break dx={dx} ({n} fluid, {tank.boundary.n_particles} wall), "
+                        f"v0 ~ N(0, 0.1^2), {n_steps} steps dt={dt:g}, checkpoints every "
+                        f"{every}; loss = mean final height of the initial top layer "
+                        f"({len(idx)} particles)",
+            "loss": float(loss), "gradient": grad, "central_fd_fp64": fd, "fd_h": fd_h,
+            "rel_err": {k: abs(grad[k] - fd[k]) / max(abs(fd[k]), 1e-300) for k in fd},
+            "forward_ms_per_step": fwd_step, "backward_ms_per_step": bwd_step,
+            "fused_fp32_integrator_ms_per_step": integ_ms,
+            "backward_over_forward_step": bwd_step / fwd_step,
+            "backward_over_fused_step": bwd_step / integ_ms}
+
+
 def run_reference(args):
     """--impl reference: the oracle (C++ FP64 restatement of the reference) on host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -363,6 +456,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-ensemble", action="store_true",
                     help="skip the 512-instance 2D ensemble (batching form)")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the differentiated 2D dam break (differentiation form)")
     ap.add_argument("--profile-form", default=None, metavar="PRECISION:WORKLOAD",
                     help="profiling mode (e.g. float32:cfg2): only warm-up + timed steps of that "
                          "form, one summary line; used under ncu")
@@ -505,6 +600,8 @@ def main():
 
     if rank == 0 and not args.no_ensemble:
         out.setdefault("forms", {})["batching"] = run_ensemble(pkg, torch, args)
+    if rank == 0 and not args.no_adjoint:
+        out.setdefault("forms", {})["differentiation"] = run_adjoint(pkg, torch)
 
     if rank == 0 and not args.no_cpu:
         semi_c, tank_c = make_case(pkg, CFG1, "float64", local)
