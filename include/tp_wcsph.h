@@ -221,6 +221,9 @@ tp_status tp_set_skin(tp_handle* h, double skin);
  */
 tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth);
 
+/* Copy of the configuration the handle was created with. */
+tp_status tp_get_config(const tp_handle* h, tp_config* out);
+
 /* Threads per block of the pair and Adami kernels: 64, 128 (default) or 256 (autotuning). */
 tp_status tp_set_launch(tp_handle* h, int32_t pair_block);
 
@@ -277,6 +280,36 @@ tp_status tp_adjoint_forward(tp_handle* h, double* v_ode, double* u_ode, double 
 tp_status tp_adjoint_backward(tp_handle* h, double* v_bar, double* u_bar, double params_bar[3]);
 /* Kernel launches issued by the differentiation form on this handle (diagnostics). */
 int64_t tp_adjoint_kernel_launches(const tp_handle* h);
+
+/*
+ * Batching form: many independent simulations per CUDA-graph launch.  Stands where the
+ * reference would run an ensemble as separate `solve` calls (one per simulation); the
+ * reference has no batched entry point.  A batch bundles handles -- each a group of instances
+ * that share one cell grid (instances of equal spacing side by side, separated by gaps wider
+ * than the kernel support, so that they never interact) -- with their device state (v_ode,
+ * u_ode in the reference layout, integrated in place) and time step.
+ *   tp_batch_autotune: per member, times `trial_steps` steps on scratch copies of the state
+ *     for pair-kernel block sizes {64, 128, 256} x list skins {0.05, 0.1, 0.2} and keeps the
+ *     fastest; outputs (per member, optional): block size, skin, ms per step.
+ *   tp_batch_capture: sizes every member's lists for `growth` x the densest cell now
+ *     (tp_prepare_lists), warms up on scratch state, then records `steps` steps of every member
+ *     into one CUDA graph, the members as parallel branches.
+ *   tp_batch_launch: replays the graph on `stream` (asynchronous); tp_batch_sync waits and
+ *     reports the first member error.
+ * The batch owns one stream per member and sets it on the member handles; tp_batch_destroy
+ * resets them to the default stream.  Handles must outlive the batch.
+ */
+typedef struct tp_batch tp_batch;
+tp_status tp_batch_create(tp_handle* const* handles, int32_t n, tp_batch** out);
+tp_status tp_batch_destroy(tp_batch* b);
+tp_status tp_batch_set_state(tp_batch* b, int32_t member, double* v_ode, double* u_ode, double dt);
+tp_status tp_batch_autotune(tp_batch* b, int32_t trial_steps, int32_t* pair_block_out,
+                            double* skin_out, double* ms_out);
+tp_status tp_batch_capture(tp_batch* b, int64_t steps, double growth);
+tp_status tp_batch_launch(tp_batch* b, void* stream);
+tp_status tp_batch_sync(tp_batch* b);
+int64_t tp_batch_steps(const tp_batch* b);
+const char* tp_batch_last_error(const tp_batch* b);
 
 /* Last error message of the handle (or of the last failed tp_create when h is NULL). */
 const char* tp_last_error(const tp_handle* h);

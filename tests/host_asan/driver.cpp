@@ -66,6 +66,27 @@ static int run(int nd, int precision) {
     bad |= tp_adjoint_forward(h, v.data(), u.data(), 1e-4, 0, 5) != TP_ERR_ARGUMENT;
     bad |= tp_adjoint_forward(h, v.data(), u.data(), -1e-4, 3, 5) != TP_ERR_ARGUMENT;
     bad |= tp_adjoint_kernel_launches(h) <= 0;
+    // batching form: one-member batch, autotune, capture, launch, sync
+    tp_batch* b = nullptr;
+    tp_handle* hs[1] = {h};
+    bad |= tp_batch_create(hs, 1, &b) != TP_OK;
+    bad |= tp_batch_launch(b, nullptr) != TP_ERR_NOT_READY;
+    bad |= tp_batch_capture(b, 2, 1.5) != TP_ERR_NOT_READY;
+    bad |= tp_batch_set_state(b, 1, v.data(), u.data(), 1e-4) != TP_ERR_ARGUMENT;
+    bad |= tp_batch_set_state(b, 0, v.data(), u.data(), 1e-4) != TP_OK;
+    int32_t blk = 0;
+    double skin = 0.0, tms = 0.0;
+    bad |= tp_batch_autotune(b, 2, &blk, &skin, &tms) != TP_OK;
+    bad |= (blk != 64 && blk != 128 && blk != 256);
+    bad |= tp_batch_capture(b, 3, 1.5) != TP_OK;
+    bad |= tp_batch_steps(b) != 3;
+    bad |= tp_batch_launch(b, nullptr) != TP_OK;
+    bad |= tp_batch_launch(b, nullptr) != TP_OK;
+    bad |= tp_batch_sync(b) != TP_OK;
+    bad |= tp_batch_destroy(b) != TP_OK;
+    tp_config back;
+    bad |= tp_get_config(h, &back) != TP_OK;
+    bad |= back.n_fluid != c.n_fluid;
     bad |= tp_destroy(h) != TP_OK;
     std::printf("nd=%d precision=%d bad=%d\n", nd, precision, bad);
     return bad;

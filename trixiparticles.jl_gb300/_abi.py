@@ -106,6 +106,17 @@ PROTOTYPES = [
      [c_void_p, c_void_p, c_void_p, c_double, c_int64, c_int64]),
     ("tp_adjoint_backward", c_int32, [c_void_p, c_void_p, c_void_p, POINTER(c_double)]),
     ("tp_adjoint_kernel_launches", c_int64, [c_void_p]),
+    ("tp_get_config", c_int32, [c_void_p, POINTER(TpConfig)]),
+    ("tp_batch_create", c_int32, [c_void_p, c_int32, c_void_p]),
+    ("tp_batch_destroy", c_int32, [c_void_p]),
+    ("tp_batch_set_state", c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_double]),
+    ("tp_batch_autotune", c_int32,
+     [c_void_p, c_int32, POINTER(c_int32), POINTER(c_double), POINTER(c_double)]),
+    ("tp_batch_capture", c_int32, [c_void_p, c_int64, c_double]),
+    ("tp_batch_launch", c_int32, [c_void_p, c_void_p]),
+    ("tp_batch_sync", c_int32, [c_void_p]),
+    ("tp_batch_steps", c_int64, [c_void_p]),
+    ("tp_batch_last_error", c_char_p, [c_void_p]),
     ("tp_last_error", c_char_p, [c_void_p]),
 ]
 

@@ -19,7 +19,8 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libtp_wcsph.so"
 
-SOURCES = ["tp_api.cu", "tp_fp64.cu", "tp_fp32.cu", "tp_noalloc.cu", "tp_adjoint.cu"]
+SOURCES = ["tp_api.cu", "tp_fp64.cu", "tp_fp32.cu", "tp_noalloc.cu", "tp_adjoint.cu",
+           "tp_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3",

@@ -1064,6 +1064,12 @@ tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth) {
     return TP_OK;
 }
 
+tp_status tp_get_config(const tp_handle* h, tp_config* out) {
+    if (!h || !out) return TP_ERR_ARGUMENT;
+    *out = h->cfg;
+    return TP_OK;
+}
+
 tp_status tp_set_launch(tp_handle* h, int32_t pair_block) {
     if (!h) return TP_ERR_ARGUMENT;
     if (pair_block != 64 && pair_block != 128 && pair_block != 256)

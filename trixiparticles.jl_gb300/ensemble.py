@@ -5,14 +5,14 @@ Instances are drawn from a seed: fluid width U[0.5, 2] m, height U[0.25, 1] m, s
 Instances that share a spacing share one cell grid: they are placed side by side along x with
 gaps wider than the kernel support, so they never interact, and one set of kernel launches
 advances all of them (one library handle per spacing group).  The whole ensemble step is
-recorded once into a CUDA graph and replayed; the pair-kernel block size and the
-neighbour-list skin of every group are chosen by `autotune` from timed trial steps.
+recorded once into a CUDA graph by the library (tp_batch_capture, the groups as parallel
+branches) and replayed; the pair-kernel block size and the neighbour-list skin of every group
+are chosen by the library's autotuner (tp_batch_autotune) from timed trial steps.
 """
 from __future__ import annotations
 
 import ctypes
 import math
-import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -23,6 +23,7 @@ from .semidiscretization import (AdamiPressureExtrapolation, ArtificialViscosity
                                  GB300Backend, GridNeighborhoodSearch, Semidiscretization,
                                  WallBoundarySystem, WeaklyCompressibleSPHSystem,
                                  WendlandC2Kernel, semidiscretize)
+from . import _abi
 from .setups import InitialCondition, dam_break
 
 TANK = (5.366, 4.0)
@@ -137,7 +138,6 @@ def _integrate(g: Group, steps: int, dt: float | None = None):
 def _bind(g: Group, stream) -> None:
     g.semi._ensure_handle()
     st = g.semi._lib.tp_set_stream(g.semi._handle, ctypes.c_void_p(stream.cuda_stream))
-    from . import _abi
     _abi.check(g.semi._lib, g.semi._handle, st)
 
 
@@ -150,75 +150,90 @@ def prepare(g: Group, stream, growth: float = 1.5) -> None:
     g.semi._call("tp_prepare_lists", g.u.data_ptr(), ctypes.c_double(growth))
 
 
-def autotune(groups: list[Group], trial_steps: int = 3, blocks=(64, 128, 256),
-             skins=(0.05, 0.1, 0.2)) -> dict:
-    """Picks (pair_block, skin) per group from CUDA-event timed trial steps from the initial
-    state; leaves each group set to its choice and returns {dx: choice}."""
-    import torch
+class Batch:
+    """The native batch of the C ABI (tp_batch_*): one member per spacing group, its device
+    state integrated in place by every graph launch."""
 
-    stream = torch.cuda.Stream()
-    out = {}
-    with torch.cuda.stream(stream):
+    def __init__(self, groups: list[Group]):
+        self.groups = groups
         for g in groups:
-            best = None
-            for skin in skins:
-                g.semi._ensure_handle()
-                g.semi._call("tp_set_skin", ctypes.c_double(skin))
-                prepare(g, stream)
-                for blk in blocks:
-                    g.semi._call("tp_set_launch", ctypes.c_int32(blk))
-                    g.v.copy_(g.ode.v0)
-                    g.u.copy_(g.ode.u0)
-                    _integrate(g, 1)  # warm
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record(stream)
-                    _integrate(g, trial_steps)
-                    e1.record(stream)
-                    e1.synchronize()
-                    ms = e0.elapsed_time(e1) / trial_steps
-                    if best is None or ms < best[0]:
-                        best = (ms, blk, skin)
-            g.semi._call("tp_set_skin", ctypes.c_double(best[2]))
-            g.semi._call("tp_set_launch", ctypes.c_int32(best[1]))
-            g.tuned = {"pair_block": best[1], "skin": best[2], "ms_per_step": best[0]}
+            if g.ode is None:
+                g.ode = semidiscretize(g.semi, (0.0, 1.0))
+            if g.v is None:
+                g.v, g.u = g.ode.v0.clone(), g.ode.u0.clone()
+        self.lib = groups[0].semi._lib
+        hs = (ctypes.c_void_p * len(groups))(*[g.semi._handle.value for g in groups])
+        b = ctypes.c_void_p()
+        st = self.lib.tp_batch_create(hs, len(groups), ctypes.byref(b))
+        if st != 0:
+            raise _abi.TpError(st, "tp_batch_create failed")
+        self._b = b
+        for k, g in enumerate(groups):
+            self._check(self.lib.tp_batch_set_state(self._b, k, g.v.data_ptr(), g.u.data_ptr(),
+                                                    ctypes.c_double(time_step(g.dx))))
+
+    def _check(self, st):
+        if st != 0:
+            raise _abi.TpError(st, (self.lib.tp_batch_last_error(self._b) or b"").decode())
+
+    def autotune(self, trial_steps: int = 3) -> dict:
+        n = len(self.groups)
+        blk = (ctypes.c_int32 * n)()
+        skin = (ctypes.c_double * n)()
+        ms = (ctypes.c_double * n)()
+        self._check(self.lib.tp_batch_autotune(self._b, trial_steps, blk, skin, ms))
+        out = {}
+        for k, g in enumerate(self.groups):
+            g.tuned = {"pair_block": int(blk[k]), "skin": float(skin[k]),
+                       "ms_per_step": float(ms[k])}
             out[g.dx] = g.tuned
-    stream.synchronize()
-    return out
+        return out
+
+    def capture(self, steps: int, growth: float = 1.5) -> None:
+        self._check(self.lib.tp_batch_capture(self._b, ctypes.c_int64(steps),
+                                              ctypes.c_double(growth)))
+
+    def launch(self, stream=None) -> None:
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        self._check(self.lib.tp_batch_launch(self._b, ctypes.c_void_p(s.cuda_stream)))
+
+    def sync(self) -> None:
+        self._check(self.lib.tp_batch_sync(self._b))
+
+    def close(self) -> None:
+        if self._b is not None:
+            self.lib.tp_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune(groups: list[Group], trial_steps: int = 3) -> dict:
+    """Picks (pair_block, skin) per group with the native autotuner (trial steps on scratch
+    copies of the state); leaves each group's handle set to its choice; returns {dx: choice}."""
+    b = Batch(groups)
+    try:
+        return b.autotune(trial_steps)
+    finally:
+        b.close()
 
 
 class EnsembleGraph:
-    """K CarpenterKennedy2N54 steps of every group as one CUDA graph: one branch per spacing
-    group (the groups run concurrently on the GPU), each branch the group's whole fused
+    """K CarpenterKennedy2N54 steps of every group as one CUDA graph (tp_batch_capture): one
+    branch per spacing group (the groups run concurrently), each branch the group's fused
     integrator (neighbour-list upkeep, Adami, pair kernel with the stage update)."""
 
     def __init__(self, groups: list[Group], steps_per_replay: int, growth: float = 1.5):
-        import torch
-
         self.groups = groups
         self.k = steps_per_replay
-        self.stream = torch.cuda.Stream()
-        self.branches = [torch.cuda.Stream() for _ in groups]
-        for g, bs in zip(groups, self.branches):
-            with torch.cuda.stream(bs):
-                prepare(g, bs, growth)
-                _integrate(g, 1)  # warm-up outside the capture
-        torch.cuda.synchronize()
-        self.reset()
-        torch.cuda.synchronize()
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph, stream=self.stream):
-            fork = torch.cuda.Event()
-            fork.record(self.stream)
-            joins = []
-            for g, bs in zip(groups, self.branches):
-                bs.wait_event(fork)
-                _integrate(g, self.k)
-                j = torch.cuda.Event()
-                j.record(bs)
-                joins.append(j)
-            for j in joins:
-                self.stream.wait_event(j)
-        torch.cuda.synchronize()
+        self.batch = Batch(groups)
+        self.batch.capture(steps_per_replay, growth)
 
     @property
     def n_particles(self) -> int:
@@ -235,12 +250,14 @@ class EnsembleGraph:
 
     def replay(self):
         """Launches the graph on the current torch stream (asynchronous)."""
-        self.graph.replay()
+        self.batch.launch()
 
     def check(self):
-        """Raises the first error any group's kernels reported (synchronises)."""
-        for g in self.groups:
-            g.semi._call("tp_sync")
+        """Waits for the graph and raises the first error any group reported."""
+        self.batch.sync()
+
+    def close(self):
+        self.batch.close()
 
 
 def instance_state(g: Group, j: int):
