@@ -20,6 +20,7 @@ module TrixiParticlesGB300
 
 using CUDA: CUDA, CuArray, CuPtr
 using KernelAbstractions: KernelAbstractions
+using ChainRulesCore: ChainRulesCore
 using TrixiParticles: TrixiParticles, WeaklyCompressibleSPHSystem, WallBoundarySystem,
                       BoundaryModelDummyParticles, AdamiPressureExtrapolation,
                       ContinuityDensity, WendlandC2Kernel, StateEquationCole,
@@ -157,5 +158,64 @@ function integrate_ck2n54!(semi, v_ode, u_ode, t0, dt, nsteps)
     check(h, ccall((:tp_sync, libtp), Cint, (Ptr{Cvoid},), h))
     return v_ode, u_ode
 end
+
+# ---- Differentiation form: rrule of a fixed-step CarpenterKennedy2N54 solve -------------
+# Forward: tp_adjoint_forward advances (v, u) in place and checkpoints every `every` steps.
+# Pullback: tp_adjoint_backward maps the cotangents of the final (v, u) to those of the initial
+# (v0, u0) and returns the gradient with respect to (alpha, delta, |g|) of the handle's config.
+function solve_ck2n54(semi, v0::CuArray{Float64}, u0::CuArray{Float64}, dt, nsteps; every=25)
+    h = handle(semi)
+    v, u = copy(v0), copy(u0)
+    check(h, ccall((:tp_adjoint_forward, libtp), Cint,
+                   (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Float64, Int64, Int64),
+                   h, v, u, dt, nsteps, every))
+    return v, u
+end
+
+function ChainRulesCore.rrule(::typeof(solve_ck2n54), semi, v0, u0, dt, nsteps; every=25)
+    v, u = solve_ck2n54(semi, v0, u0, dt, nsteps; every)
+    function solve_ck2n54_pullback(ȳ)
+        v̄, ū = ChainRulesCore.unthunk.(ȳ)
+        vb = v̄ isa ChainRulesCore.AbstractZero ? CUDA.zeros(Float64, size(v)) : copy(v̄)
+        ub = ū isa ChainRulesCore.AbstractZero ? CUDA.zeros(Float64, size(u)) : copy(ū)
+        params = zeros(Float64, 3)   # (alpha, delta, gravity magnitude)
+        h = handle(semi)
+        check(h, ccall((:tp_adjoint_backward, libtp), Cint,
+                       (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Ptr{Float64}),
+                       h, vb, ub, params))
+        semī = ChainRulesCore.Tangent{typeof(semi)}(; parameters=params)
+        return (ChainRulesCore.NoTangent(), semī, vb, ub,
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+    end
+    return (v, u), solve_ck2n54_pullback
+end
+
+# ---- Batching form: several Semidiscretizations per CUDA-graph launch ----------------------
+# members: Vector of (semi, v::CuArray, u::CuArray, dt).  Returns the batch pointer.
+function batch_create(members; steps=5, autotune=true, growth=1.5)
+    hs = [handle(m[1]) for m in members]
+    b = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:tp_batch_create, libtp), Cint, (Ptr{Ptr{Cvoid}}, Int32, Ref{Ptr{Cvoid}}),
+               hs, length(hs), b)
+    st == 0 || error("tp_batch_create failed ($st)")
+    bcheck(st) = st == 0 || error(unsafe_string(ccall((:tp_batch_last_error, libtp), Cstring,
+                                                      (Ptr{Cvoid},), b[])))
+    for (k, (semi, v, u, dt)) in enumerate(members)
+        bcheck(ccall((:tp_batch_set_state, libtp), Cint,
+                     (Ptr{Cvoid}, Int32, CuPtr{Float64}, CuPtr{Float64}, Float64),
+                     b[], k - 1, v, u, dt))
+    end
+    autotune && bcheck(ccall((:tp_batch_autotune, libtp), Cint,
+                             (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}),
+                             b[], 3, C_NULL, C_NULL, C_NULL))
+    bcheck(ccall((:tp_batch_capture, libtp), Cint, (Ptr{Cvoid}, Int64, Float64),
+                 b[], steps, growth))
+    return b[]
+end
+
+batch_launch!(b) = ccall((:tp_batch_launch, libtp), Cint, (Ptr{Cvoid}, Ptr{Cvoid}),
+                         b, CUDA.stream().handle)
+batch_sync!(b) = ccall((:tp_batch_sync, libtp), Cint, (Ptr{Cvoid},), b)
+batch_destroy!(b) = ccall((:tp_batch_destroy, libtp), Cint, (Ptr{Cvoid},), b)
 
 end # module
