@@ -264,6 +264,7 @@ void setup_phys(tp_handle* h) {
     P.two_h = 2.0 * P.h;
     P.sr2 = P.two_h * P.two_h;
     P.almostzero = std::sqrt(std::nextafter(P.sr2, INFINITY) - P.sr2);
+    P.az2 = std::nextafter(P.sr2, INFINITY) - P.sr2;
     P.hi2 = P.h_inv * P.h_inv;
     P.wc2_norm = (c.ndims == 2) ? (7.0 / (4.0 * pi)) * (P.h_inv * P.h_inv)
                                 : (21.0 / (16.0 * pi)) * ((P.h_inv * P.h_inv) * P.h_inv);
@@ -436,6 +437,12 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
     TP_CUDA(h, grow(&h->l_ff, &h->cap_ff, cff, nf));
     TP_CUDA(h, grow(&h->l_fw, &h->cap_fw, cfw, nf));
     TP_CUDA(h, grow(&h->l_wf, &h->cap_wf, cwf, nw));
+    if (h->cfg.precision == TP_PRECISION_FP64) {
+        TP_CUDA(h, grow((unsigned**)&h->e_ff, &h->ecap_ff, cff, nf));
+        TP_CUDA(h, grow((unsigned**)&h->e_fw, &h->ecap_fw, cfw, nf));
+        if (!h->ec_ff) TP_CUDA(h, dalloc(&h->ec_ff, (size_t)std::max(nf, 1)));
+        if (!h->ec_fw) TP_CUDA(h, dalloc(&h->ec_fw, (size_t)std::max(nf, 1)));
+    }
     if (debug_sync_enabled())
         std::fprintf(stderr, "tp: lists maxcell_f=%d maxcell_w=%d cap ff=%d fw=%d wf=%d nf=%d nw=%d\n",
                      maxcell_f, h->maxcell_w, h->cap_ff, h->cap_fw, h->cap_wf, nf, nw);
@@ -694,7 +701,7 @@ tp_status tp_destroy(tp_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
-                    h->d_max};
+                    h->d_max, h->e_ff, h->e_fw, h->ec_ff, h->ec_fw};
     for (void* p : more)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {

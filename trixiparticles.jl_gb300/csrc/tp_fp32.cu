@@ -40,23 +40,6 @@ __device__ __forceinline__ float eos32_inverse_dev(float p, const Phys32& P) {
     return P.rho0 * expm1f(log1pf((p - P.p_bg) / P.B) * P.inv_gamma);
 }
 
-// o_a - o_b + (c_a - c_b) * cs from a list entry (same arithmetic as the list filter).
-template <int ND>
-__device__ __forceinline__ float pair_diff(float4 ta, float cs, unsigned e, float4 cb, float& pdx,
-                                           float& pdy, float& pdz) {
-    int dx, dy, dz;
-    decode_cell_offset(e, dx, dy, dz);
-    pdx = fmaf(-(float)dx, cs, ta.x) - cb.x;
-    pdy = fmaf(-(float)dy, cs, ta.y) - cb.y;
-    float d2 = fmaf(pdy, pdy, pdx * pdx);
-    pdz = 0.0f;
-    if (ND == 3) {
-        pdz = fmaf(-(float)dz, cs, ta.z) - cb.z;
-        d2 = fmaf(pdz, pdz, d2);
-    }
-    return d2;
-}
-
 // Source state -> fluid record slot.  SRC32: the integrator's FP32 velocity/density state
 // (float4 {v, rho - rho0}) and FP32 masses; otherwise the caller's FP64 v_ode and masses.
 template <int ND, bool SRC32>

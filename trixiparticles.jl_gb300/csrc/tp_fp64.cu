@@ -9,10 +9,15 @@
 // pair.  Plain `/` in the reference stays IEEE division here.
 //
 // Neighbour lists (tp_lists.cuh) are built with an FP32 distance on cell-relative offsets whose
-// bound is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative); the pair and Adami
-// kernels then decide every listed pair exactly in FP64 with explicitly rounded products and sums
-// (no FMA contraction), so the neighbour set {b : |x_a - x_b|^2 <= (2h)^2} is the one the CPU
-// computes, visited in the CPU's order.
+// bound is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative).  Before every pair
+// pass the exact-list filter reduces them to the pairs with |x_a - x_b|^2 <= (2h)^2 decided in
+// FP64 with explicitly rounded products and sums (no FMA contraction) wherever the FP32 test is
+// not conclusive; the Adami kernel decides its listed pairs the same way.  The neighbour set is
+// therefore the one the CPU computes, visited in the CPU's order.
+//
+// On GB300 an FP64 FMA issues at 1/64 of the FP32 rate (about 20 SM cycles per warp
+// instruction), so the pair kernel is FP64-throughput bound and the code spends FP32 and
+// integer work freely to save FP64 instructions.
 #include "tp_api_internal.h"
 #include "tp_lists.cuh"
 
@@ -52,7 +57,7 @@ struct Pack64 {
     int* id_out;
     double* m_out;
     double* xb_out;  // positions at the last rebuild (slot order), written on rebuild only
-    float4* test;
+    float4* test;    // offsets against the reference cell (the cell of the last rebuild)
     double4_32a* pos;
     double4_32a* vel;
     double2* aux;
@@ -68,7 +73,7 @@ struct Pack64 {
         const double rho = w[ND];
         const double p = eos_pressure(rho, P, P.fluid_clip);
         const double mi = m[i];
-        if (rebuild) test[s] = test_record_in<ND>(x, g, cs32, key);
+        test[s] = test_record_in<ND>(x, g, cs32, key);  // every stage: the exact-list filter
         pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
         vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
         aux[s] = make_double2(mi, fast_inv(rho));
@@ -184,15 +189,69 @@ struct Update64 {
     int first;
 };
 
+// Exact pair lists of this stage: the skin list of every fluid slot reduced to the pairs with
+// |x_a - x_b|^2 <= (2h)^2 (FP64, explicitly rounded products and sums), self excluded, in list
+// (PointNeighbors) order.  The FP32 distance on the cell-relative offsets decides every candidate
+// whose d^2 lies further than 1e-5 relative from the bound (its rounding error is below 1e-6
+// relative); only candidates inside that band are decided from the FP64 records.  FP64
+// arithmetic runs at 1/64 of the FP32 rate on this GPU, so removing the ~25 % of listed
+// candidates that lie in the skin shell from the FP64 pair loop is worth an extra pass.
+template <int ND>
+__device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float cs, float lo2,
+                                           float hi2, double sr2, const double4_32a& pa,
+                                           const float4* __restrict__ test,
+                                           const double4_32a* __restrict__ pos,
+                                           const unsigned* __restrict__ list,
+                                           int cnt, bool skip_self, int* __restrict__ out) {
+    int n = 0;
+    for (int k = 0; k < cnt; ++k) {
+        const unsigned e = list[(size_t)k * n_rows + s];
+        const int b = (int)(e & kSlotMask);
+        if (skip_self && b == s) continue;
+        float p0, p1, p2;
+        const float d2f = pair_diff<ND>(ta, cs, e, test[b], p0, p1, p2);
+        bool acc = d2f <= lo2;
+        if (!acc && d2f <= hi2) {
+            const double4_32a pb = pos[b];
+            acc = dist2_rn<ND>(pa.x - pb.x, pa.y - pb.y, ND == 3 ? pa.z - pb.z : 0.0) <= sr2;
+        }
+        if (acc) out[(size_t)(n++) * n_rows + s] = b;
+    }
+    return n;
+}
+
+template <int ND>
+__global__ void __launch_bounds__(256) k_filter64(
+    double sr2, float cs, float lo2, float hi2, int nf, const float4* __restrict__ ftest,
+    const double4_32a* __restrict__ fpos, const unsigned* __restrict__ ff,
+    const int* __restrict__ ffc, const unsigned* __restrict__ fw, const int* __restrict__ fwc,
+    const float4* __restrict__ wtest, const double4_32a* __restrict__ wpos, int* __restrict__ eff,
+    int* __restrict__ effc, int* __restrict__ efw, int* __restrict__ efwc) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const float4 ta = ftest[s];
+    const double4_32a pa = fpos[s];
+    effc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, ftest, fpos, ff, ffc[s], true,
+                              eff);
+    efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, wtest, wpos, fw, fwc[s], false,
+                              efw);
+}
+
+// Pair terms in the reference's order (rhs.jl:81-117), FP64 throughout, with the arithmetic
+// arranged for the slow FP64 pipe: one reciprocal square root per pair gives both
+// r = d^2 * rsqrt(d^2) and the 1/r^2 of the density diffusion; 1 / (rho_a rho_b) is the
+// product of the per-particle fast_inv(rho) values of the pack; the zero-distance skip
+// `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28) is tested as d^2 < eps((2h)^2).  Each of these
+// differs from the reference's expression by a few ulp at most.
 template <int ND, bool INTEGRATE>
 __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
                                                 const double4_32a* __restrict__ fpos,
                                                 const double4_32a* __restrict__ fvel,
                                                 const double2* __restrict__ faux,
-                                                const unsigned* __restrict__ ff,
-                                                const int* __restrict__ ffc,
-                                                const unsigned* __restrict__ fw,
-                                                const int* __restrict__ fwc,
+                                                const int* __restrict__ eff,
+                                                const int* __restrict__ effc,
+                                                const int* __restrict__ efw,
+                                                const int* __restrict__ efwc,
                                                 const double4_32a* __restrict__ wpos,
                                                 const double4_32a* __restrict__ wstate,
                                                 unsigned* __restrict__ gate, Update64 U) {
@@ -201,30 +260,30 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
-    const double p_a = pa.w, rho_a = va.w;
+    const double p_a = pa.w, rho_a = va.w, ia = faux[s].y;
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
-    const int nff = ffc[s];
+    const int nff = effc[s];
     for (int k = 0; k < nff; ++k) {
-        const int b = (int)(ff[(size_t)k * nf + s] & kSlotMask);
+        const int b = eff[(size_t)k * nf + s];
         const double4_32a pb = fpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-        if (d2 > P.sr2) continue;
-        const double r = sqrt(d2);
-        if (r < P.almostzero) continue;
+        if (d2 < P.az2) continue;
+        const double ir = rsqrt(d2);
+        const double r = d2 * ir;
         const double4_32a vb = fvel[b];
         const double2 ab = faux[b];  // {m_b, fast_inv(rho_b)}
-        const double m_b = ab.x, rho_b = vb.w;
+        const double m_b = ab.x, rho_b = vb.w, ib = ab.y;
         // WendlandC2 kernel_deriv_div_r_unsafe * pos_diff
         const double q = r * P.h_inv;
-        const double t = 1.0 - q / 2.0;
+        const double t = 1.0 - 0.5 * q;
         const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
         const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
         // pressure_acceleration_continuity_density
-        const double coef = (-m_b) * div_fast(p_a + pb.w, rho_a * rho_b);
+        const double coef = (-m_b) * ((p_a + pb.w) * (ia * ib));
         dv0 += coef * g0;
         dv1 += coef * g1;
         if (ND == 3) dv2 += coef * g2;
@@ -235,7 +294,7 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
             if (ND == 3) vr += vd2 * pd2;
             if (vr < 0.0) {
                 const double rho_mean = (rho_a + rho_b) / 2.0;
-                const double mu = div_fast(P.visc_h * vr, r * r + P.visc_eps_h2);
+                const double mu = div_fast(P.visc_h * vr, d2 + P.visc_eps_h2);
                 const double num = ((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu);
                 const double f = div_fast(num, rho_mean);
                 dv0 += f * g0;
@@ -245,10 +304,10 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         }
         double vg = vd0 * g0 + vd1 * g1;
         if (ND == 3) vg += vd2 * g2;
-        drho += ((rho_a * ab.y) * m_b) * vg;
+        drho += ((rho_a * ib) * m_b) * vg;
         if (P.diff) {
-            const double vol_b = m_b * ab.y;
-            const double pc = div_fast(2.0 * (rho_a - rho_b), r * r);
+            const double vol_b = m_b * ib;
+            const double pc = (2.0 * (rho_a - rho_b)) * (ir * ir);
             double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
             if (ND == 3) pg += (pc * pd2) * g2;
             drho += P.diff_coef * (vol_b * pg);
@@ -257,29 +316,28 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
 
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion) ----
     double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
-    const int nfw = fwc[s];
+    const int nfw = efwc[s];
     for (int k = 0; k < nfw; ++k) {
-        const int b = (int)(fw[(size_t)k * nf + s] & kSlotMask);
+        const int b = efw[(size_t)k * nf + s];
         const double4_32a pb = wpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
-        if (d2 > P.sr2) continue;
-        const double r = sqrt(d2);
-        if (r < P.almostzero) continue;
+        if (d2 < P.az2) continue;
+        const double r = d2 * rsqrt(d2);
         const double4_32a sb = wstate[b];  // {p, rho, fast_inv(rho), 0}
-        const double m_b = pb.w, p_b = sb.x, rho_b = sb.y;
+        const double m_b = pb.w, p_b = sb.x, ib = sb.z;
         const double q = r * P.h_inv;
-        const double t = 1.0 - q / 2.0;
+        const double t = 1.0 - 0.5 * q;
         const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
         const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        const double coef = (-m_b) * div_fast(p_a + p_b, rho_a * rho_b);
+        const double coef = (-m_b) * ((p_a + p_b) * (ia * ib));
         ew0 += coef * g0;
         ew1 += coef * g1;
         if (ND == 3) ew2 += coef * g2;
         double vg = va.x * g0 + va.y * g1;
         if (ND == 3) vg += va.z * g2;
-        erho += ((rho_a * sb.z) * m_b) * vg;
+        erho += ((rho_a * ib) * m_b) * vg;
     }
 
     // dv = ((0 + S_ff) + S_fw) + g ;  drho = S_ff + S_fw
@@ -433,10 +491,16 @@ void fp64_adami(tp_handle* h) {
 template <int ND, bool INTEG>
 static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
+    const double sr2 = h->phys.sr2;
+    k_filter64<ND><<<nblk(nf, 256), 256, 0, h->stream>>>(
+        sr2, (float)h->grid.cs, (float)(sr2 * (1.0 - 1e-5)), (float)(sr2 * (1.0 + 1e-5)), nf,
+        h->f_test, (const double4_32a*)h->f_pos, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test,
+        (const double4_32a*)h->w_pos, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw);
     k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
         h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
-        (const double2*)h->f_aux, h->l_ff, h->c_ff, h->l_fw, h->c_fw,
+        (const double2*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
         (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);
+    h->launches += 1;  // the filter (the pair launch is counted by the caller)
 }
 
 void fp64_pair_kick(tp_handle* h, double* dv) {

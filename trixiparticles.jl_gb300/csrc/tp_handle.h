@@ -82,6 +82,13 @@ struct tp_handle {
     int* c_fw = nullptr;
     int* c_wf = nullptr;
     int cap_ff = 0, cap_fw = 0, cap_wf = 0;
+    // FP64 form: the exact pair lists of the current stage (|x_a - x_b| <= 2h, self excluded),
+    // filtered from l_ff / l_fw before every pair pass; plain slot indices, same layout
+    int* e_ff = nullptr;
+    int* e_fw = nullptr;
+    int* ec_ff = nullptr;
+    int* ec_fw = nullptr;
+    int ecap_ff = 0, ecap_fw = 0;
     double skin = 0.1;          // list radius 2h (1 + skin); rebuild after skin * h displacement
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
     unsigned* gate = nullptr;   // {force, max displacement bits, half-skin bits}

@@ -43,6 +43,7 @@ struct Phys {
     double sr2;        // (2h)^2, neighbour criterion d2 <= sr2
     double two_h;      // compact support 2h (kernel() cut, strict <)
     double almostzero; // sqrt(eps((2h)^2)), rhs.jl:27-28
+    double az2;        // eps((2h)^2): the zero-distance skip on d^2
     double wc2_norm;   // WendlandC2 normalisation sigma_d * h_inv^d (smoothing_kernels.jl:450-455)
     double wc2_dnorm;  // -5 * wc2_norm (kernel_deriv_div_r_unsafe prefactor)
     double hi2;        // h_inv * h_inv

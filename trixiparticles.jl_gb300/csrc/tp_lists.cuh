@@ -27,6 +27,23 @@ __device__ __forceinline__ void decode_cell_offset(unsigned e, int& dx, int& dy,
     dz = code / 9 - 1;
 }
 
+// o_a - o_b + (c_a - c_b) * cs from a list entry (same arithmetic as the list filter).
+template <int ND>
+__device__ __forceinline__ float pair_diff(float4 ta, float cs, unsigned e, float4 cb, float& pdx,
+                                           float& pdy, float& pdz) {
+    int dx, dy, dz;
+    decode_cell_offset(e, dx, dy, dz);
+    pdx = fmaf(-(float)dx, cs, ta.x) - cb.x;
+    pdy = fmaf(-(float)dy, cs, ta.y) - cb.y;
+    float d2 = fmaf(pdy, pdy, pdx * pdx);
+    pdz = 0.0f;
+    if (ND == 3) {
+        pdz = fmaf(-(float)dz, cs, ta.z) - cb.z;
+        d2 = fmaf(pdz, pdz, d2);
+    }
+    return d2;
+}
+
 // Largest displacement since the last rebuild -> gate[1] (float bits, atomicMax on unsigned).
 template <int ND>
 __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__ u,
