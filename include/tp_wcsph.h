@@ -221,6 +221,17 @@ tp_status tp_set_skin(tp_handle* h, double skin);
  */
 tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth);
 
+/*
+ * FP64 pair-pass mode.  TP_PAIR_GATHER: every fluid particle sums its own pair terms in the
+ * reference's neighbour order (bitwise reproducible run to run).  TP_PAIR_SYMMETRIC (default for
+ * the FP64 form): every fluid-fluid pair is evaluated once and its two halves go to both
+ * particles (the second by an FP64 atomic add), which halves the FP64 work of the pair pass; the
+ * terms are the same, their summation order is not, so results differ from the gather mode in
+ * the last bits and are not bitwise reproducible.  The FP32 form always gathers.
+ */
+enum { TP_PAIR_GATHER = 0, TP_PAIR_SYMMETRIC = 1 };
+tp_status tp_set_pair_mode(tp_handle* h, int32_t mode);
+
 /* Copy of the configuration the handle was created with. */
 tp_status tp_get_config(const tp_handle* h, tp_config* out);
 

@@ -38,6 +38,8 @@ static int run(int nd, int precision) {
     bad |= tp_set_skin(h, 0.2) != TP_OK;
     bad |= tp_set_launch(h, 256) != TP_OK;
     bad |= tp_set_launch(h, 100) != TP_ERR_ARGUMENT;
+    bad |= tp_set_pair_mode(h, 5) != TP_ERR_ARGUMENT;
+    bad |= tp_set_pair_mode(h, precision == 0 ? TP_PAIR_GATHER : TP_PAIR_SYMMETRIC) != TP_OK;
     bad |= tp_prepare_lists(h, u.data(), 1.5) != TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 2) != TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 1) != TP_OK;

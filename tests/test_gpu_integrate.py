@@ -12,11 +12,14 @@ from helpers import dam_break_case, initial_state, oracle_model, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def _integrate(pkg, orc, cuda, nd, dx, fluid, tank, n_steps, dt, precision, jitter=0.0):
+def _integrate(pkg, orc, cuda, nd, dx, fluid, tank, n_steps, dt, precision, jitter=0.0,
+               pair_mode=None):
     torch = cuda
     semi, tank_ = dam_break_case(pkg, nd, dx, fluid, tank, precision=precision, jitter=jitter,
                                  seed=1)
     ode = pkg.semidiscretize(semi, (0.0, n_steps * dt))
+    if pair_mode is not None:
+        semi._call("tp_set_pair_mode", pair_mode)
     sol = pkg.solve(ode, pkg.CarpenterKennedy2N54(), dt=dt, n_steps=n_steps)
     model = oracle_model(orc, semi, tank_)
     v0, u0 = initial_state(tank_)
@@ -26,9 +29,10 @@ def _integrate(pkg, orc, cuda, nd, dx, fluid, tank, n_steps, dt, precision, jitt
     return out
 
 
-def test_integrate_fp64_2d(pkg, orc, cuda):
+@pytest.mark.parametrize("mode", [0, 1], ids=["gather", "symmetric"])
+def test_integrate_fp64_2d(pkg, orc, cuda, mode):
     v, u, v_ref, u_ref, semi = _integrate(pkg, orc, cuda, 2, 0.02, (2.0, 1.0), (5.366, 4.0),
-                                          40, 1e-4, "float64")
+                                          40, 1e-4, "float64", pair_mode=mode)
     nd = 2
     vr, vg = v_ref.reshape(-1, nd + 1), v.reshape(-1, nd + 1)
     assert rel_l2(u, u_ref) <= 1e-12

@@ -1,8 +1,10 @@
 """kick!/drift! on the GPU against the FP64 oracle.
 
 Tolerances: the FP64 drop-in differs from the CPU oracle only by FMA contraction in the pair
-sums, CUDA's pow in the Cole EOS and the reference's CUDA `div_fast` (relative error < 1e-15
-per division, ext/TrixiParticlesCUDAExt.jl): relative L2 error of dv <= 1e-11.  The FP32
+sums, CUDA's pow in the Cole EOS, the reference's CUDA `div_fast` (relative error < 1e-15
+per division, ext/TrixiParticlesCUDAExt.jl), ulp-level rearrangements of reciprocals and square
+roots, and -- in the symmetric pair mode -- the summation order: relative L2 error of
+dv <= 1e-11 in both pair modes; the gather mode is bitwise reproducible.  The FP32
 precision form is held to 2e-5 relative L2 on the velocity rows and 1e-4 on the density rate.
 """
 import numpy as np
@@ -29,11 +31,13 @@ def _state(tank, case, seed=11):
     return v, u
 
 
-def _run(pkg, orc, cuda, case, precision):
+def _run(pkg, orc, cuda, case, precision, pair_mode=None):
     torch = cuda
     semi, tank = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"],
                                 jitter=case["jitter"], seed=5, precision=precision)
     ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    if pair_mode is not None:
+        semi._call("tp_set_pair_mode", pair_mode)
     v, u = _state(tank, case)
     v_t = torch.as_tensor(v.ravel(), device=semi.device)
     u_t = torch.as_tensor(u.ravel(), device=semi.device)
@@ -52,9 +56,10 @@ def _run(pkg, orc, cuda, case, precision):
     return out, dv_ref, ref, case["ndims"]
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["gather", "symmetric"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c['ndims']}d-j{c['jitter']}-v{c['vel']}")
-def test_kick_fp64_matches_oracle(pkg, orc, cuda, case):
-    out, dv_ref, ref, nd = _run(pkg, orc, cuda, case, "float64")
+def test_kick_fp64_matches_oracle(pkg, orc, cuda, case, mode):
+    out, dv_ref, ref, nd = _run(pkg, orc, cuda, case, "float64", pair_mode=mode)
     assert np.all(np.isfinite(out["dv"]))
     assert rel_l2(out["dv"], dv_ref) <= 1e-11
     g = out["dv"].reshape(-1, nd + 1)
@@ -133,4 +138,20 @@ def test_fluid_momentum_conservation(pkg, orc, cuda):
     mom = (m[:, None] * a).sum(0)
     scale = (m[:, None] * np.abs(a)).sum()
     assert np.all(np.abs(mom) <= 1e-13 * scale)
+    semi.close()
+
+
+def test_kick_fp64_gather_mode_is_reproducible(pkg, orc, cuda):
+    case = CASES[1]
+    a, _, _, _ = _run(pkg, orc, cuda, case, "float64", pair_mode=0)
+    b, _, _, _ = _run(pkg, orc, cuda, case, "float64", pair_mode=0)
+    assert np.array_equal(a["dv"], b["dv"])
+
+
+def test_pair_mode_argument_check(pkg, cuda):
+    case = CASES[0]
+    semi, _ = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"])
+    pkg.semidiscretize(semi, (0.0, 1.0))
+    with pytest.raises(pkg.TpError):
+        semi._call("tp_set_pair_mode", 7)
     semi.close()

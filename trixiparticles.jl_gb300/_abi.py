@@ -107,6 +107,7 @@ PROTOTYPES = [
     ("tp_adjoint_backward", c_int32, [c_void_p, c_void_p, c_void_p, POINTER(c_double)]),
     ("tp_adjoint_kernel_launches", c_int64, [c_void_p]),
     ("tp_get_config", c_int32, [c_void_p, POINTER(TpConfig)]),
+    ("tp_set_pair_mode", c_int32, [c_void_p, c_int32]),
     ("tp_batch_create", c_int32, [c_void_p, c_int32, c_void_p]),
     ("tp_batch_destroy", c_int32, [c_void_p]),
     ("tp_batch_set_state", c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_double]),
@@ -120,6 +121,8 @@ PROTOTYPES = [
     ("tp_last_error", c_char_p, [c_void_p]),
 ]
 
+TP_PAIR_GATHER = 0
+TP_PAIR_SYMMETRIC = 1
 TP_NOALLOC_MAX_PARTICLES = 262144
 TP_NOALLOC_MAX_CELLS = 524288
 

@@ -442,6 +442,11 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
         TP_CUDA(h, grow((unsigned**)&h->e_fw, &h->ecap_fw, cfw, nf));
         if (!h->ec_ff) TP_CUDA(h, dalloc(&h->ec_ff, (size_t)std::max(nf, 1)));
         if (!h->ec_fw) TP_CUDA(h, dalloc(&h->ec_fw, (size_t)std::max(nf, 1)));
+        if (!h->acc) {
+            TP_CUDA(h, dalloc(&h->acc, (size_t)std::max(nf, 1) * 4));
+            TP_CUDA(h, cudaMemsetAsync(h->acc, 0, (size_t)std::max(nf, 1) * 4 * sizeof(double),
+                                       h->stream));
+        }
     }
     if (debug_sync_enabled())
         std::fprintf(stderr, "tp: lists maxcell_f=%d maxcell_w=%d cap ff=%d fw=%d wf=%d nf=%d nw=%d\n",
@@ -701,7 +706,7 @@ tp_status tp_destroy(tp_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
-                    h->d_max, h->e_ff, h->e_fw, h->ec_ff, h->ec_fw};
+                    h->d_max, h->e_ff, h->e_fw, h->ec_ff, h->ec_fw, h->acc};
     for (void* p : more)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
@@ -1068,6 +1073,14 @@ tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth) {
     st = ensure_state(h);
     if (st != TP_OK) return st;
     h->lists_fixed = true;
+    return TP_OK;
+}
+
+tp_status tp_set_pair_mode(tp_handle* h, int32_t mode) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (mode != TP_PAIR_GATHER && mode != TP_PAIR_SYMMETRIC)
+        return fail(h, TP_ERR_ARGUMENT, "pair mode must be TP_PAIR_GATHER or TP_PAIR_SYMMETRIC");
+    h->pair_mode = mode;
     return TP_OK;
 }
 

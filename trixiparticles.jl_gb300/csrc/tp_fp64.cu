@@ -189,6 +189,35 @@ struct Update64 {
     int first;
 };
 
+// kick!: dv write in caller order; integrator: CarpenterKennedy2N54 stage of slot s,
+// tmp = A*tmp + dt*k ; y = y + B*tmp (du = v at stage start).
+template <int ND, bool INTEGRATE>
+__device__ __forceinline__ void stage_update(int s, const double4_32a& pa, const double4_32a& va,
+                                             const double (&k)[4], const Update64& U) {
+    if (!INTEGRATE) {
+        const int i = U.perm[s];
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
+    } else {
+        const double va_arr[4] = {va.x, va.y, ND == 3 ? va.z : va.w, va.w};
+        const double xa_arr[3] = {pa.x, pa.y, pa.z};
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) {
+            const double kv = k[d];
+            double tv = U.first ? U.dt * kv : fma(U.dt, kv, U.A * U.tv[(size_t)s * (ND + 1) + d]);
+            U.tv[(size_t)s * (ND + 1) + d] = tv;
+            U.v_out[(size_t)s * (ND + 1) + d] = fma(U.B, tv, va_arr[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double ku = va_arr[d];
+            double tu = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
+            U.tu[(size_t)s * ND + d] = tu;
+            U.u_out[(size_t)s * ND + d] = fma(U.B, tu, xa_arr[d]);
+        }
+    }
+}
+
 // Exact pair lists of this stage: the skin list of every fluid slot reduced to the pairs with
 // |x_a - x_b|^2 <= (2h)^2 (FP64, explicitly rounded products and sums), self excluded, in list
 // (PointNeighbors) order.  The FP32 distance on the cell-relative offsets decides every candidate
@@ -202,12 +231,14 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
                                            const float4* __restrict__ test,
                                            const double4_32a* __restrict__ pos,
                                            const unsigned* __restrict__ list,
-                                           int cnt, bool skip_self, int* __restrict__ out) {
+                                           int cnt, int skip, int* __restrict__ out) {
+    // skip: 0 keep all (walls), 1 drop self (fluid, gather mode), 2 keep b > s only (fluid,
+    // symmetric mode: every pair once, at its lower slot)
     int n = 0;
     for (int k = 0; k < cnt; ++k) {
         const unsigned e = list[(size_t)k * n_rows + s];
         const int b = (int)(e & kSlotMask);
-        if (skip_self && b == s) continue;
+        if ((skip == 1 && b == s) || (skip == 2 && b <= s)) continue;
         float p0, p1, p2;
         const float d2f = pair_diff<ND>(ta, cs, e, test[b], p0, p1, p2);
         bool acc = d2f <= lo2;
@@ -226,15 +257,14 @@ __global__ void __launch_bounds__(256) k_filter64(
     const double4_32a* __restrict__ fpos, const unsigned* __restrict__ ff,
     const int* __restrict__ ffc, const unsigned* __restrict__ fw, const int* __restrict__ fwc,
     const float4* __restrict__ wtest, const double4_32a* __restrict__ wpos, int* __restrict__ eff,
-    int* __restrict__ effc, int* __restrict__ efw, int* __restrict__ efwc) {
+    int* __restrict__ effc, int* __restrict__ efw, int* __restrict__ efwc, int half) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nf) return;
     const float4 ta = ftest[s];
     const double4_32a pa = fpos[s];
-    effc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, ftest, fpos, ff, ffc[s], true,
-                              eff);
-    efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, wtest, wpos, fw, fwc[s], false,
-                              efw);
+    effc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, ftest, fpos, ff, ffc[s],
+                              half ? 2 : 1, eff);
+    efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, wtest, wpos, fw, fwc[s], 0, efw);
 }
 
 // Pair terms in the reference's order (rhs.jl:81-117), FP64 throughout, with the arithmetic
@@ -346,30 +376,145 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     k[1] = (dv1 + ew1) + P.g[1];
     k[2] = (ND == 3) ? (dv2 + ew2) + P.g[2] : 0.0;
     k[ND] = drho + erho;
+    stage_update<ND, INTEGRATE>(s, pa, va, k, U);
+}
 
-    if (!INTEGRATE) {
-        const int i = U.perm[s];
-#pragma unroll
-        for (int d = 0; d <= ND; ++d) U.dv[(size_t)i * (ND + 1) + d] = k[d];
-    } else {
-        // CarpenterKennedy2N54 stage: tmp = A*tmp + dt*k ; u = u + B*tmp (du = v at stage start)
-        const double va_arr[4] = {va.x, va.y, ND == 3 ? va.z : va.w, va.w};
-        const double xa_arr[3] = {pa.x, pa.y, pa.z};
-#pragma unroll
-        for (int d = 0; d <= ND; ++d) {
-            const double kv = k[d];
-            double tv = U.first ? U.dt * kv : fma(U.dt, kv, U.A * U.tv[(size_t)s * (ND + 1) + d]);
-            U.tv[(size_t)s * (ND + 1) + d] = tv;
-            U.v_out[(size_t)s * (ND + 1) + d] = fma(U.B, tv, va_arr[d]);
+// Symmetric pair pass: every fluid-fluid pair once, at its lower slot a (the exact half list
+// holds b > a).  The terms of b are the ones b would evaluate itself -- with x_ba = -x_ab,
+// v_ba = -v_ab and grad W_ba = -grad W_ab the shared factors (kernel gradient, pressure sum over
+// rho_a rho_b, mu and 1/rho_mean, v_ab . grad W, the diffusion projection) are evaluated once --
+// and reach b through FP64 atomic adds into its accumulator {dv, drho}; a adds its own sum once
+// at the end.  Fluid-wall pairs stay one-sided.  k_update64 then applies gravity and the stage.
+template <int ND>
+__global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
+                                                 const double4_32a* __restrict__ fpos,
+                                                 const double4_32a* __restrict__ fvel,
+                                                 const double2* __restrict__ faux,
+                                                 const int* __restrict__ eff,
+                                                 const int* __restrict__ effc,
+                                                 const int* __restrict__ efw,
+                                                 const int* __restrict__ efwc,
+                                                 const double4_32a* __restrict__ wpos,
+                                                 const double4_32a* __restrict__ wstate,
+                                                 double* __restrict__ acc,
+                                                 unsigned* __restrict__ gate) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
+    if (s >= nf) return;
+    const double4_32a pa = fpos[s];
+    const double4_32a va = fvel[s];
+    const double2 aa = faux[s];
+    const double p_a = pa.w, rho_a = va.w, m_a = aa.x, ia = aa.y;
+
+    double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
+    const int nff = effc[s];
+    for (int k = 0; k < nff; ++k) {
+        const int b = eff[(size_t)k * nf + s];
+        const double4_32a pb = fpos[b];
+        const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
+        const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
+        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        if (d2 < P.az2) continue;
+        const double ir = rsqrt(d2);
+        const double r = d2 * ir;
+        const double4_32a vb = fvel[b];
+        const double2 ab = faux[b];
+        const double m_b = ab.x, rho_b = vb.w, ib = ab.y;
+        const double q = r * P.h_inv;
+        const double t = 1.0 - 0.5 * q;
+        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+        // pressure: a gets -m_b X grad W_ab, b gets -m_a X grad W_ba = m_a X grad W_ab
+        const double X = (p_a + pb.w) * (ia * ib);
+        const double ca = (-m_b) * X, cb = m_a * X;
+        dv0 += ca * g0;
+        dv1 += ca * g1;
+        if (ND == 3) dv2 += ca * g2;
+        double b0 = cb * g0, b1 = cb * g1, b2 = cb * g2;
+        const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
+        const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
+        if (P.visc) {
+            double vr = vd0 * pd0 + vd1 * pd1;
+            if (ND == 3) vr += vd2 * pd2;
+            if (vr < 0.0) {
+                const double rho_mean = (rho_a + rho_b) / 2.0;
+                const double mu = div_fast(P.visc_h * vr, d2 + P.visc_eps_h2);
+                const double R = fast_inv(rho_mean);
+                const double fa = (((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu)) * R;
+                const double fb = (((m_a * P.alpha) * P.c) * mu + (m_a * P.beta) * (mu * mu)) * R;
+                dv0 += fa * g0;
+                dv1 += fa * g1;
+                if (ND == 3) dv2 += fa * g2;
+                b0 -= fb * g0;
+                b1 -= fb * g1;
+                b2 -= fb * g2;
+            }
         }
-#pragma unroll
-        for (int d = 0; d < ND; ++d) {
-            const double ku = va_arr[d];
-            double tu = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
-            U.tu[(size_t)s * ND + d] = tu;
-            U.u_out[(size_t)s * ND + d] = fma(U.B, tu, xa_arr[d]);
+        double vg = vd0 * g0 + vd1 * g1;
+        if (ND == 3) vg += vd2 * g2;
+        drho += ((rho_a * ib) * m_b) * vg;
+        double br = ((rho_b * ia) * m_a) * vg;
+        if (P.diff) {
+            const double pc = (2.0 * (rho_a - rho_b)) * (ir * ir);
+            double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
+            if (ND == 3) pg += (pc * pd2) * g2;
+            drho += P.diff_coef * ((m_b * ib) * pg);
+            br += P.diff_coef * ((m_a * ia) * (-pg));
         }
+        double* ab4 = acc + (size_t)b * 4;
+        atomicAdd(ab4 + 0, b0);
+        atomicAdd(ab4 + 1, b1);
+        if (ND == 3) atomicAdd(ab4 + 2, b2);
+        atomicAdd(ab4 + 3, br);
     }
+
+    const int nfw = efwc[s];
+    for (int k = 0; k < nfw; ++k) {
+        const int b = efw[(size_t)k * nf + s];
+        const double4_32a pb = wpos[b];
+        const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
+        const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
+        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        if (d2 < P.az2) continue;
+        const double r = d2 * rsqrt(d2);
+        const double4_32a sb = wstate[b];
+        const double m_b = pb.w, p_b = sb.x, ib = sb.z;
+        const double q = r * P.h_inv;
+        const double t = 1.0 - 0.5 * q;
+        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
+        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
+        const double coef = (-m_b) * ((p_a + p_b) * (ia * ib));
+        dv0 += coef * g0;
+        dv1 += coef * g1;
+        if (ND == 3) dv2 += coef * g2;
+        double vg = va.x * g0 + va.y * g1;
+        if (ND == 3) vg += va.z * g2;
+        drho += ((rho_a * ib) * m_b) * vg;
+    }
+    double* a4 = acc + (size_t)s * 4;
+    atomicAdd(a4 + 0, dv0);
+    atomicAdd(a4 + 1, dv1);
+    if (ND == 3) atomicAdd(a4 + 2, dv2);
+    atomicAdd(a4 + 3, drho);
+}
+
+// Gravity + stage update (or the kick! write) from the symmetric pass's accumulators, which are
+// cleared for the next pass.
+template <int ND, bool INTEGRATE>
+__global__ void __launch_bounds__(256) k_update64(Phys P, int nf,
+                                                  const double4_32a* __restrict__ fpos,
+                                                  const double4_32a* __restrict__ fvel,
+                                                  double* __restrict__ acc, Update64 U) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    double4_32a a4 = *(const double4_32a*)(acc + (size_t)s * 4);
+    *(double4_32a*)(acc + (size_t)s * 4) = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    double k[4];
+    k[0] = a4.x + P.g[0];
+    k[1] = a4.y + P.g[1];
+    k[2] = (ND == 3) ? a4.z + P.g[2] : 0.0;
+    k[ND] = a4.w;
+    stage_update<ND, INTEGRATE>(s, fpos[s], fvel[s], k, U);
 }
 
 // Neighbour counting (diagnostics): fluid-fluid, fluid-wall for fluid slots, or wall-fluid.
@@ -492,15 +637,26 @@ template <int ND, bool INTEG>
 static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
     const double sr2 = h->phys.sr2;
+    const bool sym = h->pair_mode == TP_PAIR_SYMMETRIC;
     k_filter64<ND><<<nblk(nf, 256), 256, 0, h->stream>>>(
         sr2, (float)h->grid.cs, (float)(sr2 * (1.0 - 1e-5)), (float)(sr2 * (1.0 + 1e-5)), nf,
         h->f_test, (const double4_32a*)h->f_pos, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test,
-        (const double4_32a*)h->w_pos, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw);
-    k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
-        h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
-        (const double2*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
-        (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);
-    h->launches += 1;  // the filter (the pair launch is counted by the caller)
+        (const double4_32a*)h->w_pos, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw, sym ? 1 : 0);
+    if (sym) {
+        k_pair64s<ND><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
+            h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
+            (const double2*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
+            (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, h->acc, gate);
+        k_update64<ND, INTEG><<<nblk(nf, 256), 256, 0, h->stream>>>(
+            h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->acc, U);
+        h->launches += 2;  // filter + update (the pair launch is counted by the caller)
+    } else {
+        k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
+            h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
+            (const double2*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
+            (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);
+        h->launches += 1;  // the filter
+    }
 }
 
 void fp64_pair_kick(tp_handle* h, double* dv) {

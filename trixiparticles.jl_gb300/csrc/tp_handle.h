@@ -89,6 +89,9 @@ struct tp_handle {
     int* ec_ff = nullptr;
     int* ec_fw = nullptr;
     int ecap_ff = 0, ecap_fw = 0;
+    // FP64 form, symmetric pair mode: per-slot accumulator {dv (3), drho} of the pair pass
+    double* acc = nullptr;
+    int pair_mode = 1;  // TP_PAIR_SYMMETRIC (FP64 default) or TP_PAIR_GATHER
     double skin = 0.1;          // list radius 2h (1 + skin); rebuild after skin * h displacement
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
     unsigned* gate = nullptr;   // {force, max displacement bits, half-skin bits}
