@@ -289,6 +289,11 @@ void setup_phys(tp_handle* h) {
     P.diff_coef = (P.delta * ((P.h + P.h) / 2.0)) * P.c;
     for (int d = 0; d < 3; ++d) P.g[d] = (d < c.ndims) ? c.acceleration[d] : 0.0;
     P.p_off = c.pressure_offset;
+    P.sg_c = P.wc2_dnorm * P.hi2;
+    P.half_hinv = 0.5 * P.h_inv;
+    P.alpha_c = P.alpha * P.c;
+    P.visc_k = P.alpha_c * P.visc_h;
+    P.diff2 = 2.0 * P.diff_coef;
 
     Phys32& Q = h->phys32;
     const float h32 = (float)P.h;
@@ -658,7 +663,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->f_test, nf));
     A(dalloc((double4_32a**)&h->f_pos, nf));
     A(dalloc((double4_32a**)&h->f_vel, nf));
-    A(dalloc((double2**)&h->f_aux, nf));
+    A(dalloc((double4_32a**)&h->f_aux, nf));
     A(dalloc(&h->m_f, nf));
     A(dalloc(&h->w_key, nw));
     A(dalloc(&h->w_tmp, nw));

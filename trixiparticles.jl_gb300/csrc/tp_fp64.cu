@@ -60,7 +60,7 @@ struct Pack64 {
     float4* test;    // offsets against the reference cell (the cell of the last rebuild)
     double4_32a* pos;
     double4_32a* vel;
-    double2* aux;
+    double4_32a* aux;  // {m, m / rho, 1 / rho, 0} with 1 / rho = fast_inv(rho)
     GridDesc g;
     double cs32;
     Phys P;
@@ -76,7 +76,8 @@ struct Pack64 {
         test[s] = test_record_in<ND>(x, g, cs32, key);  // every stage: the exact-list filter
         pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
         vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
-        aux[s] = make_double2(mi, fast_inv(rho));
+        const double ir = fast_inv(rho);
+        aux[s] = make_double4_32a(mi, mi * ir, ir, 0.0);
         if (rebuild && xb_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
@@ -168,7 +169,8 @@ __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_3
     if (V > 2.220446049250313e-16) Ps = Ps / V;
     if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
     const double rho_w = eos_inverse(Ps, P);
-    wstate[w] = make_double4_32a(Ps, rho_w, fast_inv(rho_w), 0.0);
+    const double ir_w = fast_inv(rho_w);
+    wstate[w] = make_double4_32a(Ps, rho_w, ir_w, xw.w * ir_w);  // {p, rho, 1/rho, m/rho}
     wvol[w] = V;
 }
 
@@ -232,13 +234,16 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
                                            const double4_32a* __restrict__ pos,
                                            const unsigned* __restrict__ list,
                                            int cnt, int skip, int* __restrict__ out) {
-    // skip: 0 keep all (walls), 1 drop self (fluid, gather mode), 2 keep b > s only (fluid,
-    // symmetric mode: every pair once, at its lower slot)
+    // skip: 0 keep all (walls), 1 drop self (fluid, gather mode), 2 keep the pairs that s owns
+    // (fluid, symmetric mode: the owner of {s, b} is the lower slot when s + b is odd and the
+    // higher one when it is even, which gives every particle about half of its neighbours
+    // wherever it sits in its cell)
     int n = 0;
     for (int k = 0; k < cnt; ++k) {
         const unsigned e = list[(size_t)k * n_rows + s];
         const int b = (int)(e & kSlotMask);
-        if ((skip == 1 && b == s) || (skip == 2 && b <= s)) continue;
+        if (b == s && skip != 0) continue;
+        if (skip == 2 && ((b > s) != (((s ^ b) & 1) != 0))) continue;
         float p0, p1, p2;
         const float d2f = pair_diff<ND>(ta, cs, e, test[b], p0, p1, p2);
         bool acc = d2f <= lo2;
@@ -267,17 +272,33 @@ __global__ void __launch_bounds__(256) k_filter64(
     efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, wtest, wpos, fw, fwc[s], 0, efw);
 }
 
-// Pair terms in the reference's order (rhs.jl:81-117), FP64 throughout, with the arithmetic
-// arranged for the slow FP64 pipe: one reciprocal square root per pair gives both
-// r = d^2 * rsqrt(d^2) and the 1/r^2 of the density diffusion; 1 / (rho_a rho_b) is the
-// product of the per-particle fast_inv(rho) values of the pack; the zero-distance skip
-// `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28) is tested as d^2 < eps((2h)^2).  Each of these
-// differs from the reference's expression by a few ulp at most.
+// Pair terms of rhs.jl:81-117 (pressure, Monaghan viscosity, continuity, Molteni-Colagrossi
+// diffusion), FP64 throughout, written for the slow FP64 pipe with the identities that follow
+// from grad W_ab = sg * x_ab (sg = sg_c (1 - q/2)^3, kernel_deriv_div_r_unsafe):
+//   pressure + viscosity: dv_a += (c_p + c_v) sg x_ab, one scalar for both terms;
+//   continuity: v_ab . grad W = sg (v_ab . x_ab), the dot product the viscosity switch needs;
+//   diffusion: psi_ab . grad W = 2 (rho_a - rho_b) / r^2 (x_ab . sg x_ab) = 2 (rho_a - rho_b) sg;
+//   Monaghan: mu / rho_mean from one reciprocal of (r^2 + eps h^2) rho_mean;
+//   1 / (rho_a rho_b) and m_b / rho_b from the per-particle fast_inv(rho) of the pack;
+//   r = d^2 rsqrt(d^2); the zero-distance skip `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28)
+//   tested as d^2 < eps((2h)^2).
+// Each term equals the reference's expression up to a few ulp of rounding.
+__device__ __forceinline__ double monaghan_coef(const Phys& P, double m_b, double vr, double d2,
+                                                double rho_a, double rho_b) {
+    // m_b (alpha c mu + beta mu^2) / rho_mean, mu = h vr / (r^2 + eps h^2)   (vr < 0)
+    const double den = d2 + P.visc_eps_h2;
+    const double rm = 0.5 * (rho_a + rho_b);
+    const double R = fast_inv(den * rm);
+    if (P.beta == 0.0) return (m_b * P.visc_k) * vr * R;
+    const double mu = (P.visc_h * vr) * (rm * R);
+    return (m_b * mu) * (P.alpha_c + P.beta * mu) * (den * R);
+}
+
 template <int ND, bool INTEGRATE>
 __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
                                                 const double4_32a* __restrict__ fpos,
                                                 const double4_32a* __restrict__ fvel,
-                                                const double2* __restrict__ faux,
+                                                const double4_32a* __restrict__ faux,
                                                 const int* __restrict__ eff,
                                                 const int* __restrict__ effc,
                                                 const int* __restrict__ efw,
@@ -290,7 +311,7 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
-    const double p_a = pa.w, rho_a = va.w, ia = faux[s].y;
+    const double p_a = pa.w, rho_a = va.w, ia = faux[s].z;
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
@@ -300,51 +321,29 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         const double4_32a pb = fpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
-        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        double d2 = pd0 * pd0 + pd1 * pd1;
+        if (ND == 3) d2 += pd2 * pd2;
         if (d2 < P.az2) continue;
-        const double ir = rsqrt(d2);
-        const double r = d2 * ir;
+        const double r = d2 * rsqrt(d2);
+        const double t = fma(-r, P.half_hinv, 1.0);
+        const double sg = P.sg_c * ((t * t) * t);
         const double4_32a vb = fvel[b];
-        const double2 ab = faux[b];  // {m_b, fast_inv(rho_b)}
-        const double m_b = ab.x, rho_b = vb.w, ib = ab.y;
-        // WendlandC2 kernel_deriv_div_r_unsafe * pos_diff
-        const double q = r * P.h_inv;
-        const double t = 1.0 - 0.5 * q;
-        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        // pressure_acceleration_continuity_density
-        const double coef = (-m_b) * ((p_a + pb.w) * (ia * ib));
-        dv0 += coef * g0;
-        dv1 += coef * g1;
-        if (ND == 3) dv2 += coef * g2;
+        const double4_32a ab = faux[b];  // {m_b, m_b / rho_b, 1 / rho_b, 0}
         const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
         const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
-        if (P.visc) {
-            double vr = vd0 * pd0 + vd1 * pd1;
-            if (ND == 3) vr += vd2 * pd2;
-            if (vr < 0.0) {
-                const double rho_mean = (rho_a + rho_b) / 2.0;
-                const double mu = div_fast(P.visc_h * vr, d2 + P.visc_eps_h2);
-                const double num = ((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu);
-                const double f = div_fast(num, rho_mean);
-                dv0 += f * g0;
-                dv1 += f * g1;
-                if (ND == 3) dv2 += f * g2;
-            }
-        }
-        double vg = vd0 * g0 + vd1 * g1;
-        if (ND == 3) vg += vd2 * g2;
-        drho += ((rho_a * ib) * m_b) * vg;
-        if (P.diff) {
-            const double vol_b = m_b * ib;
-            const double pc = (2.0 * (rho_a - rho_b)) * (ir * ir);
-            double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
-            if (ND == 3) pg += (pc * pd2) * g2;
-            drho += P.diff_coef * (vol_b * pg);
-        }
+        double vr = vd0 * pd0 + vd1 * pd1;
+        if (ND == 3) vr += vd2 * pd2;
+        double c = -(ab.y * ia) * (p_a + pb.w);
+        if (P.visc && vr < 0.0) c += monaghan_coef(P, ab.x, vr, d2, rho_a, vb.w);
+        c *= sg;
+        dv0 += c * pd0;
+        dv1 += c * pd1;
+        if (ND == 3) dv2 += c * pd2;
+        drho += (rho_a * ab.y) * (sg * vr);
+        if (P.diff) drho += (ab.y * (rho_a - vb.w)) * (sg * P.diff2);
     }
 
-    // ---- fluid-wall (wall viscosity = nothing, no density diffusion) ----
+    // ---- fluid-wall (wall viscosity = nothing, no density diffusion, wall velocity 0) ----
     double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
     const int nfw = efwc[s];
     for (int k = 0; k < nfw; ++k) {
@@ -352,22 +351,20 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         const double4_32a pb = wpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
-        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        double d2 = pd0 * pd0 + pd1 * pd1;
+        if (ND == 3) d2 += pd2 * pd2;
         if (d2 < P.az2) continue;
         const double r = d2 * rsqrt(d2);
-        const double4_32a sb = wstate[b];  // {p, rho, fast_inv(rho), 0}
-        const double m_b = pb.w, p_b = sb.x, ib = sb.z;
-        const double q = r * P.h_inv;
-        const double t = 1.0 - 0.5 * q;
-        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        const double coef = (-m_b) * ((p_a + p_b) * (ia * ib));
-        ew0 += coef * g0;
-        ew1 += coef * g1;
-        if (ND == 3) ew2 += coef * g2;
-        double vg = va.x * g0 + va.y * g1;
-        if (ND == 3) vg += va.z * g2;
-        erho += ((rho_a * ib) * m_b) * vg;
+        const double t = fma(-r, P.half_hinv, 1.0);
+        const double sg = P.sg_c * ((t * t) * t);
+        const double4_32a sb = wstate[b];  // {p, rho, 1/rho, m/rho}
+        const double c = (-(sb.w * ia) * (p_a + sb.x)) * sg;
+        ew0 += c * pd0;
+        ew1 += c * pd1;
+        if (ND == 3) ew2 += c * pd2;
+        double vx = va.x * pd0 + va.y * pd1;
+        if (ND == 3) vx += va.z * pd2;
+        erho += (rho_a * sb.w) * (sg * vx);
     }
 
     // dv = ((0 + S_ff) + S_fw) + g ;  drho = S_ff + S_fw
@@ -379,17 +376,19 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     stage_update<ND, INTEGRATE>(s, pa, va, k, U);
 }
 
-// Symmetric pair pass: every fluid-fluid pair once, at its lower slot a (the exact half list
-// holds b > a).  The terms of b are the ones b would evaluate itself -- with x_ba = -x_ab,
-// v_ba = -v_ab and grad W_ba = -grad W_ab the shared factors (kernel gradient, pressure sum over
-// rho_a rho_b, mu and 1/rho_mean, v_ab . grad W, the diffusion projection) are evaluated once --
-// and reach b through FP64 atomic adds into its accumulator {dv, drho}; a adds its own sum once
-// at the end.  Fluid-wall pairs stay one-sided.  k_update64 then applies gravity and the stage.
+// Symmetric pair pass: every fluid-fluid pair once, at its owner a (the exact half list holds
+// the pairs a owns).  b receives the terms it would evaluate itself -- with x_ba = -x_ab,
+// v_ba = -v_ab, grad W_ba = -grad W_ab the shared factors (sg, p_a + p_b, the Monaghan
+// reciprocal, v_ab . x_ab, rho_a - rho_b) are evaluated once -- through FP64 atomic adds into
+// its accumulator {dv, drho}; a adds its own sum once at the end.  Lanes of a warp start their
+// walk at different points of their lists, so that the atomic adds of neighbouring lanes (whose
+// candidate sequences are nearly the same) do not hit the same particle at the same time.
+// Fluid-wall pairs stay one-sided.  k_update64 then applies gravity and the stage.
 template <int ND>
 __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
                                                  const double4_32a* __restrict__ fpos,
                                                  const double4_32a* __restrict__ fvel,
-                                                 const double2* __restrict__ faux,
+                                                 const double4_32a* __restrict__ faux,
                                                  const int* __restrict__ eff,
                                                  const int* __restrict__ effc,
                                                  const int* __restrict__ efw,
@@ -403,93 +402,90 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
-    const double2 aa = faux[s];
-    const double p_a = pa.w, rho_a = va.w, m_a = aa.x, ia = aa.y;
+    const double4_32a aa = faux[s];
+    const double p_a = pa.w, rho_a = va.w, m_a = aa.x, vol_a = aa.y, ia = aa.z;
 
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
     const int nff = effc[s];
-    for (int k = 0; k < nff; ++k) {
+    int k = (int)(((unsigned)(threadIdx.x & 31) * (unsigned)nff) >> 5);
+    for (int it = 0; it < nff; ++it, ++k) {
+        if (k == nff) k = 0;
         const int b = eff[(size_t)k * nf + s];
         const double4_32a pb = fpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
-        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        double d2 = pd0 * pd0 + pd1 * pd1;
+        if (ND == 3) d2 += pd2 * pd2;
         if (d2 < P.az2) continue;
-        const double ir = rsqrt(d2);
-        const double r = d2 * ir;
+        const double r = d2 * rsqrt(d2);
+        const double t = fma(-r, P.half_hinv, 1.0);
+        const double sg = P.sg_c * ((t * t) * t);
         const double4_32a vb = fvel[b];
-        const double2 ab = faux[b];
-        const double m_b = ab.x, rho_b = vb.w, ib = ab.y;
-        const double q = r * P.h_inv;
-        const double t = 1.0 - 0.5 * q;
-        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        // pressure: a gets -m_b X grad W_ab, b gets -m_a X grad W_ba = m_a X grad W_ab
-        const double X = (p_a + pb.w) * (ia * ib);
-        const double ca = (-m_b) * X, cb = m_a * X;
-        dv0 += ca * g0;
-        dv1 += ca * g1;
-        if (ND == 3) dv2 += ca * g2;
-        double b0 = cb * g0, b1 = cb * g1, b2 = cb * g2;
+        const double4_32a ab = faux[b];
+        const double rho_b = vb.w;
         const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
         const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
-        if (P.visc) {
-            double vr = vd0 * pd0 + vd1 * pd1;
-            if (ND == 3) vr += vd2 * pd2;
-            if (vr < 0.0) {
-                const double rho_mean = (rho_a + rho_b) / 2.0;
-                const double mu = div_fast(P.visc_h * vr, d2 + P.visc_eps_h2);
-                const double R = fast_inv(rho_mean);
-                const double fa = (((m_b * P.alpha) * P.c) * mu + (m_b * P.beta) * (mu * mu)) * R;
-                const double fb = (((m_a * P.alpha) * P.c) * mu + (m_a * P.beta) * (mu * mu)) * R;
-                dv0 += fa * g0;
-                dv1 += fa * g1;
-                if (ND == 3) dv2 += fa * g2;
-                b0 -= fb * g0;
-                b1 -= fb * g1;
-                b2 -= fb * g2;
+        double vr = vd0 * pd0 + vd1 * pd1;
+        if (ND == 3) vr += vd2 * pd2;
+        const double Pab = p_a + pb.w;
+        // a: -m_b (p_a+p_b)/(rho_a rho_b) grad W_ab ; b: -m_a (p_a+p_b)/(rho_a rho_b) grad W_ba
+        double ca = -(ab.y * ia) * Pab;
+        double cb = (vol_a * ab.z) * Pab;
+        if (P.visc && vr < 0.0) {
+            const double den = d2 + P.visc_eps_h2;
+            const double rm = 0.5 * (rho_a + rho_b);
+            const double R = fast_inv(den * rm);
+            if (P.beta == 0.0) {
+                const double w = vr * R;
+                ca += (ab.x * P.visc_k) * w;
+                cb -= (m_a * P.visc_k) * w;
+            } else {
+                const double mu = (P.visc_h * vr) * (rm * R);
+                const double w = mu * (P.alpha_c + P.beta * mu) * (den * R);
+                ca += ab.x * w;
+                cb -= m_a * w;
             }
         }
-        double vg = vd0 * g0 + vd1 * g1;
-        if (ND == 3) vg += vd2 * g2;
-        drho += ((rho_a * ib) * m_b) * vg;
-        double br = ((rho_b * ia) * m_a) * vg;
+        ca *= sg;
+        cb *= sg;
+        dv0 += ca * pd0;
+        dv1 += ca * pd1;
+        if (ND == 3) dv2 += ca * pd2;
+        const double svr = sg * vr;
+        drho += (rho_a * ab.y) * svr;
+        double br = (rho_b * vol_a) * svr;
         if (P.diff) {
-            const double pc = (2.0 * (rho_a - rho_b)) * (ir * ir);
-            double pg = (pc * pd0) * g0 + (pc * pd1) * g1;
-            if (ND == 3) pg += (pc * pd2) * g2;
-            drho += P.diff_coef * ((m_b * ib) * pg);
-            br += P.diff_coef * ((m_a * ia) * (-pg));
+            const double dd = (rho_a - rho_b) * (sg * P.diff2);
+            drho += ab.y * dd;
+            br -= vol_a * dd;
         }
         double* ab4 = acc + (size_t)b * 4;
-        atomicAdd(ab4 + 0, b0);
-        atomicAdd(ab4 + 1, b1);
-        if (ND == 3) atomicAdd(ab4 + 2, b2);
+        atomicAdd(ab4 + 0, cb * pd0);
+        atomicAdd(ab4 + 1, cb * pd1);
+        if (ND == 3) atomicAdd(ab4 + 2, cb * pd2);
         atomicAdd(ab4 + 3, br);
     }
 
     const int nfw = efwc[s];
-    for (int k = 0; k < nfw; ++k) {
-        const int b = efw[(size_t)k * nf + s];
+    for (int kw = 0; kw < nfw; ++kw) {
+        const int b = efw[(size_t)kw * nf + s];
         const double4_32a pb = wpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
-        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        double d2 = pd0 * pd0 + pd1 * pd1;
+        if (ND == 3) d2 += pd2 * pd2;
         if (d2 < P.az2) continue;
         const double r = d2 * rsqrt(d2);
+        const double t = fma(-r, P.half_hinv, 1.0);
+        const double sg = P.sg_c * ((t * t) * t);
         const double4_32a sb = wstate[b];
-        const double m_b = pb.w, p_b = sb.x, ib = sb.z;
-        const double q = r * P.h_inv;
-        const double t = 1.0 - 0.5 * q;
-        const double sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-        const double g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        const double coef = (-m_b) * ((p_a + p_b) * (ia * ib));
-        dv0 += coef * g0;
-        dv1 += coef * g1;
-        if (ND == 3) dv2 += coef * g2;
-        double vg = va.x * g0 + va.y * g1;
-        if (ND == 3) vg += va.z * g2;
-        drho += ((rho_a * ib) * m_b) * vg;
+        const double c = (-(sb.w * ia) * (p_a + sb.x)) * sg;
+        dv0 += c * pd0;
+        dv1 += c * pd1;
+        if (ND == 3) dv2 += c * pd2;
+        double vx = va.x * pd0 + va.y * pd1;
+        if (ND == 3) vx += va.z * pd2;
+        drho += (rho_a * sb.w) * (sg * vx);
     }
     double* a4 = acc + (size_t)s * 4;
     atomicAdd(a4 + 0, dv0);
@@ -570,7 +566,7 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
     pk.test = h->f_test;
     pk.pos = (double4_32a*)h->f_pos;
     pk.vel = (double4_32a*)h->f_vel;
-    pk.aux = (double2*)h->f_aux;
+    pk.aux = (double4_32a*)h->f_aux;
     pk.g = h->grid;
     pk.cs32 = (double)(float)h->grid.cs;
     pk.P = h->phys;
@@ -645,7 +641,7 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     if (sym) {
         k_pair64s<ND><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
-            (const double2*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
+            (const double4_32a*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
             (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, h->acc, gate);
         k_update64<ND, INTEG><<<nblk(nf, 256), 256, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->acc, U);
@@ -653,7 +649,7 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     } else {
         k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
-            (const double2*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
+            (const double4_32a*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
             (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);
         h->launches += 1;  // the filter
     }

@@ -59,6 +59,12 @@ struct Phys {
     double diff_coef;  // (delta * ((h + h) / 2)) * c
     double g[3];
     double p_off;
+    // derived constants of the FP64 pair kernels
+    double sg_c;       // wc2_dnorm * hi2: grad W = sg_c (1 - q/2)^3 x_ab
+    double half_hinv;  // 0.5 * h_inv: 1 - q/2 = 1 - r * half_hinv
+    double visc_k;     // alpha * c * visc_h (Monaghan with beta = 0)
+    double alpha_c;    // alpha * c
+    double diff2;      // 2 * diff_coef
 };
 
 // FP32 copies of the constants used by the precision form.
