@@ -435,6 +435,8 @@ def run_profile_form(args):
     pkg.load_library()
     semi, tank = make_case(pkg, cfg, prec, 0)
     ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    if args.pair_mode is not None:
+        semi._call("tp_set_pair_mode", args.pair_mode)
     v, u, ms, launches, ph = run_form(pkg, torch, semi, ode, args.steps, args.warmup, cfg["dt"],
                                       prec)
     n = semi.n_fluid + semi.n_wall
@@ -461,6 +463,8 @@ def main():
     ap.add_argument("--profile-form", default=None, metavar="PRECISION:WORKLOAD",
                     help="profiling mode (e.g. float32:cfg2): only warm-up + timed steps of that "
                          "form, one summary line; used under ncu")
+    ap.add_argument("--pair-mode", type=int, default=None, choices=[0, 1],
+                    help="FP64 pair pass of --profile-form: 0 gather, 1 symmetric")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

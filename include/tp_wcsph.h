@@ -222,12 +222,14 @@ tp_status tp_set_skin(tp_handle* h, double skin);
 tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth);
 
 /*
- * FP64 pair-pass mode.  TP_PAIR_GATHER: every fluid particle sums its own pair terms in the
- * reference's neighbour order (bitwise reproducible run to run).  TP_PAIR_SYMMETRIC (default for
- * the FP64 form): every fluid-fluid pair is evaluated once and its two halves go to both
- * particles (the second by an FP64 atomic add), which halves the FP64 work of the pair pass; the
- * terms are the same, their summation order is not, so results differ from the gather mode in
- * the last bits and are not bitwise reproducible.  The FP32 form always gathers.
+ * FP64 pair-pass mode.  TP_PAIR_GATHER (default): every fluid particle sums its own pair terms
+ * in the reference's neighbour order (bitwise reproducible run to run).  TP_PAIR_SYMMETRIC:
+ * every fluid-fluid pair is evaluated once and its two halves go to both particles (the second
+ * by an FP64 atomic add), which cuts the FP64 arithmetic per pair by about 40 %; the terms are
+ * the same, their summation order is not, so results differ from the gather mode in the last
+ * bits and are not bitwise reproducible.  On GB300 the symmetric pass is not faster (lane
+ * imbalance of the half lists and atomic traffic eat the saving); it is kept for GPUs with a
+ * different FP64 / atomic balance.  The FP32 form always gathers.
  */
 enum { TP_PAIR_GATHER = 0, TP_PAIR_SYMMETRIC = 1 };
 tp_status tp_set_pair_mode(tp_handle* h, int32_t mode);

@@ -91,7 +91,7 @@ struct tp_handle {
     int ecap_ff = 0, ecap_fw = 0;
     // FP64 form, symmetric pair mode: per-slot accumulator {dv (3), drho} of the pair pass
     double* acc = nullptr;
-    int pair_mode = 1;  // TP_PAIR_SYMMETRIC (FP64 default) or TP_PAIR_GATHER
+    int pair_mode = 0;  // TP_PAIR_GATHER (default) or TP_PAIR_SYMMETRIC
     double skin = 0.1;          // list radius 2h (1 + skin); rebuild after skin * h displacement
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
     unsigned* gate = nullptr;   // {force, max displacement bits, half-skin bits}
