@@ -153,7 +153,7 @@ __global__ void k_scatter_pressure(const void* __restrict__ rec, const int* __re
                                    double* __restrict__ p, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    p[perm[s]] = F32 ? (double)((const float2*)rec)[s].x : ((const double4_32a*)rec)[s].w;
+    p[perm[s]] = F32 ? (double)((const float4*)rec)[s].x : ((const double4_32a*)rec)[s].w;
 }
 
 template <bool F32>
@@ -322,6 +322,11 @@ void setup_phys(tp_handle* h) {
     Q.diff_coef = (float)P.diff_coef;
     for (int d = 0; d < 3; ++d) Q.g[d] = (float)P.g[d];
     Q.p_off = (float)P.p_off;
+    Q.sg_c = Q.wc2_dnorm * Q.hi2;
+    Q.half_hinv = 0.5f * Q.h_inv;
+    Q.visc_k = Q.visc_ac * Q.visc_h;
+    Q.diff2 = 2.0f * Q.diff_coef;
+    Q.az2 = std::nextafter(Q.sr2, INFINITY) - Q.sr2;
 }
 
 bool setup_grid(tp_handle* h, std::string& msg) {

@@ -58,7 +58,7 @@ struct Pack32 {
     double* xb_out;
     float4* test;
     float4* vel;
-    float2* aux;
+    float4* aux;  // {p, m, m / rho, 1 / rho}
     GridDesc g;
     double cs32, rho0;
     Phys32 P;
@@ -82,7 +82,8 @@ struct Pack32 {
         // offsets against the reference cell `key` (the cell of the last rebuild)
         test[s] = test_record_in<ND>(x, g, cs32, key);
         vel[s] = w;
-        aux[s] = make_float2(eos32(w.w, P, P.fluid_clip), mi);
+        const float irho = __frcp_rn(P.rho0 + w.w);
+        aux[s] = make_float4(eos32(w.w, P, P.fluid_clip), mi, mi * irho, irho);
         if (rebuild && xb_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
@@ -100,7 +101,7 @@ struct Pack32 {
     }
 };
 
-// FP32 wall state: {p, rho - rho0, m, 0}; masses are set once, p and rho by the Adami pass.
+// FP32 wall state: {p, rho - rho0, m, m / rho}; masses are set once, the rest by the Adami pass.
 __global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4* __restrict__ st,
                                     int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4*
                                                  double* __restrict__ wvol,
                                                  const float4* __restrict__ ftest,
                                                  const float4* __restrict__ fvel,
-                                                 const float2* __restrict__ faux) {
+                                                 const float4* __restrict__ faux) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const float4 tw = wtest[w];
@@ -147,7 +148,8 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4*
     if ((double)vw > 2.220446049250313e-16) pw = pw / vw;
     if (P.wall_clip) pw = (pw != pw || pw > 0.0f) ? pw : 0.0f;
     const float m = wstate[w].z;
-    wstate[w] = make_float4(pw, eos32_inverse_dev(pw, P), m, 0.0f);
+    const float dr = eos32_inverse_dev(pw, P);
+    wstate[w] = make_float4(pw, dr, m, m * __frcp_rn(P.rho0 + dr));  // {p, rho - rho0, m, m/rho}
     wvol[w] = (double)vw;
 }
 
@@ -165,10 +167,14 @@ struct Update32 {
     int first;
 };
 
+// Pair terms with the same identities as the FP64 kernels (grad W_ab = sg x_ab: one scalar for
+// pressure + viscosity, continuity through sg (v_ab . x_ab), diffusion as 2 (rho_a - rho_b) sg,
+// one reciprocal for the Monaghan mu / rho_mean), in FP32 on the cell-relative differences, with
+// Kahan-compensated per-particle sums.
 template <int ND, bool INTEGRATE>
 __global__ void __launch_bounds__(256) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
-                                                const float2* __restrict__ faux,
+                                                const float4* __restrict__ faux,
                                                 const unsigned* __restrict__ ff,
                                                 const int* __restrict__ ffc,
                                                 const unsigned* __restrict__ fw,
@@ -181,7 +187,8 @@ __global__ void __launch_bounds__(256) k_pair32(Phys32 P, int nf, const float4* 
     if (s >= nf) return;
     const float4 ta = ftest[s];
     const float4 va = fvel[s];
-    const float p_a = faux[s].x;
+    const float4 aa = faux[s];  // {p, m, m/rho, 1/rho}
+    const float p_a = aa.x, ia = aa.w;
     const float drho_a = va.w;
     const float rho_a = P.rho0 + drho_a;
 
@@ -192,47 +199,34 @@ __global__ void __launch_bounds__(256) k_pair32(Phys32 P, int nf, const float4* 
         const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
         const float d2 = pair_diff<ND>(ta, P.cs, e, ftest[b], pd0, pd1, pd2);
-        if (d2 > P.sr2) continue;
-        const float r = sqrtf(d2);
-        if (r < P.almostzero) continue;
+        if (d2 > P.sr2 || d2 < P.az2) continue;
+        const float r = d2 * rsqrtf(d2);
         const float4 vb = fvel[b];
-        const float2 ab = faux[b];  // {p_b, m_b}
-        const float m_b = ab.y;
-        const float rho_b = P.rho0 + vb.w;
-        const float q = r * P.h_inv;
-        const float t = 1.0f - 0.5f * q;
-        const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-        const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        const float coef = -m_b * __fdividef(p_a + ab.x, rho_a * rho_b);
-        float e0 = coef * g0, e1 = coef * g1, e2 = coef * g2;
+        const float4 ab = faux[b];  // {p_b, m_b, m_b / rho_b, 1 / rho_b}
+        const float t = fmaf(-r, P.half_hinv, 1.0f);
+        const float sg = P.sg_c * ((t * t) * t);
         const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
         const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
-        if (P.visc) {
-            float vr = vd0 * pd0 + vd1 * pd1;
-            if (ND == 3) vr += vd2 * pd2;
-            if (vr < 0.0f) {
-                const float rho_mean = 0.5f * (rho_a + rho_b);
-                const float mu = __fdividef(P.visc_h * vr, r * r + P.visc_eps_h2);
-                const float num = (m_b * P.visc_ac) * mu + (m_b * P.beta) * (mu * mu);
-                const float f = __fdividef(num, rho_mean);
-                e0 += f * g0;
-                e1 += f * g1;
-                e2 += f * g2;
+        float vr = vd0 * pd0 + vd1 * pd1;
+        if (ND == 3) vr += vd2 * pd2;
+        float c = -(ab.z * ia) * (p_a + ab.x);
+        if (P.visc && vr < 0.0f) {
+            const float den = d2 + P.visc_eps_h2;
+            const float rm = 0.5f * (rho_a + P.rho0 + vb.w);
+            const float R = __fdividef(1.0f, den * rm);
+            if (P.beta == 0.0f) {
+                c += (ab.y * P.visc_k) * vr * R;
+            } else {
+                const float mu = (P.visc_h * vr) * (rm * R);
+                c += (ab.y * mu) * (P.visc_ac + P.beta * mu) * (den * R);
             }
         }
-        a0.add(e0);
-        a1.add(e1);
-        if (ND == 3) a2.add(e2);
-        float vg = vd0 * g0 + vd1 * g1;
-        if (ND == 3) vg += vd2 * g2;
-        float er = (__fdividef(rho_a, rho_b) * m_b) * vg;
-        if (P.diff) {
-            const float vol_b = __fdividef(m_b, rho_b);
-            const float pc = __fdividef(2.0f * (drho_a - vb.w), r * r);
-            float pg = pd0 * g0 + pd1 * g1;
-            if (ND == 3) pg += pd2 * g2;
-            er += P.diff_coef * (vol_b * (pc * pg));
-        }
+        c *= sg;
+        a0.add(c * pd0);
+        a1.add(c * pd1);
+        if (ND == 3) a2.add(c * pd2);
+        float er = (rho_a * ab.z) * (sg * vr);
+        if (P.diff) er += (ab.z * (drho_a - vb.w)) * (sg * P.diff2);
         ar.add(er);
     }
 
@@ -243,22 +237,19 @@ __global__ void __launch_bounds__(256) k_pair32(Phys32 P, int nf, const float4* 
         const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
         const float d2 = pair_diff<ND>(ta, P.cs, e, wtest[b], pd0, pd1, pd2);
-        if (d2 > P.sr2) continue;
-        const float r = sqrtf(d2);
-        if (r < P.almostzero) continue;
-        const float4 sb = wstate[b];  // {p, rho - rho0, m, 0}
-        const float m_b = sb.z, p_b = sb.x, rho_b = P.rho0 + sb.y;
-        const float q = r * P.h_inv;
-        const float t = 1.0f - 0.5f * q;
-        const float sg = (P.wc2_dnorm * ((t * t) * t)) * P.hi2;
-        const float g0 = sg * pd0, g1 = sg * pd1, g2 = sg * pd2;
-        const float coef = -m_b * __fdividef(p_a + p_b, rho_a * rho_b);
-        w0.add(coef * g0);
-        w1.add(coef * g1);
-        if (ND == 3) w2.add(coef * g2);
-        float vg = va.x * g0 + va.y * g1;
-        if (ND == 3) vg += va.z * g2;
-        wr.add((__fdividef(rho_a, rho_b) * m_b) * vg);
+        if (d2 > P.sr2 || d2 < P.az2) continue;
+        const float r = d2 * rsqrtf(d2);
+        const float4 sb = wstate[b];  // {p, rho - rho0, m, m / rho}
+        const float vol_b = sb.w;
+        const float t = fmaf(-r, P.half_hinv, 1.0f);
+        const float sg = P.sg_c * ((t * t) * t);
+        const float c = (-(vol_b * ia) * (p_a + sb.x)) * sg;
+        w0.add(c * pd0);
+        w1.add(c * pd1);
+        if (ND == 3) w2.add(c * pd2);
+        float vx = va.x * pd0 + va.y * pd1;
+        if (ND == 3) vx += va.z * pd2;
+        wr.add((rho_a * vol_b) * (sg * vx));
     }
 
     double k[4];
@@ -330,7 +321,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         pk.xb_out = h->x_build;
         pk.test = h->f_test;
         pk.vel = (float4*)h->f_vel;
-        pk.aux = (float2*)h->f_aux;
+        pk.aux = (float4*)h->f_aux;
         pk.g = h->grid;
         pk.cs32 = cs32;
         pk.rho0 = h->cfg.reference_density;
@@ -363,18 +354,18 @@ void fp32_adami(tp_handle* h) {
     if (h->cfg.ndims == 2)
         k_adami32<2><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
-            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux);
+            h->f_test, (const float4*)h->f_vel, (const float4*)h->f_aux);
     else
         k_adami32<3><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
-            h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux);
+            h->f_test, (const float4*)h->f_vel, (const float4*)h->f_aux);
 }
 
 template <int ND, bool INTEG>
 static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
     const int nf = (int)h->cfg.n_fluid;
     k_pair32<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
-        h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float2*)h->f_aux, h->l_ff,
+        h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float4*)h->f_aux, h->l_ff,
         h->c_ff, h->l_fw, h->c_fw, h->w_test, (const float4*)h->w_state, gate, U);
 }
 

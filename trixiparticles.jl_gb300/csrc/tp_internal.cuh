@@ -76,6 +76,8 @@ struct Phys32 {
     float beta, visc_h, visc_eps_h2, visc_ac, diff_coef;
     float g[3];
     float p_off;
+    // derived constants of the FP32 pair kernel (see the FP64 ones)
+    float sg_c, half_hinv, visc_k, diff2, az2;
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
