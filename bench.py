@@ -380,6 +380,60 @@ def run_adjoint(pkg, torch, dx=0.01, n_steps=500, every=25, fd_h=1e-4, seed=7):
             "backward_over_fused_step": bwd_step / integ_ms}
 
 
+def run_precision_study(pkg, torch, checkpoints=(100, 500, 1000), jitters=(0.0, 0.05),
+                        seed=2024):
+    """Precision form against the FP64 drop-in on the dx = 0.0064 geometry: relative L2 errors of
+    rho, v and x after 100 / 500 / 1000 CK2N54 steps, on the lattice start and on a jittered
+    start (fluid positions perturbed by uniform +-0.05 dx noise from a seeded generator, the
+    same perturbed input for both forms).  The FP64 drop-in stands in for the FP64 oracle at
+    this size (it matches the oracle to 1e-9 relative in the parity tests)."""
+    cfg = CFG2
+    out = {"workload": cfg["name"], "checkpoints": list(checkpoints), "cases": []}
+    for jit in jitters:
+        tank, eos = pkg.dam_break(3, cfg["dx"], cfg["fluid"], cfg["tank"], n_layers=3)
+        if jit:
+            rng = np.random.default_rng(seed)
+            tank.fluid.coordinates += rng.uniform(-jit * cfg["dx"], jit * cfg["dx"],
+                                                  tank.fluid.coordinates.shape)
+        states = {}
+        semis = {}
+        for prec in ("float64", "float32"):
+            semi = pkg.dam_break_semidiscretization(tank, eos, 1.75 * cfg["dx"], precision=prec)
+            ode = pkg.semidiscretize(semi, (0.0, 1.0))
+            semis[prec] = semi
+            states[prec] = (ode.v0.clone(), ode.u0.clone())
+        rows = []
+        done = 0
+        t_form = {"float64": 0.0, "float32": 0.0}
+        for cp in checkpoints:
+            for prec, semi in semis.items():
+                v, u = states[prec]
+                semi._set_stream()
+                t0 = time.perf_counter()
+                semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                           ctypes.c_double(cfg["dt"]), ctypes.c_int64(cp - done))
+                semi.sync()
+                t_form[prec] += time.perf_counter() - t0
+            v64 = states["float64"][0].view(-1, 4).cpu().numpy()
+            v32 = states["float32"][0].view(-1, 4).cpu().numpy()
+            u64 = states["float64"][1].view(-1, 3).cpu().numpy()
+            u32 = states["float32"][1].view(-1, 3).cpu().numpy()
+
+            def rl2(a, b):
+                return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+            rows.append({"step": cp, "rel_l2_rho": rl2(v32[:, 3], v64[:, 3]),
+                         "rel_l2_v": rl2(v32[:, :3], v64[:, :3]), "rel_l2_x": rl2(u32, u64)})
+            done = cp
+        for semi in semis.values():
+            semi.close()
+        out["cases"].append({"jitter_dx": jit, "seed": seed if jit else None,
+                             "n_fluid": tank.fluid.n_particles,
+                             "n_wall": tank.boundary.n_particles, "errors": rows,
+                             "seconds": {k: round(v, 2) for k, v in t_form.items()}})
+    return out
+
+
 def run_reference(args):
     """--impl reference: the oracle (C++ FP64 restatement of the reference) on host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -465,9 +519,21 @@ def main():
                          "form, one summary line; used under ncu")
     ap.add_argument("--pair-mode", type=int, default=None, choices=[0, 1],
                     help="FP64 pair pass of --profile-form: 0 gather, 1 symmetric")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="FP32 form vs FP64 drop-in errors after 100/500/1000 steps (dx=0.0064, "
+                         "lattice and jittered starts); prints one JSON line")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.precision_study:
+        import torch
+
+        import __graft_entry__ as g
+
+        pkg = g.load_package()
+        pkg.load_library()
+        print(json.dumps(run_precision_study(pkg, torch)), flush=True)
+        return 0
     if args.profile_form:
         return run_profile_form(args)
 
