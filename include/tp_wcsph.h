@@ -234,6 +234,27 @@ tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth);
 enum { TP_PAIR_GATHER = 0, TP_PAIR_SYMMETRIC = 1 };
 tp_status tp_set_pair_mode(tp_handle* h, int32_t mode);
 
+/*
+ * interpolate_points (src/general/interpolation.jl:480-697) at n_points points (device array,
+ * (ndims, n_points) reference layout) from the fluid state (v_ode, u_ode): the SPH interpolation
+ * with the WendlandC2 kernel of smoothing length `smoothing_length` (support 2 h), after the
+ * system update the reference performs first (fluid pressure from the current density; the
+ * Adami wall state when walls take part).  Outputs (device arrays): computed_density
+ * (sum m_b W), velocity (ndims, n_points), pressure, density (Shepard-normalised), and
+ * neighbor_count; points where computed_density < eps() -- or, with cut_off_bnd, where the wall
+ * particles add more kernel-weighted mass than the fluid -- get NaN and a zero count.
+ * clip_negative_pressure clips the interpolated pressure contributions at 0;
+ * include_wall_velocity renormalises the velocity with the wall particles' volume (fixed walls:
+ * zero velocity).  Points must lie inside the FullGridCellList box.  FP64 in both precision
+ * forms.  Asynchronous on the handle's stream.
+ */
+tp_status tp_interpolate_points(tp_handle* h, const double* v_ode, const double* u_ode,
+                                const double* points, int64_t n_points, double smoothing_length,
+                                int32_t cut_off_bnd, int32_t clip_negative_pressure,
+                                int32_t include_wall_velocity, double* computed_density,
+                                double* velocity, double* pressure, double* density,
+                                int32_t* neighbor_count);
+
 /* Copy of the configuration the handle was created with. */
 tp_status tp_get_config(const tp_handle* h, tp_config* out);
 

@@ -52,6 +52,8 @@ def lib():
         L.orc_integrate_ck2n54.restype = c_int
         L.orc_integrate_ck2n54.argtypes = [c_void_p, dp, dp, c_double, c_int64]
         L.orc_ck2n54_coefficients.argtypes = [dp, dp, dp]
+        L.orc_interpolate.argtypes = [c_void_p, dp, dp, dp, c_int64, c_double, c_int, c_int,
+                                      c_int, dp, dp, dp, dp, ip]
         L.orc_nhs.restype = c_int
         L.orc_nhs.argtypes = [c_void_p, dp, dp, ip, ip, ip, ip, ip]
         for name in ("orc_wendland_c2", "orc_wendland_c2_deriv_div_r"):
@@ -140,6 +142,24 @@ class Model:
         du = np.zeros(self.nf * self.nd)
         self.L.orc_drift(self.h, _dp(du), _dp(v))
         return du
+
+    def interpolate(self, v, u, points, smoothing_length, cut_off_bnd=True,
+                    clip_negative_pressure=False, include_wall_velocity=False):
+        """interpolate_points at `points` (n, nd): dict of computed_density, velocity (n, nd),
+        pressure, density, neighbor_count."""
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, self.nd)
+        n = pts.shape[0]
+        cd, pr, de = np.zeros(n), np.zeros(n), np.zeros(n)
+        ve = np.zeros((n, self.nd))
+        cnt = np.zeros(n, dtype=np.int32)
+        self.L.orc_interpolate(self.h, _dp(v), _dp(u), _dp(pts), n, smoothing_length,
+                               int(cut_off_bnd), int(clip_negative_pressure),
+                               int(include_wall_velocity), _dp(cd), _dp(ve), _dp(pr), _dp(de),
+                               _ip(cnt))
+        return dict(computed_density=cd, velocity=ve, pressure=pr, density=de,
+                    neighbor_count=cnt)
 
     def integrate(self, v: np.ndarray, u: np.ndarray, dt: float, n_steps: int):
         v = np.array(v, dtype=np.float64).reshape(-1)

@@ -366,6 +366,79 @@ struct Model {
         }
     }
 
+    // interpolate_points (src/general/interpolation.jl:480-697) after the system update the
+    // PostprocessCallback performs (update_systems_and_nhs, semidiscretization.jl:616-646:
+    // fluid pressure from the current density, Adami wall state).  The neighbourhood searches
+    // are copies with search radius = compact support 2 h_i (process_neighborhood_searches,
+    // :492-534), i.e. cells of size 2 h_i; neighbours are visited system by system (fluid, then
+    // wall) in that grid's order.  Outputs per point: computed_density, velocity (nd), pressure,
+    // density, neighbor_count.
+    void interpolate(const double* v, const double* u, const double* pts, int64_t np,
+                     double hi, bool cut_off_bnd, bool clip, bool wall_velocity, double* cd,
+                     double* vel, double* pres, double* dens, int32_t* count) {
+        fluid_cl.build(grid, u, nf);
+        fluid_pressure(v);
+        adami(v, u);
+        tp_config c2 = cfg;
+        c2.smoothing_length = hi;  // Grid::init takes cell size 2 * smoothing_length
+        Grid gi;
+        gi.init(c2);
+        CellList fcl, wcl;
+        fcl.build(gi, u, nf);
+        const bool walls = cut_off_bnd || wall_velocity;
+        if (walls) wcl.build(gi, xw.data(), nw);
+        const double sr = 2.0 * hi;
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int64_t i = 0; i < np; ++i) {
+            const double* x = pts + i * nd;
+            double rho_c = 0.0, other = 0.0, shep = 0.0, shep_w = 0.0;
+            double vv[3] = {0, 0, 0}, pp = 0.0, dd = 0.0;
+            int32_t cnt = 0;
+            foreach_neighbor(gi, fcl, u, x, sr, [&](int32_t b, const double*, double r) {
+                const double m_b = mf[b];
+                const double rho_b = v[b * (nd + 1) + nd];
+                const double vol = m_b / rho_b;
+                const double W = wc2_kernel(nd, r, hi);
+                if (wall_velocity) shep_w += vol * W;
+                rho_c += m_b * W;
+                shep += vol * W;
+                for (int d = 0; d < nd; ++d) vv[d] += (v[b * (nd + 1) + d] * vol) * W;
+                double p = pf[b];
+                if (clip) p = std::max(0.0, p);
+                pp += (p * vol) * W;
+                dd += (rho_b * vol) * W;
+                ++cnt;
+            });
+            if (walls)
+                foreach_neighbor(gi, wcl, xw.data(), x, sr, [&](int32_t b, const double*, double r) {
+                    const double m_b = mw[b];
+                    const double vol = m_b / rhow[b];
+                    const double W = wc2_kernel(nd, r, hi);
+                    if (wall_velocity) shep_w += vol * W;  // wall velocity 0 adds nothing else
+                    other += m_b * W;
+                    ++cnt;
+                });
+            const bool cut = rho_c < kEps || (cut_off_bnd && other > rho_c);
+            if (cut) {
+                cd[i] = NAN;
+                count[i] = 0;
+                for (int d = 0; d < nd; ++d) vel[i * nd + d] = NAN;
+                pres[i] = NAN;
+                dens[i] = NAN;
+            } else {
+                cd[i] = rho_c;
+                count[i] = cnt;
+                for (int d = 0; d < nd; ++d) vel[i * nd + d] = vv[d] / shep;
+                pres[i] = pp / shep;
+                dens[i] = dd / shep;
+                if (wall_velocity) {
+                    const double k = shep_w / shep;
+                    for (int d = 0; d < nd; ++d) vel[i * nd + d] /= k;
+                }
+            }
+        }
+    }
+
     // drift! -> set_velocity!, semidiscretization.jl:561-571 (delta_v = 0).
     void drift(double* du, const double* v) const {
         for (int64_t i = 0; i < nf; ++i)
@@ -462,6 +535,17 @@ int orc_integrate_ck2n54(orc_model* p, double* v, double* u, double dt, int64_t 
         }
     }
     return status;
+}
+
+void orc_interpolate(orc_model* p, const double* v, const double* u, const double* points,
+                     int64_t n_points, double smoothing_length, int cut_off_bnd,
+                     int clip_negative_pressure, int include_wall_velocity,
+                     double* computed_density, double* velocity, double* pressure,
+                     double* density, int32_t* neighbor_count) {
+    reinterpret_cast<Model*>(p)->interpolate(v, u, points, n_points, smoothing_length,
+                                             cut_off_bnd != 0, clip_negative_pressure != 0,
+                                             include_wall_velocity != 0, computed_density,
+                                             velocity, pressure, density, neighbor_count);
 }
 
 void orc_ck2n54_coefficients(double* A, double* B, double* C) {

@@ -68,6 +68,21 @@ static int run(int nd, int precision) {
     bad |= tp_adjoint_forward(h, v.data(), u.data(), 1e-4, 0, 5) != TP_ERR_ARGUMENT;
     bad |= tp_adjoint_forward(h, v.data(), u.data(), -1e-4, 3, 5) != TP_ERR_ARGUMENT;
     bad |= tp_adjoint_kernel_launches(h) <= 0;
+    // interpolation: with and without walls, argument checks
+    {
+        const int64_t np = 7;
+        std::vector<double> pts(np * nd, 0.5), cd(np), vel(np * nd), pr(np), de(np);
+        std::vector<int32_t> cnt(np);
+        bad |= tp_interpolate_points(h, v.data(), u.data(), pts.data(), np, 0.07, 1, 1, 1,
+                                     cd.data(), vel.data(), pr.data(), de.data(),
+                                     cnt.data()) != TP_OK;
+        bad |= tp_interpolate_points(h, v.data(), u.data(), pts.data(), np, 0.035, 0, 0, 0,
+                                     cd.data(), vel.data(), pr.data(), de.data(),
+                                     cnt.data()) != TP_OK;
+        bad |= tp_interpolate_points(h, v.data(), u.data(), pts.data(), np, -1.0, 0, 0, 0,
+                                     cd.data(), vel.data(), pr.data(), de.data(),
+                                     cnt.data()) != TP_ERR_ARGUMENT;
+    }
     // batching form: one-member batch, autotune, capture, launch, sync
     tp_batch* b = nullptr;
     tp_handle* hs[1] = {h};

@@ -15,7 +15,7 @@ CSRC = ROOT / "trixiparticles.jl_gb300" / "csrc"
 INC = ROOT / "include"
 HERE = Path(__file__).resolve().parent / "host_asan"
 SOURCES = ["tp_api.cu", "tp_fp64.cu", "tp_fp32.cu", "tp_noalloc.cu", "tp_adjoint.cu",
-           "tp_batch.cu"]
+           "tp_batch.cu", "tp_interp.cu"]
 
 
 def test_host_paths_under_asan(tmp_path):

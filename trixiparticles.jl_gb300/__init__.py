@@ -28,7 +28,8 @@ from .semidiscretization import (
     solve,
 )
 from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
-from . import adjoint, ensemble
+from . import adjoint, ensemble, interpolation
+from .interpolation import interpolate_line, interpolate_points
 
 __all__ = [
     "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
@@ -36,6 +37,7 @@ __all__ = [
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
     "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
-    "adjoint", "build", "dam_break", "ensemble", "dam_break_semidiscretization", "default_config", "drift", "kick",
+    "adjoint", "build", "dam_break", "ensemble", "interpolate_line", "interpolate_points",
+    "interpolation", "dam_break_semidiscretization", "default_config", "drift", "kick",
     "load_library", "semidiscretize", "solve",
 ]

@@ -108,6 +108,9 @@ PROTOTYPES = [
     ("tp_adjoint_kernel_launches", c_int64, [c_void_p]),
     ("tp_get_config", c_int32, [c_void_p, POINTER(TpConfig)]),
     ("tp_set_pair_mode", c_int32, [c_void_p, c_int32]),
+    ("tp_interpolate_points", c_int32,
+     [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_double, c_int32, c_int32, c_int32,
+      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("tp_batch_create", c_int32, [c_void_p, c_int32, c_void_p]),
     ("tp_batch_destroy", c_int32, [c_void_p]),
     ("tp_batch_set_state", c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_double]),

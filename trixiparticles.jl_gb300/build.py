@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libtp_wcsph.so"
 
 SOURCES = ["tp_api.cu", "tp_fp64.cu", "tp_fp32.cu", "tp_noalloc.cu", "tp_adjoint.cu",
-           "tp_batch.cu"]
+           "tp_batch.cu", "tp_interp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3",

@@ -1086,6 +1086,32 @@ tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth) {
     return TP_OK;
 }
 
+tp_status tp_interpolate_points(tp_handle* h, const double* v_ode, const double* u_ode,
+                                const double* points, int64_t n_points, double smoothing_length,
+                                int32_t cut_off_bnd, int32_t clip_negative_pressure,
+                                int32_t include_wall_velocity, double* computed_density,
+                                double* velocity, double* pressure, double* density,
+                                int32_t* neighbor_count) {
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    if (n_points < 0 || !(smoothing_length > 0.0) || !std::isfinite(smoothing_length))
+        return fail(h, TP_ERR_ARGUMENT, "tp_interpolate_points: bad point count or smoothing length");
+    if (n_points == 0) return TP_OK;
+    if (!v_ode || !u_ode || !points || !computed_density || !velocity || !pressure || !density ||
+        !neighbor_count)
+        return fail(h, TP_ERR_ARGUMENT, "tp_interpolate_points: null array");
+    const bool walls = cut_off_bnd || include_wall_velocity;
+    // update_systems_and_nhs before the interpolation: cell list of the current fluid state and,
+    // when walls take part, their Adami state
+    st = walls ? rhs_from_caller(h, u_ode, v_ode) : sort_fluid_cells(h, u_ode, nullptr);
+    if (st != TP_OK) return st;
+    interp_launch(h, v_ode, u_ode, points, (long long)n_points, smoothing_length, walls,
+                  cut_off_bnd != 0, clip_negative_pressure != 0, include_wall_velocity != 0,
+                  computed_density, velocity, pressure, density, neighbor_count);
+    TP_LAUNCHED(h, "interpolate points");
+    return TP_OK;
+}
+
 tp_status tp_set_pair_mode(tp_handle* h, int32_t mode) {
     if (!h) return TP_ERR_ARGUMENT;
     if (mode != TP_PAIR_GATHER && mode != TP_PAIR_SYMMETRIC)

@@ -34,6 +34,13 @@ tp_status sort_fluid_cells(tp_handle* h, const double* u, int* maxcell);
 extern const double kCK2N54_A[5];
 extern const double kCK2N54_B[5];
 
+// Interpolation at points (tp_interp.cu); fluid cell sort (and, with walls, the Adami pass) of
+// the same state must precede it on the handle's stream.
+void interp_launch(tp_handle* h, const double* v, const double* u, const double* pts,
+                   long long np, double hi, int walls, int cut_off_bnd, int clip,
+                   int wall_velocity, double* cd, double* vel, double* pres, double* dens,
+                   int* count);
+
 // Differentiation form (tp_adjoint.cu)
 void adjoint_release(tp_handle* h);
 
