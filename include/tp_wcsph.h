@@ -261,6 +261,16 @@ tp_status tp_get_config(const tp_handle* h, tp_config* out);
 /* Threads per block of the pair and Adami kernels: 64, 128 (default) or 256 (autotuning). */
 tp_status tp_set_launch(tp_handle* h, int32_t pair_block);
 
+/*
+ * SymplecticPositionVerlet (ext/TrixiParticlesOrdinaryDiffEqSymplecticRKExt.jl:89-171): n_steps
+ * steps of size dt on (v_ode, u_ode) in place, two kick! evaluations per step -- half drift,
+ * half kick, kick at the midpoint, velocity update, the scheme's density update
+ * rho = rho_prev (2 - eps) / (2 + eps) with eps = -(drho/dt) dt / rho_half, second half drift.
+ * Each kick rebuilds the neighbour search from the caller-ordered state (as tp_kick).
+ */
+tp_status tp_integrate_spv(tp_handle* h, double* v_ode, double* u_ode, double t0, double dt,
+                           int64_t n_steps);
+
 /* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
 int64_t tp_kernel_launches(const tp_handle* h);
 

@@ -52,6 +52,8 @@ def lib():
         L.orc_integrate_ck2n54.restype = c_int
         L.orc_integrate_ck2n54.argtypes = [c_void_p, dp, dp, c_double, c_int64]
         L.orc_ck2n54_coefficients.argtypes = [dp, dp, dp]
+        L.orc_integrate_spv.restype = c_int
+        L.orc_integrate_spv.argtypes = [c_void_p, dp, dp, c_double, c_int64]
         L.orc_interpolate.argtypes = [c_void_p, dp, dp, dp, c_int64, c_double, c_int, c_int,
                                       c_int, dp, dp, dp, dp, ip]
         L.orc_nhs.restype = c_int
@@ -160,6 +162,13 @@ class Model:
                                _ip(cnt))
         return dict(computed_density=cd, velocity=ve, pressure=pr, density=de,
                     neighbor_count=cnt)
+
+    def integrate_spv(self, v: np.ndarray, u: np.ndarray, dt: float, n_steps: int):
+        """SymplecticPositionVerlet steps (2 RHS evaluations per step)."""
+        v = np.array(v, dtype=np.float64).reshape(-1)
+        u = np.array(u, dtype=np.float64).reshape(-1)
+        st = self.L.orc_integrate_spv(self.h, _dp(v), _dp(u), dt, n_steps)
+        return v, u, st
 
     def integrate(self, v: np.ndarray, u: np.ndarray, dt: float, n_steps: int):
         v = np.array(v, dtype=np.float64).reshape(-1)

@@ -537,6 +537,40 @@ int orc_integrate_ck2n54(orc_model* p, double* v, double* u, double dt, int64_t 
     return status;
 }
 
+// SymplecticPositionVerlet (ext/TrixiParticlesOrdinaryDiffEqSymplecticRKExt.jl:89-171), the
+// @muladd forms as fused multiply-adds:
+//   u_h = uprev + (dt/2) v_prev;  v_h = vprev + (dt/2) kick(vprev, uprev);  k = kick(v_h, u_h);
+//   v = vprev + dt k (velocity rows);  rho = rho_prev (2 - eps) / (2 + eps),
+//   eps = (-k_rho / rho_h) dt;  u = u_h + (dt/2) v.
+int orc_integrate_spv(orc_model* p, double* v, double* u, double dt, int64_t n_steps) {
+    Model* m = reinterpret_cast<Model*>(p);
+    const int nd = m->nd;
+    const int64_t nf = m->nf, nvv = nf * (nd + 1), nuu = nf * nd;
+    std::vector<double> kv(nvv), ku(nuu), vh(nvv), uh(nuu);
+    const double half = 0.5, dth = dt * half;
+    int status = 0;
+    for (int64_t step = 0; step < n_steps; ++step) {
+        m->drift(ku.data(), v);
+        for (int64_t i = 0; i < nuu; ++i) uh[i] = std::fma(dth, ku[i], u[i]);
+        m->kick(kv.data(), v, u);
+        if (!m->grid_ok) status = 3;
+        for (int64_t i = 0; i < nvv; ++i) vh[i] = std::fma(dth, kv[i], v[i]);
+        m->kick(kv.data(), vh.data(), uh.data());
+        if (!m->grid_ok) status = 3;
+        for (int64_t a = 0; a < nf; ++a) {
+            for (int d = 0; d < nd; ++d)
+                v[a * (nd + 1) + d] = std::fma(dt, kv[a * (nd + 1) + d], v[a * (nd + 1) + d]);
+            const double rho_prev = v[a * (nd + 1) + nd];
+            const double rho_half = vh[a * (nd + 1) + nd];
+            const double eps = (-kv[a * (nd + 1) + nd] / rho_half) * dt;
+            v[a * (nd + 1) + nd] = rho_prev * (2.0 - eps) / (2.0 + eps);
+        }
+        m->drift(ku.data(), v);
+        for (int64_t i = 0; i < nuu; ++i) u[i] = std::fma(dth, ku[i], uh[i]);
+    }
+    return status;
+}
+
 void orc_interpolate(orc_model* p, const double* v, const double* u, const double* points,
                      int64_t n_points, double smoothing_length, int cut_off_bnd,
                      int clip_negative_pressure, int include_wall_velocity,

@@ -56,6 +56,8 @@ static int run(int nd, int precision) {
     bad |= tp_cell_sort_noalloc(&c, u.data(), c.n_fluid, cell.data(), order.data(), nullptr) !=
            TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, -1) != TP_ERR_ARGUMENT;
+    bad |= tp_integrate_spv(h, v.data(), u.data(), 0.0, 1e-4, 3) != TP_OK;
+    bad |= tp_integrate_spv(h, v.data(), u.data(), 0.0, 1e-4, -2) != TP_ERR_ARGUMENT;
     // differentiation form: forward with checkpoints, two backward sweeps, argument checks
     double pbar[3];
     std::vector<double> vbar(v.size(), 0.5), ubar(u.size(), 0.25);

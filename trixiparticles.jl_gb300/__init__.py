@@ -18,6 +18,7 @@ from .semidiscretization import (
     GridNeighborhoodSearch,
     ODEProblem,
     Semidiscretization,
+    SymplecticPositionVerlet,
     WallBoundarySystem,
     WeaklyCompressibleSPHSystem,
     WendlandC2Kernel,
@@ -35,7 +36,8 @@ __all__ = [
     "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
     "CarpenterKennedy2N54", "ContinuityDensity", "DensityDiffusionMolteniColagrossi",
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
-    "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole", "TpConfig",
+    "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole",
+    "SymplecticPositionVerlet", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
     "adjoint", "build", "dam_break", "ensemble", "interpolate_line", "interpolate_points",
     "interpolation", "dam_break_semidiscretization", "default_config", "drift", "kick",

@@ -99,6 +99,43 @@ __global__ void k_drift(double* __restrict__ du, const double* __restrict__ v, i
     for (int d = 0; d < ND; ++d) du[(size_t)i * ND + d] = v[(size_t)i * (ND + 1) + d];
 }
 
+// SymplecticPositionVerlet pieces (the @muladd forms as fma):
+// u_h = u + (dt/2) v[0:nd]
+template <int ND>
+__global__ void k_spv_half_drift(const double* __restrict__ u, const double* __restrict__ v,
+                                 double dth, double* __restrict__ uh, int n) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+        uh[(size_t)a * ND + d] = fma(dth, v[(size_t)a * (ND + 1) + d], u[(size_t)a * ND + d]);
+}
+
+// v_h = v + (dt/2) k (all rows)
+__global__ void k_spv_half_kick(const double* __restrict__ v, const double* __restrict__ k,
+                                double dth, double* __restrict__ vh, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) vh[i] = fma(dth, k[i], v[i]);
+}
+
+// v = v + dt k (velocity rows); rho = rho (2 - eps) / (2 + eps), eps = (-k_rho / rho_h) dt;
+// u = u_h + (dt/2) v
+template <int ND>
+__global__ void k_spv_finish(double* __restrict__ v, double* __restrict__ u,
+                             const double* __restrict__ k, const double* __restrict__ vh,
+                             const double* __restrict__ uh, double dt, double dth, int n) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    double* va = v + (size_t)a * (ND + 1);
+    const double* ka = k + (size_t)a * (ND + 1);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) va[d] = fma(dt, ka[d], va[d]);
+    const double eps = (-ka[ND] / vh[(size_t)a * (ND + 1) + ND]) * dt;
+    va[ND] = va[ND] * (2.0 - eps) / (2.0 + eps);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) u[(size_t)a * ND + d] = fma(dth, va[d], uh[(size_t)a * ND + d]);
+}
+
 __global__ void k_gate_init(unsigned* __restrict__ gate, float threshold) {
     if (threadIdx.x == 0) {
         gate[0] = 1u;
@@ -716,7 +753,7 @@ tp_status tp_destroy(tp_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
-                    h->d_max, h->e_ff, h->e_fw, h->ec_ff, h->ec_fw, h->acc};
+                    h->d_max, h->e_ff, h->e_fw, h->ec_ff, h->ec_fw, h->acc, h->spv};
     for (void* p : more)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
@@ -809,6 +846,56 @@ tp_status tp_kick(tp_handle* h, double* dv_ode, const double* v_ode, const doubl
     h->launches += (nf > 0);
     mark(h, 3);
     finish_timing(h);
+    return TP_OK;
+}
+
+tp_status tp_integrate_spv(tp_handle* h, double* v_ode, double* u_ode, double t0, double dt,
+                           int64_t n_steps) {
+    (void)t0;
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    if (n_steps < 0 || !std::isfinite(dt))
+        return fail(h, TP_ERR_ARGUMENT, "tp_integrate_spv: bad step count or dt");
+    const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
+    if (nf == 0 || n_steps == 0) return TP_OK;
+    if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_integrate_spv: null array");
+    const size_t nv = (size_t)nf * (nd + 1), nu = (size_t)nf * nd;
+    if (!h->spv) TP_CUDA(h, dalloc(&h->spv, 2 * nv + nu));  // k, v_h, u_h
+    double* k = h->spv;
+    double* vh = k + nv;
+    double* uh = vh + nv;
+    const double dth = dt * 0.5;
+    auto kick = [&](const double* v, const double* u) -> tp_status {
+        tp_status s2 = rhs_from_caller(h, u, v);
+        if (s2 != TP_OK) return s2;
+        if (h->cfg.precision == TP_PRECISION_FP32)
+            fp32_pair_kick(h, k);
+        else
+            fp64_pair_kick(h, k);
+        TP_LAUNCHED(h, "spv kick");
+        h->launches += 1;
+        return TP_OK;
+    };
+    for (int64_t step = 0; step < n_steps; ++step) {
+        if (nd == 2)
+            k_spv_half_drift<2><<<nblk(nf, 256), 256, 0, h->stream>>>(u_ode, v_ode, dth, uh, nf);
+        else
+            k_spv_half_drift<3><<<nblk(nf, 256), 256, 0, h->stream>>>(u_ode, v_ode, dth, uh, nf);
+        st = kick(v_ode, u_ode);
+        if (st != TP_OK) return st;
+        k_spv_half_kick<<<nblk((long)nv, 256), 256, 0, h->stream>>>(v_ode, k, dth, vh,
+                                                                   (long long)nv);
+        st = kick(vh, uh);
+        if (st != TP_OK) return st;
+        if (nd == 2)
+            k_spv_finish<2><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, u_ode, k, vh, uh, dt,
+                                                                   dth, nf);
+        else
+            k_spv_finish<3><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, u_ode, k, vh, uh, dt,
+                                                                   dth, nf);
+        TP_LAUNCHED(h, "spv update");
+        h->launches += 3;
+    }
     return TP_OK;
 }
 

@@ -119,6 +119,9 @@ struct tp_handle {
     double phase_ms[tp::kNumPhases] = {};
     long long launches = 0;  // kernel launches issued on this handle
 
+    // ---- SymplecticPositionVerlet scratch: k, v_half, u_half (caller order) ----
+    double* spv = nullptr;
+
     // ---- differentiation form: checkpoints, tape and adjoint buffers (tp_adjoint.cu) ----
     tp::AdjointState* adj = nullptr;
 };

@@ -378,6 +378,12 @@ class CarpenterKennedy2N54:
     williamson_condition: bool = False
 
 
+@dataclass(frozen=True)
+class SymplecticPositionVerlet:
+    """The reference's SymplecticPositionVerlet (2 kick! evaluations per step, density updated
+    by rho_prev (2 - eps) / (2 + eps))."""
+
+
 @dataclass
 class ODESolution:
     v: object
@@ -391,8 +397,9 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
           save_everystep: bool = False) -> ODESolution:
     """Fixed-step CarpenterKennedy2N54 from tspan[0] for `n_steps` steps (default: to tspan[1]).
     The state is advanced by the fused library integrator; v/u of the result are new tensors."""
-    if not isinstance(alg, CarpenterKennedy2N54):
-        raise _argument_error("only CarpenterKennedy2N54 is provided by the GB300 backend")
+    if not isinstance(alg, (CarpenterKennedy2N54, SymplecticPositionVerlet)):
+        raise _argument_error("only CarpenterKennedy2N54 and SymplecticPositionVerlet are "
+                              "provided by the GB300 backend")
     semi = ode.p["semi"]
     t0, t1 = ode.tspan
     if n_steps is None:
@@ -400,8 +407,10 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
     v = ode.v0.clone()
     u = ode.u0.clone()
     semi._set_stream()
-    semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(t0),
-               ctypes.c_double(dt), ctypes.c_int64(n_steps))
+    entry = "tp_integrate_spv" if isinstance(alg, SymplecticPositionVerlet) else \
+        "tp_integrate_ck2n54"
+    semi._call(entry, v.data_ptr(), u.data_ptr(), ctypes.c_double(t0), ctypes.c_double(dt),
+               ctypes.c_int64(n_steps))
     semi.sync()
     return ODESolution(v=v, u=u, t=t0 + n_steps * dt, n_steps=n_steps)
 
