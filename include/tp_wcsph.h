@@ -271,6 +271,18 @@ tp_status tp_set_launch(tp_handle* h, int32_t pair_block);
 tp_status tp_integrate_spv(tp_handle* h, double* v_ode, double* u_ode, double t0, double dt,
                            int64_t n_steps);
 
+/*
+ * SortingCallback's sort_particles! (src/callbacks/sorting.jl:116-158): reorders the fluid
+ * particles of (v_ode, u_ode) in place by their neighbour-search cell -- the stable order of the
+ * lexicographic cell coordinates (cx, cy, cz), as Julia's sortperm over SVector cell coordinates
+ * -- and writes the permutation (new position j holds old particle perm_out[j], 0-based) when
+ * perm_out is non-null (device).  The reference moves coordinates, velocity, density and
+ * pressure but not the masses (a TODO there); sort_masses = 0 keeps that behaviour, 1 also
+ * moves the handle's fluid masses with their particles.  Asynchronous.
+ */
+tp_status tp_sort_particles(tp_handle* h, double* v_ode, double* u_ode, int32_t sort_masses,
+                            int32_t* perm_out);
+
 /* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
 int64_t tp_kernel_launches(const tp_handle* h);
 

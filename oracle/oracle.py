@@ -52,6 +52,8 @@ def lib():
         L.orc_integrate_ck2n54.restype = c_int
         L.orc_integrate_ck2n54.argtypes = [c_void_p, dp, dp, c_double, c_int64]
         L.orc_ck2n54_coefficients.argtypes = [dp, dp, dp]
+        L.orc_sort_perm.restype = c_int
+        L.orc_sort_perm.argtypes = [c_void_p, dp, c_int64, ip]
         L.orc_integrate_spv.restype = c_int
         L.orc_integrate_spv.argtypes = [c_void_p, dp, dp, c_double, c_int64]
         L.orc_interpolate.argtypes = [c_void_p, dp, dp, dp, c_int64, c_double, c_int, c_int,
@@ -188,6 +190,16 @@ def nhs(cfg, x_f: np.ndarray, x_w: np.ndarray):
     st = L.orc_nhs(ctypes.byref(cfg), _dp(xf), _dp(xw), _ip(out["cell"]), _ip(out["order"]),
                    _ip(out["nnb_ff"]), _ip(out["nnb_fw"]), _ip(out["nnb_wf"]))
     return out, st
+
+
+def sort_perm(cfg, x: np.ndarray) -> np.ndarray:
+    """SortingCallback permutation of coordinates x (n, nd)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    perm = np.zeros(x.shape[0], dtype=np.int32)
+    st = lib().orc_sort_perm(ctypes.byref(cfg), _dp(x.reshape(-1)), x.shape[0], _ip(perm))
+    if st != 0:
+        raise RuntimeError("oracle: bad configuration")
+    return perm
 
 
 def ck2n54_coefficients():

@@ -19,6 +19,7 @@
 //     solution 3, applied as  tmp = dt*k; u += B1*tmp;  then per stage i>=2:
 //     tmp = A_i*tmp; tmp += dt*k; u += B_i*tmp  (muladd fused, as the @muladd of that package).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -569,6 +570,24 @@ int orc_integrate_spv(orc_model* p, double* v, double* u, double dt, int64_t n_s
         for (int64_t i = 0; i < nuu; ++i) u[i] = std::fma(dth, ku[i], uh[i]);
     }
     return status;
+}
+
+// SortingCallback's permutation (src/callbacks/sorting.jl:135-158): sortperm over the
+// SVector cell coordinates (lexicographic, stable), cells as in the neighbour search.
+int orc_sort_perm(const tp_config* cfg, const double* x, int64_t n, int32_t* perm) {
+    Grid g;
+    if (!g.init(*cfg)) return 1;
+    std::vector<std::array<int64_t, 3>> cc(n);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t c[3];
+        g.cell_of(x + i * g.nd, c);
+        cc[i] = {c[0], c[1], c[2]};
+    }
+    std::vector<int32_t> p(n);
+    std::iota(p.begin(), p.end(), 0);
+    std::stable_sort(p.begin(), p.end(), [&](int32_t a, int32_t b) { return cc[a] < cc[b]; });
+    std::copy(p.begin(), p.end(), perm);
+    return 0;
 }
 
 void orc_interpolate(orc_model* p, const double* v, const double* u, const double* points,

@@ -57,6 +57,11 @@ static int run(int nd, int precision) {
            TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, -1) != TP_ERR_ARGUMENT;
     bad |= tp_integrate_spv(h, v.data(), u.data(), 0.0, 1e-4, 3) != TP_OK;
+    {
+        std::vector<int32_t> perm(c.n_fluid);
+        bad |= tp_sort_particles(h, v.data(), u.data(), 1, perm.data()) != TP_OK;
+        bad |= tp_sort_particles(h, v.data(), u.data(), 0, nullptr) != TP_OK;
+    }
     bad |= tp_integrate_spv(h, v.data(), u.data(), 0.0, 1e-4, -2) != TP_ERR_ARGUMENT;
     // differentiation form: forward with checkpoints, two backward sweeps, argument checks
     double pbar[3];

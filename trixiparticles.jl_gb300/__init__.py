@@ -18,6 +18,7 @@ from .semidiscretization import (
     GridNeighborhoodSearch,
     ODEProblem,
     Semidiscretization,
+    SortingCallback,
     SymplecticPositionVerlet,
     WallBoundarySystem,
     WeaklyCompressibleSPHSystem,
@@ -37,7 +38,7 @@ __all__ = [
     "CarpenterKennedy2N54", "ContinuityDensity", "DensityDiffusionMolteniColagrossi",
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
     "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole",
-    "SymplecticPositionVerlet", "TpConfig",
+    "SortingCallback", "SymplecticPositionVerlet", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
     "adjoint", "build", "dam_break", "ensemble", "interpolate_line", "interpolate_points",
     "interpolation", "dam_break_semidiscretization", "default_config", "drift", "kick",

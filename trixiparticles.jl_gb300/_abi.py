@@ -109,6 +109,7 @@ PROTOTYPES = [
     ("tp_get_config", c_int32, [c_void_p, POINTER(TpConfig)]),
     ("tp_set_pair_mode", c_int32, [c_void_p, c_int32]),
     ("tp_integrate_spv", c_int32, [c_void_p, c_void_p, c_void_p, c_double, c_double, c_int64]),
+    ("tp_sort_particles", c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     ("tp_interpolate_points", c_int32,
      [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_double, c_int32, c_int32, c_int32,
       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

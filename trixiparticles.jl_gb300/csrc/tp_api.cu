@@ -99,6 +99,22 @@ __global__ void k_drift(double* __restrict__ du, const double* __restrict__ v, i
     for (int d = 0; d < ND; ++d) du[(size_t)i * ND + d] = v[(size_t)i * (ND + 1) + d];
 }
 
+// Gather of the caller-ordered state into the order perm (new j <- old perm[j]).
+template <int ND>
+__global__ void k_permute_state(const int* __restrict__ perm, const double* __restrict__ v,
+                                const double* __restrict__ u, const double* __restrict__ m,
+                                double* __restrict__ v2, double* __restrict__ u2,
+                                double* __restrict__ m2, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int i = perm[j];
+#pragma unroll
+    for (int d = 0; d <= ND; ++d) v2[(size_t)j * (ND + 1) + d] = v[(size_t)i * (ND + 1) + d];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) u2[(size_t)j * ND + d] = u[(size_t)i * ND + d];
+    if (m2) m2[j] = m[i];
+}
+
 // SymplecticPositionVerlet pieces (the @muladd forms as fma):
 // u_h = u + (dt/2) v[0:nd]
 template <int ND>
@@ -401,9 +417,17 @@ bool setup_grid(tp_handle* h, std::string& msg) {
 // `gate`: device rebuild gate (null = always).  `maxcell`: if non-null, receives (atomicMax) the
 // largest cell occupancy of this sort.
 tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start,
-                         const unsigned* gate = nullptr, int* maxcell = nullptr) {
+                         const unsigned* gate = nullptr, int* maxcell = nullptr,
+                         bool lex = false) {
     if (n > 0) {
-        if (h->cfg.ndims == 2)
+        if (lex) {
+            if (h->cfg.ndims == 2)
+                k_cell_keys<2, true><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key,
+                                                                           h->f_count, h->d_err);
+            else
+                k_cell_keys<3, true><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key,
+                                                                           h->f_count, h->d_err);
+        } else if (h->cfg.ndims == 2)
             k_cell_keys<2><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
                                                                  h->d_err, gate);
         else
@@ -846,6 +870,43 @@ tp_status tp_kick(tp_handle* h, double* dv_ode, const double* v_ode, const doubl
     h->launches += (nf > 0);
     mark(h, 3);
     finish_timing(h);
+    return TP_OK;
+}
+
+tp_status tp_sort_particles(tp_handle* h, double* v_ode, double* u_ode, int32_t sort_masses,
+                            int32_t* perm_out) {
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
+    if (nf == 0) return TP_OK;
+    if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_sort_particles: null array");
+    const size_t nv = (size_t)nf * (nd + 1), nu = (size_t)nf * nd;
+    if (!h->spv) TP_CUDA(h, dalloc(&h->spv, 2 * nv + nu));  // scratch: v, u, m fit in it
+    st = sort_particles(h, u_ode, nf, h->f_key, h->f_tmp, h->f_start, nullptr, nullptr, true);
+    if (st != TP_OK) return st;
+    k_rank_pack<<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_tmp, h->f_key, h->f_start, nf,
+                                                       h->f_perm, h->f_skey, NoPack{}, nullptr);
+    double* v2 = h->spv;
+    double* u2 = v2 + nv;
+    double* m2 = sort_masses ? u2 + nu : nullptr;
+    if (nd == 2)
+        k_permute_state<2><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_perm, v_ode, u_ode, h->m_f,
+                                                                  v2, u2, m2, nf);
+    else
+        k_permute_state<3><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_perm, v_ode, u_ode, h->m_f,
+                                                                  v2, u2, m2, nf);
+    TP_LAUNCHED(h, "sort particles");
+    h->launches += 2;
+    TP_CUDA(h, cudaMemcpyAsync(v_ode, v2, nv * sizeof(double), cudaMemcpyDeviceToDevice,
+                               h->stream));
+    TP_CUDA(h, cudaMemcpyAsync(u_ode, u2, nu * sizeof(double), cudaMemcpyDeviceToDevice,
+                               h->stream));
+    if (m2)
+        TP_CUDA(h, cudaMemcpyAsync(h->m_f, m2, (size_t)nf * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+    if (perm_out)
+        TP_CUDA(h, cudaMemcpyAsync(perm_out, h->f_perm, (size_t)nf * sizeof(int),
+                                   cudaMemcpyDeviceToDevice, h->stream));
     return TP_OK;
 }
 

@@ -34,7 +34,9 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-template <int ND>
+// LEX: key with z fastest, i.e. lexicographic order of (cx, cy, cz) -- the order of Julia's
+// sortperm over SVector cell coordinates (SortingCallback); default: x fastest (the cell list).
+template <int ND, bool LEX = false>
 __global__ void __launch_bounds__(256) k_cell_keys(const double* __restrict__ u, int n,
                                                    GridDesc g, int* __restrict__ key,
                                                    int* __restrict__ count, int* __restrict__ err,
@@ -50,7 +52,7 @@ __global__ void __launch_bounds__(256) k_cell_keys(const double* __restrict__ u,
     int c[3];
     const int e = cell_coords<ND>(x, g, c);
     if (e) atomicOr(err, e);
-    const int k = cell_key(c, g);
+    const int k = LEX ? c[2] + g.n[2] * (c[1] + g.n[1] * c[0]) : cell_key(c, g);
     key[i] = k;
     const unsigned peers = __match_any_sync(vmask, k);
     if (lane_id() == __ffs(peers) - 1) atomicAdd(&count[k], __popc(peers));

@@ -384,6 +384,37 @@ class SymplecticPositionVerlet:
     by rho_prev (2 - eps) / (2 + eps))."""
 
 
+class SortingCallback:
+    """SortingCallback(; interval=-1, dt=0.0, initial_sort=true) (src/callbacks/sorting.jl:
+    24-55): reorder the fluid particles by neighbour-search cell at the end of every `interval`
+    steps, or at the first step after every `dt` of integration time, and (initial_sort) once
+    before the first step.  `sort_masses` (not in the reference) also moves the fluid masses with
+    their particles; the reference leaves them in place (a TODO there), which is the default."""
+
+    def __init__(self, *, interval: int = -1, dt: float = 0.0, initial_sort: bool = True,
+                 sort_masses: bool = False):
+        if dt > 0 and interval > 0:
+            raise _argument_error("setting both `interval` and `dt` is not supported")
+        if dt <= 0 and interval <= 0:
+            raise _argument_error("either `interval` or `dt` must be set to a positive value")
+        self.interval = int(interval) if dt <= 0 else None
+        self.dt = float(dt) if dt > 0 else None
+        self.initial_sort = bool(initial_sort)
+        self.sort_masses = bool(sort_masses)
+        self.last_t = 0.0
+
+    def sort(self, semi, v, u, perm=None):
+        """Sorts (v, u) in place; returns the composed permutation (original index of every
+        current particle) when `perm` (the previous one) is given."""
+        import torch
+
+        p = torch.empty(semi.n_fluid, dtype=torch.int32, device=v.device)
+        semi._set_stream()
+        semi._call("tp_sort_particles", v.data_ptr(), u.data_ptr(), int(self.sort_masses),
+                   p.data_ptr())
+        return p.long() if perm is None else perm[p.long()]
+
+
 @dataclass
 class ODESolution:
     v: object
@@ -391,10 +422,11 @@ class ODESolution:
     t: float
     n_steps: int
     retcode: str = "Success"
+    perm: object = None  # with a SortingCallback: original index of every particle
 
 
 def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int | None = None,
-          save_everystep: bool = False) -> ODESolution:
+          save_everystep: bool = False, callback=None) -> ODESolution:
     """Fixed-step CarpenterKennedy2N54 from tspan[0] for `n_steps` steps (default: to tspan[1]).
     The state is advanced by the fused library integrator; v/u of the result are new tensors."""
     if not isinstance(alg, (CarpenterKennedy2N54, SymplecticPositionVerlet)):
@@ -409,10 +441,40 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
     semi._set_stream()
     entry = "tp_integrate_spv" if isinstance(alg, SymplecticPositionVerlet) else \
         "tp_integrate_ck2n54"
-    semi._call(entry, v.data_ptr(), u.data_ptr(), ctypes.c_double(t0), ctypes.c_double(dt),
-               ctypes.c_int64(n_steps))
+    cbs = callback if isinstance(callback, (list, tuple)) else \
+        ([] if callback is None else [callback])
+    sorters = [c for c in cbs if isinstance(c, SortingCallback)]
+    if len(sorters) != len(cbs):
+        raise _argument_error("only SortingCallback is supported as a callback")
+
+    def advance(t, k):
+        semi._call(entry, v.data_ptr(), u.data_ptr(), ctypes.c_double(t), ctypes.c_double(dt),
+                   ctypes.c_int64(k))
+
+    perm = None
+    if not sorters:
+        advance(t0, n_steps)
+    else:
+        cb = sorters[0]
+        cb.last_t = t0
+        if cb.initial_sort:
+            perm = cb.sort(semi, v, u)
+        done = 0
+        while done < n_steps:
+            if cb.interval is not None:
+                k = min(cb.interval, n_steps - done)
+            else:  # first step after every dt of integration time
+                k = max(1, min(n_steps - done,
+                               int(math.ceil((cb.last_t + cb.dt - (t0 + done * dt)) / dt
+                                             - 1e-9))))
+            advance(t0 + done * dt, k)
+            done += k
+            t = t0 + done * dt
+            if cb.interval is not None or t - cb.last_t >= cb.dt - 1e-12:
+                perm = cb.sort(semi, v, u, perm)
+                cb.last_t = t
     semi.sync()
-    return ODESolution(v=v, u=u, t=t0 + n_steps * dt, n_steps=n_steps)
+    return ODESolution(v=v, u=u, t=t0 + n_steps * dt, n_steps=n_steps, perm=perm)
 
 
 def dam_break_semidiscretization(tank, eos, smoothing_length: float, *, precision="float64",
