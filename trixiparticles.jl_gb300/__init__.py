@@ -30,7 +30,8 @@ from .semidiscretization import (
     solve,
 )
 from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
-from . import adjoint, ensemble, interpolation
+from . import adjoint, ensemble, interpolation, vtk
+from .vtk import SolutionSavingCallback, trixi2vtk, vtk2trixi
 from .interpolation import interpolate_line, interpolate_points
 
 __all__ = [
@@ -40,7 +41,8 @@ __all__ = [
     "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole",
     "SortingCallback", "SymplecticPositionVerlet", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
-    "adjoint", "build", "dam_break", "ensemble", "interpolate_line", "interpolate_points",
+    "SolutionSavingCallback", "adjoint", "build", "dam_break", "ensemble", "trixi2vtk",
+    "vtk", "vtk2trixi", "interpolate_line", "interpolate_points",
     "interpolation", "dam_break_semidiscretization", "default_config", "drift", "kick",
     "load_library", "semidiscretize", "solve",
 ]

@@ -427,8 +427,10 @@ class ODESolution:
 
 def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int | None = None,
           save_everystep: bool = False, callback=None) -> ODESolution:
-    """Fixed-step CarpenterKennedy2N54 from tspan[0] for `n_steps` steps (default: to tspan[1]).
-    The state is advanced by the fused library integrator; v/u of the result are new tensors."""
+    """Fixed-step CarpenterKennedy2N54 or SymplecticPositionVerlet from tspan[0] for `n_steps`
+    steps (default: to tspan[1]), advanced by the library's fused integrators; v/u of the result
+    are new tensors.  `callback`: SortingCallback and/or SolutionSavingCallback (one or a list),
+    applied between integrator calls at their step / time intervals."""
     if not isinstance(alg, (CarpenterKennedy2N54, SymplecticPositionVerlet)):
         raise _argument_error("only CarpenterKennedy2N54 and SymplecticPositionVerlet are "
                               "provided by the GB300 backend")
@@ -441,38 +443,49 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
     semi._set_stream()
     entry = "tp_integrate_spv" if isinstance(alg, SymplecticPositionVerlet) else \
         "tp_integrate_ck2n54"
+    from .vtk import SolutionSavingCallback
+
     cbs = callback if isinstance(callback, (list, tuple)) else \
         ([] if callback is None else [callback])
-    sorters = [c for c in cbs if isinstance(c, SortingCallback)]
-    if len(sorters) != len(cbs):
-        raise _argument_error("only SortingCallback is supported as a callback")
+    for c in cbs:
+        if not isinstance(c, (SortingCallback, SolutionSavingCallback)):
+            raise _argument_error("only SortingCallback and SolutionSavingCallback are "
+                                  "supported as callbacks")
 
     def advance(t, k):
         semi._call(entry, v.data_ptr(), u.data_ptr(), ctypes.c_double(t), ctypes.c_double(dt),
                    ctypes.c_int64(k))
 
+    def next_step(c, done):
+        if c.interval is not None:
+            return (done // c.interval + 1) * c.interval
+        return max(done + 1, int(math.ceil((c.last_t + c.dt - t0) / dt - 1e-9)))
+
     perm = None
-    if not sorters:
-        advance(t0, n_steps)
-    else:
-        cb = sorters[0]
-        cb.last_t = t0
-        if cb.initial_sort:
-            perm = cb.sort(semi, v, u)
-        done = 0
-        while done < n_steps:
-            if cb.interval is not None:
-                k = min(cb.interval, n_steps - done)
-            else:  # first step after every dt of integration time
-                k = max(1, min(n_steps - done,
-                               int(math.ceil((cb.last_t + cb.dt - (t0 + done * dt)) / dt
-                                             - 1e-9))))
-            advance(t0 + done * dt, k)
-            done += k
-            t = t0 + done * dt
-            if cb.interval is not None or t - cb.last_t >= cb.dt - 1e-12:
-                perm = cb.sort(semi, v, u, perm)
-                cb.last_t = t
+    for c in cbs:
+        c.last_t = t0
+        if isinstance(c, SortingCallback) and c.initial_sort:
+            perm = c.sort(semi, v, u, perm)
+        if isinstance(c, SolutionSavingCallback) and c.save_initial_solution:
+            c.save(semi, v, u, t0)
+    done = 0
+    while done < n_steps:
+        nxt = min([n_steps] + [next_step(c, done) for c in cbs])
+        advance(t0 + done * dt, nxt - done)
+        done = nxt
+        t = t0 + done * dt
+        for c in cbs:
+            if next_step(c, done - 1) != done:
+                continue
+            if isinstance(c, SortingCallback):
+                perm = c.sort(semi, v, u, perm)
+                c.last_t = t
+            else:
+                c.save(semi, v, u, t)
+    for c in cbs:
+        if isinstance(c, SolutionSavingCallback) and c.save_final_solution and \
+                c.last_t != t0 + n_steps * dt:
+            c.save(semi, v, u, t0 + n_steps * dt)
     semi.sync()
     return ODESolution(v=v, u=u, t=t0 + n_steps * dt, n_steps=n_steps, perm=perm)
 
