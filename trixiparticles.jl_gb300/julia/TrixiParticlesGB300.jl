@@ -18,7 +18,7 @@
 # installed where it was written, so it has not been executed.
 module TrixiParticlesGB300
 
-using CUDA: CUDA, CuArray, CuPtr
+using CUDA: CUDA, CuArray, CuMatrix, CuPtr
 using KernelAbstractions: KernelAbstractions
 using ChainRulesCore: ChainRulesCore
 using TrixiParticles: TrixiParticles, WeaklyCompressibleSPHSystem, WallBoundarySystem,
@@ -157,6 +157,43 @@ function integrate_ck2n54!(semi, v_ode, u_ode, t0, dt, nsteps)
                    h, v_ode, u_ode, t0, dt, nsteps))
     check(h, ccall((:tp_sync, libtp), Cint, (Ptr{Cvoid},), h))
     return v_ode, u_ode
+end
+
+# ---- SymplecticPositionVerlet, SortingCallback's sort, interpolation ----------------------
+function integrate_spv!(semi, v_ode, u_ode, t0, dt, nsteps)
+    h = handle(semi)
+    check(h, ccall((:tp_integrate_spv, libtp), Cint,
+                   (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Float64, Float64, Int64),
+                   h, v_ode, u_ode, t0, dt, nsteps))
+    return v_ode, u_ode
+end
+
+# sort_particles! of SortingCallback (the reference leaves masses in place: sort_masses=false)
+function sort_particles!(semi, v_ode, u_ode; sort_masses=false)
+    h = handle(semi)
+    perm = CUDA.zeros(Int32, length(u_ode) ÷ ndims(semi.systems[1]))
+    check(h, ccall((:tp_sort_particles, libtp), Cint,
+                   (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Int32, CuPtr{Int32}),
+                   h, v_ode, u_ode, sort_masses, perm))
+    return perm .+ Int32(1)
+end
+
+function interpolate_points(points::CuMatrix{Float64}, semi, v_ode, u_ode; smoothing_length,
+                            cut_off_bnd=true, clip_negative_pressure=false,
+                            include_wall_velocity=false)
+    h = handle(semi)
+    n = size(points, 2)
+    cd, p, rho = CUDA.zeros(n), CUDA.zeros(n), CUDA.zeros(n)
+    vel = CUDA.zeros(size(points, 1), n)
+    count = CUDA.zeros(Int32, n)
+    check(h, ccall((:tp_interpolate_points, libtp), Cint,
+                   (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, CuPtr{Float64}, Int64, Float64,
+                    Int32, Int32, Int32, CuPtr{Float64}, CuPtr{Float64}, CuPtr{Float64},
+                    CuPtr{Float64}, CuPtr{Int32}),
+                   h, v_ode, u_ode, points, n, smoothing_length, cut_off_bnd,
+                   clip_negative_pressure, include_wall_velocity, cd, vel, p, rho, count))
+    return (; computed_density=cd, point_coords=points, neighbor_count=count, velocity=vel,
+            pressure=p, density=rho)
 end
 
 # ---- Differentiation form: rrule of a fixed-step CarpenterKennedy2N54 solve -------------
