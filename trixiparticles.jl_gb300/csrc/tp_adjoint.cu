@@ -125,12 +125,33 @@ __device__ __forceinline__ T pos_diff(const double* __restrict__ xa, const doubl
 }
 
 // ------------------------------------------------------------------------------------------
-// Neighbour lists in caller order (entry k of particle i at list[k * n + i])
+// Neighbour lists in caller order (entry k of particle i at list[k * n + i]).  The search covers
+// the +-1 cells and reaches a second cell along an axis where the point lies within
+// m = r_list - cs of that cell face (the list radius exceeds the 2h cell size).
 // ------------------------------------------------------------------------------------------
+struct CellReach {
+    int lo[3], hi[3];  // inclusive cell ranges, clamped to the grid
+};
+
+__device__ __forceinline__ CellReach cell_reach(const GridDesc& g, const int c[3],
+                                                const double* x, int nd, double m) {
+    CellReach R;
+    for (int d = 0; d < 3; ++d) {
+        if (d < nd) {
+            const double o = x[d] - (double)(g.cmin[d] + c[d]) * g.cs;
+            R.lo[d] = max(c[d] - (o <= m ? 2 : 1), 0);
+            R.hi[d] = min(c[d] + (o >= g.cs - m ? 2 : 1), g.n[d] - 1);
+        } else {
+            R.lo[d] = R.hi[d] = 0;
+        }
+    }
+    return R;
+}
+
 template <int ND>
 __global__ void __launch_bounds__(128) k_adj_fluid_lists(
-    GridDesc g, double rl2, int nf, const double* __restrict__ x, const int* __restrict__ key,
-    const int* __restrict__ fstart, const int* __restrict__ fperm,
+    GridDesc g, double rl2, double m, int nf, const double* __restrict__ x,
+    const int* __restrict__ key, const int* __restrict__ fstart, const int* __restrict__ fperm,
     const double4_32a* __restrict__ wpos, const int* __restrict__ wstart, int* __restrict__ ff,
     int* __restrict__ ffc, int cap_ff, int* __restrict__ fw, int* __restrict__ fwc, int cap_fw,
     double* __restrict__ xb, int* __restrict__ err) {
@@ -144,12 +165,12 @@ __global__ void __launch_bounds__(128) k_adj_fluid_lists(
     }
     int c[3];
     key_to_coords(key[a], g, c);
+    const CellReach R = cell_reach(g, c, xa, ND, m);
     int n1 = 0, n2 = 0;
-    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz)
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            for (int s = fstart[row]; s < fstart[row + 3]; ++s) {
+    for (int cz = R.lo[2]; cz <= R.hi[2]; ++cz)
+        for (int cy = R.lo[1]; cy <= R.hi[1]; ++cy) {
+            const int rb = g.n[0] * (cy + g.n[1] * cz);
+            for (int s = fstart[rb + R.lo[0]]; s < fstart[rb + R.hi[0] + 1]; ++s) {
                 const int b = fperm[s];
                 if (b == a) continue;
                 double d2 = 0.0;
@@ -163,7 +184,7 @@ __global__ void __launch_bounds__(128) k_adj_fluid_lists(
                     ++n1;
                 }
             }
-            for (int w = wstart[row]; w < wstart[row + 3]; ++w) {
+            for (int w = wstart[rb + R.lo[0]]; w < wstart[rb + R.hi[0] + 1]; ++w) {
                 const double4_32a pw = wpos[w];
                 const double pwx[3] = {pw.x, pw.y, pw.z};
                 double d2 = 0.0;
@@ -185,7 +206,7 @@ __global__ void __launch_bounds__(128) k_adj_fluid_lists(
 
 template <int ND>
 __global__ void __launch_bounds__(128) k_adj_wall_lists(
-    GridDesc g, double rl2, int nw, const double4_32a* __restrict__ wpos,
+    GridDesc g, double rl2, double m, int nw, const double4_32a* __restrict__ wpos,
     const int* __restrict__ wskey, const double* __restrict__ x, const int* __restrict__ fstart,
     const int* __restrict__ fperm, int* __restrict__ wf, int* __restrict__ wfc, int cap_wf,
     int* __restrict__ err) {
@@ -195,12 +216,12 @@ __global__ void __launch_bounds__(128) k_adj_wall_lists(
     const double xw[3] = {pw.x, pw.y, pw.z};
     int c[3];
     key_to_coords(wskey[w], g, c);
+    const CellReach R = cell_reach(g, c, xw, ND, m);
     int n1 = 0;
-    const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz)
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int row = (c[0] - 1) + g.n[0] * ((c[1] + dy) + g.n[1] * (c[2] + dz));
-            for (int s = fstart[row]; s < fstart[row + 3]; ++s) {
+    for (int cz = R.lo[2]; cz <= R.hi[2]; ++cz)
+        for (int cy = R.lo[1]; cy <= R.hi[1]; ++cy) {
+            const int rb = g.n[0] * (cy + g.n[1] * cz);
+            for (int s = fstart[rb + R.lo[0]]; s < fstart[rb + R.hi[0] + 1]; ++s) {
                 const int b = fperm[s];
                 double d2 = 0.0;
 #pragma unroll
@@ -1050,14 +1071,16 @@ tp_status build_lists_at(tp_handle* h, const double* x) {
     if (st != TP_OK) return st;
     const double r = 2.0 * h->cfg.smoothing_length * (1.0 + A.skin);
     const double rl2 = r * r;
+    const double m = r - h->grid.cs;
     if (A.nf > 0)
         k_adj_fluid_lists<ND><<<nb(A.nf, 128), 128, 0, h->stream>>>(
-            h->grid, rl2, A.nf, x, h->f_key, h->f_start, h->f_perm, (const double4_32a*)h->w_pos,
-            h->w_start, A.ff, A.ffc, A.cap_ff, A.fw, A.fwc, A.cap_fw, A.xb, h->d_err);
+            h->grid, rl2, m, A.nf, x, h->f_key, h->f_start, h->f_perm,
+            (const double4_32a*)h->w_pos, h->w_start, A.ff, A.ffc, A.cap_ff, A.fw, A.fwc, A.cap_fw,
+            A.xb, h->d_err);
     if (A.nw > 0)
         k_adj_wall_lists<ND><<<nb(A.nw, 128), 128, 0, h->stream>>>(
-            h->grid, rl2, A.nw, (const double4_32a*)h->w_pos, h->w_skey, x, h->f_start, h->f_perm,
-            A.wf, A.wfc, A.cap_wf, h->d_err);
+            h->grid, rl2, m, A.nw, (const double4_32a*)h->w_pos, h->w_skey, x, h->f_start,
+            h->f_perm, A.wf, A.wfc, A.cap_wf, h->d_err);
     ADJ_LAUNCHED(h, "adjoint lists");
     A.kernels += 2;
     return TP_OK;

@@ -275,9 +275,9 @@ tp_status check_config(const tp_config* c, std::string& msg) {
         msg = "precision must be TP_PRECISION_FP64 or TP_PRECISION_FP32";
         return TP_ERR_ARGUMENT;
     }
-    if (c->n_fluid < 0 || c->n_wall < 0 || c->n_fluid >= (int64_t(1) << 30) ||
-        c->n_wall >= (int64_t(1) << 30)) {
-        msg = "particle counts must be in [0, 2^30)";
+    if (c->n_fluid < 0 || c->n_wall < 0 || c->n_fluid >= (int64_t(1) << kSlotBits) ||
+        c->n_wall >= (int64_t(1) << kSlotBits)) {
+        msg = "particle counts must be in [0, 2^25)";
         return TP_ERR_ARGUMENT;
     }
     if (!(c->smoothing_length > 0.0) || !std::isfinite(c->smoothing_length)) {
@@ -531,15 +531,17 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
     const double r = 2.0 * h->cfg.smoothing_length * (1.0 + skin);
     const float r2f = (float)(r * r * (1.0 + 1e-5));
     const float cs = (float)h->grid.cs;
+    // the search reaches two cells towards faces closer than r_list - cs (1e-5 cs rounding margin)
+    const float m = (float)(r - h->grid.cs + 1e-5 * h->grid.cs);
     auto run = [&](auto ndc) {
         constexpr int ND = decltype(ndc)::value;
         if (nf > 0)
             k_build_fluid_lists<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
-                h->grid, cs, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_start,
+                h->grid, cs, m, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_start,
                 h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate);
         if (nw > 0)
             k_build_wall_lists<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
-                h->grid, cs, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_start, h->l_wf,
+                h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_start, h->l_wf,
                 h->c_wf, h->cap_wf, h->d_err, gate);
     };
     if (h->cfg.ndims == 2)

@@ -7,25 +7,40 @@
 // reopens the rebuild gate before that can happen (see tp_nhs.cuh for the gate).
 //
 // Layout: entry k of slot s at list[k * stride + s] (stride = number of query slots), so the 32
-// lanes of a warp read one 128-byte line per k.  An entry is the candidate slot (27 bits) and
-// the candidate's cell offset code (dx+1) + 3(dy+1) + 9(dz+1) relative to the query's cell at
-// build time (top 5 bits), which the FP32 form needs to form cell-relative differences.
-// Entries are in PointNeighbors visiting order (rows in (dz, dy) order, ascending slots).
+// lanes of a warp read one 128-byte line per k.  An entry is the candidate slot (25 bits) and
+// the candidate's cell offset code (dx+2) + 5(dy+2) + 25(dz+2) relative to the query's cell at
+// build time (top 7 bits), which the FP32 form needs to form cell-relative differences.
+//
+// Cells are 2h wide (the reference's grid) and the list radius 2h (1 + skin) is larger, so a
+// query within 2h skin of a cell face can have candidates two cells away along that axis: the
+// search covers +-1 cells always and +-2 along an axis whenever the query's offset lies within
+// r_list - cs of the corresponding face.  Entries are in CartesianIndices order of the searched
+// cells (rows in (dz, dy) order, ascending slots within a row), so the pairs within 2h -- all in
+// the +-1 cells -- keep the PointNeighbors visiting order.
 #pragma once
 
+#include <climits>
+
 #include "tp_nhs.cuh"
-#include "tp_warpnbr.cuh"
 
 namespace tp {
 
 #define TP_ERRBIT_CAPACITY 4
 
+constexpr int kSlotBits = 25;  // slot field of a list entry: at most 2^25 particles per set
+constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;
+
 __device__ __forceinline__ void decode_cell_offset(unsigned e, int& dx, int& dy, int& dz) {
     const int code = (int)(e >> kSlotBits);
-    dx = code % 3 - 1;
-    dy = (code / 3) % 3 - 1;
-    dz = code / 9 - 1;
+    dx = code % 5 - 2;
+    dy = (code / 5) % 5 - 2;
+    dz = code / 25 - 2;
 }
+
+// Reach of the cell search of a query at offset o in its cell along one axis: 2 cells towards a
+// face closer than m = r_list - cs, else 1.
+__device__ __forceinline__ int reach_lo(float o, float m) { return o <= m ? 2 : 1; }
+__device__ __forceinline__ int reach_hi(float o, float cs, float m) { return o >= cs - m ? 2 : 1; }
 
 // o_a - o_b + (c_a - c_b) * cs from a list entry (same arithmetic as the list filter).
 template <int ND>
@@ -66,9 +81,13 @@ __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__
     if ((threadIdx.x & 31) == 0 && d > 0.0f) atomicMax(&gate[1], __float_as_uint(d));
 }
 
-// Same staging loop as warp_neighbors, but every hit goes straight into the lane's list column.
+// Warp-cooperative candidate search: lanes are grouped by their (cy, cz) row; for each searched
+// row the group's candidates form one contiguous slot range (cells are linearised x fastest),
+// which the warp streams through shared memory 32 test records at a time; every lane tests every
+// staged record against its own cell range and radius and appends hits to its list column.
+// m = r_list - cs (plus a rounding margin) decides where the search reaches two cells.
 template <int ND>
-__device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, bool active,
+__device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m, bool active,
                                             const int c[3], float4 oa,
                                             const int* __restrict__ start,
                                             const float4* __restrict__ test, float r2f,
@@ -77,6 +96,9 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, bool ac
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int cnt = 0;
+    const int xl = reach_lo(oa.x, m), xh = reach_hi(oa.x, cs, m);
+    const int yl = reach_lo(oa.y, m), yh = reach_hi(oa.y, cs, m);
+    const int zl = (ND == 3) ? reach_lo(oa.z, m) : 0, zh = (ND == 3) ? reach_hi(oa.z, cs, m) : 0;
     const int yz = active ? (c[1] + g.n[1] * c[2]) : -1;
     unsigned todo = __ballot_sync(FULL, active);
     while (todo) {
@@ -85,25 +107,31 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, bool ac
         const bool ing = active && (yz == yz0);
         const unsigned grp = __ballot_sync(FULL, ing);
         todo &= ~grp;
-        const int cxmin = __reduce_min_sync(FULL, ing ? c[0] : INT_MAX);
-        const int cxmax = __reduce_max_sync(FULL, ing ? c[0] : INT_MIN);
         const int cy = yz0 % g.n[1], cz = yz0 / g.n[1];
         const float cxa = (float)c[0];
-        const int zlo = (ND == 3) ? -1 : 0, zhi = (ND == 3) ? 1 : 0;
-        for (int dz = zlo; dz <= zhi; ++dz) {
-            for (int dy = -1; dy <= 1; ++dy) {
+        const int zr = (ND == 3) ? 2 : 0;
+        for (int dz = -zr; dz <= zr; ++dz) {
+            if (cz + dz < 0 || cz + dz >= g.n[2]) continue;
+            for (int dy = -2; dy <= 2; ++dy) {
+                if (cy + dy < 0 || cy + dy >= g.n[1]) continue;
+                const bool need = ing && dy >= -yl && dy <= yh && dz >= -zl && dz <= zh;
+                if (!__ballot_sync(FULL, need)) continue;
+                const int xa = need ? max(c[0] - xl, 0) : INT_MAX;
+                const int xb = need ? min(c[0] + xh, g.n[0] - 1) : INT_MIN;
+                const int gxa = __reduce_min_sync(FULL, xa);
+                const int gxb = __reduce_max_sync(FULL, xb);
                 const int rb = g.n[0] * ((cy + dy) + g.n[1] * (cz + dz));
-                const int lo = start[rb + cxmin - 1];
-                const int hi = start[rb + cxmax + 2];
+                const int lo = start[rb + gxa];
+                const int hi = start[rb + gxb + 1];
                 if (lo >= hi) continue;
                 int mlo = 0, mhi = 0;
-                if (ing) {
-                    mlo = start[rb + c[0] - 1];
-                    mhi = start[rb + c[0] + 2];
+                if (need) {
+                    mlo = start[rb + xa];
+                    mhi = start[rb + xb + 1];
                 }
                 const float sy = fmaf(-(float)dy, cs, oa.y);
                 const float sz = fmaf(-(float)dz, cs, oa.z);
-                const unsigned rowcode = (unsigned)(3 * (dy + 1) + 9 * (dz + 1));
+                const unsigned rowcode = 5u * (unsigned)(dy + 2) + 25u * (unsigned)(dz + 2);
                 for (int base = lo; base < hi; base += 32) {
                     const int j = base + lane;
                     if (j < hi) cand[lane] = test[j];
@@ -120,7 +148,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, bool ac
                             d2 = fmaf(pdz, pdz, d2);
                         }
                         if (jj >= mlo && jj < mhi && d2 <= r2f) {
-                            const unsigned code = rowcode + (unsigned)((int)(cb.w - cxa) + 1);
+                            const unsigned code = rowcode + (unsigned)((int)(cb.w - cxa) + 2);
                             if (cnt < cap) list[(size_t)cnt * stride + s] = (unsigned)jj | (code << kSlotBits);
                             ++cnt;
                         }
@@ -136,7 +164,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, bool ac
 // Fluid slots: fluid-fluid and fluid-wall lists.
 template <int ND>
 __global__ void __launch_bounds__(128) k_build_fluid_lists(
-    GridDesc g, float cs, float r2f, int nf, const float4* __restrict__ ftest,
+    GridDesc g, float cs, float m, float r2f, int nf, const float4* __restrict__ ftest,
     const int* __restrict__ fskey, const int* __restrict__ fstart,
     const float4* __restrict__ wtest, const int* __restrict__ wstart, unsigned* __restrict__ ff,
     int* __restrict__ ffc, int cap_ff, unsigned* __restrict__ fw, int* __restrict__ fwc,
@@ -150,9 +178,9 @@ __global__ void __launch_bounds__(128) k_build_fluid_lists(
     const float4 ta = ftest[si];
     int c[3];
     key_to_coords(fskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, active, c, ta, fstart, ftest, r2f, cand, ff, nf,
+    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, ff, nf,
                                     cap_ff, s);
-    const int n2 = warp_collect<ND>(g, cs, active, c, ta, wstart, wtest, r2f, cand, fw, nf,
+    const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wtest, r2f, cand, fw, nf,
                                     cap_fw, s);
     if (!active) return;
     ffc[s] = min(n1, cap_ff);
@@ -163,7 +191,7 @@ __global__ void __launch_bounds__(128) k_build_fluid_lists(
 // Wall slots: wall-fluid lists (the Adami gather).
 template <int ND>
 __global__ void __launch_bounds__(128) k_build_wall_lists(
-    GridDesc g, float cs, float r2f, int nw, const float4* __restrict__ wtest,
+    GridDesc g, float cs, float m, float r2f, int nw, const float4* __restrict__ wtest,
     const int* __restrict__ wskey, const float4* __restrict__ ftest,
     const int* __restrict__ fstart, unsigned* __restrict__ wf, int* __restrict__ wfc, int cap_wf,
     int* __restrict__ err, const unsigned* __restrict__ gate) {
@@ -176,7 +204,7 @@ __global__ void __launch_bounds__(128) k_build_wall_lists(
     const float4 ta = wtest[si];
     int c[3];
     key_to_coords(wskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, active, c, ta, fstart, ftest, r2f, cand, wf, nw,
+    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, wf, nw,
                                     cap_wf, s);
     if (!active) return;
     wfc[s] = min(n1, cap_wf);
