@@ -47,8 +47,7 @@ def test_pair_two_cells_apart_is_not_missed(lib, pkg, orc, cuda, precision):
     v_ref, u_ref, st = model.integrate(v0, u0, dt, n)
     assert st == 0
     v_ref = v_ref.reshape(-1, 3)
-    free = v0.copy()
-    assert not np.allclose(v_ref[:, 0], free[:, 0])  # the pair did interact
+    assert np.all(np.abs(v_ref[:, 2] - 1000.0) > 1e-3)  # the pair did interact (rho rose)
 
     h = ctypes.c_void_p()
     assert lib.tp_create(ctypes.byref(c), ctypes.byref(h)) == 0
