@@ -346,6 +346,7 @@ void setup_phys(tp_handle* h) {
     P.half_hinv = 0.5 * P.h_inv;
     P.alpha_c = P.alpha * P.c;
     P.visc_k = P.alpha_c * P.visc_h;
+    P.visc_k2 = 2.0 * P.visc_k;
     P.diff2 = 2.0 * P.diff_coef;
 
     Phys32& Q = h->phys32;

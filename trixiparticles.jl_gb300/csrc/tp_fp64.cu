@@ -60,7 +60,7 @@ struct Pack64 {
     float4* test;    // offsets against the reference cell (the cell of the last rebuild)
     double4_32a* pos;
     double4_32a* vel;
-    double4_32a* aux;  // {m, m / rho, 1 / rho, 0} with 1 / rho = fast_inv(rho)
+    double4_32a* aux;  // {m, m / rho, 1 / rho, 2 m alpha c h} with 1 / rho = fast_inv(rho)
     GridDesc g;
     double cs32;
     Phys P;
@@ -77,7 +77,7 @@ struct Pack64 {
         pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
         vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
         const double ir = fast_inv(rho);
-        aux[s] = make_double4_32a(mi, mi * ir, ir, 0.0);
+        aux[s] = make_double4_32a(mi, mi * ir, ir, mi * P.visc_k2);
         if (rebuild && xb_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
@@ -147,24 +147,22 @@ __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_3
         const double4_32a xb = fpos[b];
         const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
         const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
-        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);
+        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);  // exact support test, as the CPU
         if (d2 > P.sr2) continue;
-        const double r = sqrt(d2);
+        const double r = d2 > 0.0 ? d2 * rsqrt(d2) : 0.0;
         const double rho_f = fvel[b].w;
-        double hp = __dadd_rn(__dmul_rn(P.g[0], __dmul_rn(rho_f, pd0)),
-                              __dmul_rn(P.g[1], __dmul_rn(rho_f, pd1)));
-        if (ND == 3) hp = __dadd_rn(hp, __dmul_rn(P.g[2], __dmul_rn(rho_f, pd2)));
-        const double sum = __dadd_rn(__dadd_rn(__dadd_rn(P.p_off, xb.w), 0.0), hp);
+        double hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
+        if (ND == 3) hp += P.g[2] * (rho_f * pd2);
+        const double sum = (P.p_off + xb.w) + hp;
         double W = 0.0;
         if (r < P.two_h) {
-            const double q = __dmul_rn(r, P.h_inv);
-            const double t = 1.0 - q / 2.0;
-            const double t2 = __dmul_rn(t, t);
-            W = __dmul_rn(__dmul_rn(P.wc2_norm, __dmul_rn(t2, t2)),
-                          __dadd_rn(__dmul_rn(2.0, q), 1.0));
+            const double q = r * P.h_inv;
+            const double t = fma(-0.5, q, 1.0);
+            const double t2 = t * t;
+            W = (P.wc2_norm * (t2 * t2)) * fma(2.0, q, 1.0);
         }
-        Ps = __dadd_rn(Ps, __dmul_rn(sum, W));
-        V = __dadd_rn(V, W);
+        Ps = fma(sum, W, Ps);
+        V += W;
     }
     if (V > 2.220446049250313e-16) Ps = Ps / V;
     if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
@@ -229,7 +227,8 @@ __device__ __forceinline__ void stage_update(int s, const double4_32a& pa, const
 // candidates that lie in the skin shell from the FP64 pair loop is worth an extra pass.
 template <int ND>
 __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float cs, float lo2,
-                                           float hi2, double sr2, const double4_32a& pa,
+                                           float hi2, float zero2, double sr2, double az2,
+                                           const double4_32a& pa,
                                            const float4* __restrict__ test,
                                            const double4_32a* __restrict__ pos,
                                            const unsigned* __restrict__ list,
@@ -247,9 +246,12 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
         float p0, p1, p2;
         const float d2f = pair_diff<ND>(ta, cs, e, test[b], p0, p1, p2);
         bool acc = d2f <= lo2;
-        if (!acc && d2f <= hi2) {
+        if ((!acc && d2f <= hi2) || (acc && d2f < zero2)) {
+            // decided in FP64: the support bound, and the zero-distance skip of rhs.jl:27-28
+            // (distance < sqrt(eps((2h)^2)), tested as d^2 < eps((2h)^2)) for near-coincident pairs
             const double4_32a pb = pos[b];
-            acc = dist2_rn<ND>(pa.x - pb.x, pa.y - pb.y, ND == 3 ? pa.z - pb.z : 0.0) <= sr2;
+            const double d2 = dist2_rn<ND>(pa.x - pb.x, pa.y - pb.y, ND == 3 ? pa.z - pb.z : 0.0);
+            acc = d2 <= sr2 && !(d2 < az2);
         }
         if (acc) out[(size_t)(n++) * n_rows + s] = b;
     }
@@ -258,7 +260,8 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
 
 template <int ND>
 __global__ void __launch_bounds__(256) k_filter64(
-    double sr2, float cs, float lo2, float hi2, int nf, const float4* __restrict__ ftest,
+    double sr2, double az2, float cs, float lo2, float hi2, float zero2, int nf,
+    const float4* __restrict__ ftest,
     const double4_32a* __restrict__ fpos, const unsigned* __restrict__ ff,
     const int* __restrict__ ffc, const unsigned* __restrict__ fw, const int* __restrict__ fwc,
     const float4* __restrict__ wtest, const double4_32a* __restrict__ wpos, int* __restrict__ eff,
@@ -267,9 +270,10 @@ __global__ void __launch_bounds__(256) k_filter64(
     if (s >= nf) return;
     const float4 ta = ftest[s];
     const double4_32a pa = fpos[s];
-    effc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, ftest, fpos, ff, ffc[s],
-                              half ? 2 : 1, eff);
-    efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, sr2, pa, wtest, wpos, fw, fwc[s], 0, efw);
+    effc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, zero2, sr2, az2, pa, ftest, fpos, ff,
+                              ffc[s], half ? 2 : 1, eff);
+    efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, zero2, sr2, az2, pa, wtest, wpos, fw,
+                              fwc[s], 0, efw);
 }
 
 // Pair terms of rhs.jl:81-117 (pressure, Monaghan viscosity, continuity, Molteni-Colagrossi
@@ -283,15 +287,15 @@ __global__ void __launch_bounds__(256) k_filter64(
 //   r = d^2 rsqrt(d^2); the zero-distance skip `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28)
 //   tested as d^2 < eps((2h)^2).
 // Each term equals the reference's expression up to a few ulp of rounding.
-__device__ __forceinline__ double monaghan_coef(const Phys& P, double m_b, double vr, double d2,
-                                                double rho_a, double rho_b) {
-    // m_b (alpha c mu + beta mu^2) / rho_mean, mu = h vr / (r^2 + eps h^2)   (vr < 0)
+__device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a& ab, double vr,
+                                                double d2, double rho_sum) {
+    // m_b (alpha c mu + beta mu^2) / rho_mean, mu = h vr / (r^2 + eps h^2), rho_mean = rho_sum / 2
+    // (vr < 0); ab.w = 2 m_b alpha c h
     const double den = d2 + P.visc_eps_h2;
-    const double rm = 0.5 * (rho_a + rho_b);
-    const double R = fast_inv(den * rm);
-    if (P.beta == 0.0) return (m_b * P.visc_k) * vr * R;
-    const double mu = (P.visc_h * vr) * (rm * R);
-    return (m_b * mu) * (P.alpha_c + P.beta * mu) * (den * R);
+    const double R = fast_inv(den * rho_sum);
+    if (P.beta == 0.0) return ab.w * vr * R;
+    const double mu = (P.visc_h * vr) * (rho_sum * R);
+    return (ab.x * mu) * (P.alpha_c + P.beta * mu) * (2.0 * den * R);
 }
 
 template <int ND, bool INTEGRATE>
@@ -323,24 +327,24 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        if (d2 < P.az2) continue;
-        const double r = d2 * rsqrt(d2);
+        const double r = d2 * rsqrt(d2);  // d2 >= eps((2h)^2): the filter dropped closer pairs
         const double t = fma(-r, P.half_hinv, 1.0);
         const double sg = P.sg_c * ((t * t) * t);
         const double4_32a vb = fvel[b];
-        const double4_32a ab = faux[b];  // {m_b, m_b / rho_b, 1 / rho_b, 0}
+        const double4_32a ab = faux[b];  // {m_b, m_b / rho_b, 1 / rho_b, 2 m_b alpha c h}
         const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
         const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
         double vr = vd0 * pd0 + vd1 * pd1;
         if (ND == 3) vr += vd2 * pd2;
         double c = -(ab.y * ia) * (p_a + pb.w);
-        if (P.visc && vr < 0.0) c += monaghan_coef(P, ab.x, vr, d2, rho_a, vb.w);
+        if (P.visc && vr < 0.0) c += monaghan_coef(P, ab, vr, d2, rho_a + vb.w);
         c *= sg;
         dv0 += c * pd0;
         dv1 += c * pd1;
         if (ND == 3) dv2 += c * pd2;
-        drho += (rho_a * ab.y) * (sg * vr);
-        if (P.diff) drho += (ab.y * (rho_a - vb.w)) * (sg * P.diff2);
+        // continuity (rho_a / rho_b) m_b v_ab . grad W  +  diffusion m_b / rho_b psi . grad W
+        const double dd = P.diff ? P.diff2 * (rho_a - vb.w) : 0.0;
+        drho += (ab.y * sg) * fma(rho_a, vr, dd);
     }
 
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion, wall velocity 0) ----
@@ -353,7 +357,6 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        if (d2 < P.az2) continue;
         const double r = d2 * rsqrt(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
         const double sg = P.sg_c * ((t * t) * t);
@@ -416,7 +419,6 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        if (d2 < P.az2) continue;
         const double r = d2 * rsqrt(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
         const double sg = P.sg_c * ((t * t) * t);
@@ -474,7 +476,6 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        if (d2 < P.az2) continue;
         const double r = d2 * rsqrt(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
         const double sg = P.sg_c * ((t * t) * t);
@@ -635,7 +636,8 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     const double sr2 = h->phys.sr2;
     const bool sym = h->pair_mode == TP_PAIR_SYMMETRIC;
     k_filter64<ND><<<nblk(nf, 256), 256, 0, h->stream>>>(
-        sr2, (float)h->grid.cs, (float)(sr2 * (1.0 - 1e-5)), (float)(sr2 * (1.0 + 1e-5)), nf,
+        sr2, h->phys.az2, (float)h->grid.cs, (float)(sr2 * (1.0 - 1e-5)),
+        (float)(sr2 * (1.0 + 1e-5)), (float)(sr2 * 1e-6), nf,
         h->f_test, (const double4_32a*)h->f_pos, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test,
         (const double4_32a*)h->w_pos, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw, sym ? 1 : 0);
     if (sym) {

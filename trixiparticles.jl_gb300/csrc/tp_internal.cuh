@@ -63,6 +63,7 @@ struct Phys {
     double sg_c;       // wc2_dnorm * hi2: grad W = sg_c (1 - q/2)^3 x_ab
     double half_hinv;  // 0.5 * h_inv: 1 - q/2 = 1 - r * half_hinv
     double visc_k;     // alpha * c * visc_h (Monaghan with beta = 0)
+    double visc_k2;    // 2 * visc_k (per-particle 2 m alpha c h of the pack)
     double alpha_c;    // alpha * c
     double diff2;      // 2 * diff_coef
 };
