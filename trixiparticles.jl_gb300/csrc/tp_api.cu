@@ -152,9 +152,9 @@ __global__ void k_spv_finish(double* __restrict__ v, double* __restrict__ u,
     for (int d = 0; d < ND; ++d) u[(size_t)a * ND + d] = fma(dth, va[d], uh[(size_t)a * ND + d]);
 }
 
-__global__ void k_gate_init(unsigned* __restrict__ gate, float threshold) {
+__global__ void k_gate_init(unsigned* __restrict__ gate, float threshold, int force) {
     if (threadIdx.x == 0) {
-        gate[0] = 1u;
+        gate[0] = force ? 1u : 0u;
         gate[1] = 0u;
         gate[2] = __float_as_uint(threshold);
     }
@@ -420,6 +420,7 @@ bool setup_grid(tp_handle* h, std::string& msg) {
 tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start,
                          const unsigned* gate = nullptr, int* maxcell = nullptr,
                          bool lex = false) {
+    if (!gate) h->kick_valid = false;  // an unconditional sort replaces the kick! path's lists
     if (n > 0) {
         if (lex) {
             if (h->cfg.ndims == 2)
@@ -499,6 +500,7 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
     const int cwf = cff;
     auto grow = [&](unsigned** buf, int* cap, int want, int n) -> cudaError_t {
         if (*cap >= want && *buf) return cudaSuccess;
+        h->kick_valid = false;  // the lists are re-allocated and must be rebuilt
         if (*buf) cudaFree(*buf);
         *buf = nullptr;
         *cap = 0;
@@ -615,6 +617,7 @@ tp_status ensure_state(tp_handle* h) {
 // One RHS evaluation of the cell-sorted pipeline from caller-ordered device arrays:
 // sort + pack, exact lists (no skin), Adami.  The pair pass follows in the caller.
 tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
+    h->kick_valid = false;  // builds exact-radius lists, which the kick! path cannot reuse
     const int nf = (int)h->cfg.n_fluid;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
     tp_status st = h->lists_fixed ? TP_OK : ensure_lists(h, u);
@@ -631,6 +634,54 @@ tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
     h->launches += (nf > 0);
     st = build_lists(h, 0.0, nullptr);
     if (st != TP_OK) return st;
+    mark(h, 1);
+    if (f32)
+        fp32_adami(h);
+    else
+        fp64_adami(h);
+    TP_LAUNCHED(h, "adami");
+    h->launches += (h->cfg.n_wall > 0);
+    mark(h, 2);
+    return TP_OK;
+}
+
+// The kick! path: the state comes in caller order every call.  Between list rebuilds the slot
+// records are refreshed in place from the caller arrays through the permutation of the last
+// rebuild and the skin lists are reused; a rebuild (cell sort, stable rank, lists at radius
+// 2h (1 + skin)) happens on the device when some particle has moved more than skin * h since
+// the last one, or when anything else replaced this handle's cell list.  Pairs are decided
+// exactly at every call, so the result equals a fresh neighbour search.
+tp_status rhs_kick(tp_handle* h, const double* u, const double* v) {
+    const int nf = (int)h->cfg.n_fluid;
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    tp_status st = h->lists_fixed ? TP_OK : ensure_lists(h, u);
+    if (st != TP_OK) return st;
+    if (!h->x_build) TP_CUDA(h, dalloc(&h->x_build, (size_t)std::max(nf, 1) * h->cfg.ndims));
+    const bool force = !h->kick_valid;
+    mark(h, 0);
+    k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length),
+                                         force ? 1 : 0);
+    h->launches += 1;
+    if (!force && nf > 0) {
+        if (h->cfg.ndims == 2)
+            k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(u, h->x_build, nf, h->gate,
+                                                                     h->f_perm);
+        else
+            k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(u, h->x_build, nf, h->gate,
+                                                                     h->f_perm);
+        h->launches += 1;
+    }
+    st = sort_particles(h, u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);
+    if (st != TP_OK) return st;
+    if (f32)
+        fp32_pack(h, u, v, h->m_f, nullptr, nullptr, h->gate);
+    else if (nf > 0)
+        fp64_pack(h, u, v, h->m_f, nullptr, nullptr, h->gate);
+    TP_LAUNCHED(h, "kick pack");
+    h->launches += (nf > 0);
+    st = build_lists(h, h->skin, h->gate);
+    if (st != TP_OK) return st;
+    h->kick_valid = true;
     mark(h, 1);
     if (f32)
         fp32_adami(h);
@@ -863,7 +914,7 @@ tp_status tp_kick(tp_handle* h, double* dv_ode, const double* v_ode, const doubl
     if (nf > 0 && (dv_ode == v_ode || (const double*)dv_ode == u_ode))
         return fail(h, TP_ERR_ARGUMENT, "tp_kick: dv_ode must not alias v_ode or u_ode");
     begin_timing(h);
-    st = rhs_from_caller(h, u_ode, v_ode);
+    st = rhs_kick(h, u_ode, v_ode);
     if (st != TP_OK) return st;
     if (h->cfg.precision == TP_PRECISION_FP32)
         fp32_pair_kick(h, dv_ode);
@@ -930,7 +981,7 @@ tp_status tp_integrate_spv(tp_handle* h, double* v_ode, double* u_ode, double t0
     double* uh = vh + nv;
     const double dth = dt * 0.5;
     auto kick = [&](const double* v, const double* u) -> tp_status {
-        tp_status s2 = rhs_from_caller(h, u, v);
+        tp_status s2 = rhs_kick(h, u, v);
         if (s2 != TP_OK) return s2;
         if (h->cfg.precision == TP_PRECISION_FP32)
             fp32_pair_kick(h, k);
@@ -1004,6 +1055,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     begin_timing(h);
 
     // Load the caller state into slot-ordered storage (identity order to begin with).
+    h->kick_valid = false;  // the integrator re-sorts its own slot-ordered state
     PhysState& s0 = h->st[h->cur];
     TP_CUDA(h, cudaMemcpyAsync(s0.u, u_ode, (size_t)nf * nd * sizeof(double),
                                cudaMemcpyDeviceToDevice, h->stream));
@@ -1033,7 +1085,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     }
     // Rebuild gate: force the first rebuild of this call; threshold = skin * h.  Written by a
     // kernel (not a host copy) so that a captured graph carries the values of capture time.
-    k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length));
+    k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length), 1);
     TP_LAUNCHED(h, "gate init");
     h->launches += 1;
 
@@ -1288,7 +1340,10 @@ tp_status tp_set_launch(tp_handle* h, int32_t pair_block) {
 tp_status tp_set_skin(tp_handle* h, double skin) {
     if (!h) return TP_ERR_ARGUMENT;
     if (!(skin >= 0.0 && skin <= 1.0)) return fail(h, TP_ERR_ARGUMENT, "skin must be in [0, 1]");
-    if (skin != h->skin) h->lists_fixed = false;  // capacities were sized for the old skin
+    if (skin != h->skin) {
+        h->lists_fixed = false;  // capacities were sized for the old skin
+        h->kick_valid = false;
+    }
     h->skin = skin;
     return TP_OK;
 }

@@ -59,10 +59,12 @@ struct Pack32 {
     float4* test;
     float4* vel;
     float4* aux;  // {p, m, m / rho, 1 / rho}
+    const int* src_perm;  // kick! path: without a rebuild, slot s packs caller particle perm[s]
     GridDesc g;
     double cs32, rho0;
     Phys32 P;
     __device__ void operator()(int i, int s, int key, bool rebuild) const {
+        if (!rebuild && src_perm) i = src_perm[s];
         double x[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
@@ -321,6 +323,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
             pk.id_out = dst->id;
             pk.m_out = (float*)dst->m;
         }
+        pk.src_perm = (!S32 && gate) ? h->f_perm : nullptr;
         pk.xb_out = h->x_build;
         pk.test = h->f_test;
         pk.vel = (float4*)h->f_vel;

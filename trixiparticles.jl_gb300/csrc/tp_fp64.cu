@@ -61,10 +61,12 @@ struct Pack64 {
     double4_32a* pos;
     double4_32a* vel;
     double4_32a* aux;  // {m, m / rho, 1 / rho, 2 m alpha c h} with 1 / rho = fast_inv(rho)
+    const int* src_perm;  // kick! path: without a rebuild, slot s packs caller particle perm[s]
     GridDesc g;
     double cs32;
     Phys P;
     __device__ void operator()(int i, int s, int key, bool rebuild) const {
+        if (!rebuild && src_perm) i = src_perm[s];
         double x[3] = {0, 0, 0}, w[4] = {0, 0, 0, 0};
 #pragma unroll
         for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
@@ -554,6 +556,7 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
     pk.u = u;
     pk.v = v;
     pk.m = m;
+    pk.src_perm = (!src && gate) ? h->f_perm : nullptr;
     if (src) {
         pk.tu = src->tu;
         pk.tv = (const double*)src->tv;

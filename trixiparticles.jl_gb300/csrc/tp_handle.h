@@ -98,6 +98,8 @@ struct tp_handle {
     int* d_max = nullptr;       // scratch for the largest cell occupancy
     int maxcell_w = 0;          // largest wall cell occupancy (walls are static)
     bool lists_fixed = false;   // capacity fixed by tp_prepare_lists (no sizing sync per call)
+    bool kick_valid = false;    // kick! path: cell list, slot records and skin lists belong to the
+                                // caller's ordering (refresh in place until a rebuild is due)
     int pair_block = 128;       // threads per block of the pair / Adami kernels (autotuned)
 
     // ---- integrator ping-pong state ----

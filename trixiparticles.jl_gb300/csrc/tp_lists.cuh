@@ -60,17 +60,20 @@ __device__ __forceinline__ float pair_diff(float4 ta, float cs, unsigned e, floa
 }
 
 // Largest displacement since the last rebuild -> gate[1] (float bits, atomicMax on unsigned).
+// `perm` (optional): slot -> index into u (caller-ordered positions of the kick! path).
 template <int ND>
 __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__ u,
                                                       const double* __restrict__ xb, int n,
-                                                      unsigned* __restrict__ gate) {
+                                                      unsigned* __restrict__ gate,
+                                                      const int* __restrict__ perm = nullptr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     float d = 0.0f;
     if (s < n) {
+        const int i = perm ? perm[s] : s;
         double d2 = 0.0;
 #pragma unroll
         for (int k = 0; k < ND; ++k) {
-            const double e = u[(size_t)s * ND + k] - xb[(size_t)s * ND + k];
+            const double e = u[(size_t)i * ND + k] - xb[(size_t)s * ND + k];
             d2 += e * e;
         }
         d = (float)sqrt(d2);
