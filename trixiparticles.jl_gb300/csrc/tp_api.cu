@@ -152,6 +152,30 @@ __global__ void k_spv_finish(double* __restrict__ v, double* __restrict__ u,
     for (int d = 0; d < ND; ++d) u[(size_t)a * ND + d] = fma(dth, va[d], uh[(size_t)a * ND + d]);
 }
 
+// Warm start of the integrator: slot s takes caller particle id[s] (the previous call's slot
+// order), so the lists of that call stay valid.
+template <int ND, bool F32>
+__global__ void k_gather_load(const int* __restrict__ id, const double* __restrict__ u,
+                              const double* __restrict__ v, const double* __restrict__ m,
+                              double rho0, double* __restrict__ su, void* __restrict__ sv,
+                              void* __restrict__ sm, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = id[s];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) su[(size_t)s * ND + d] = u[(size_t)i * ND + d];
+    const double* vv = v + (size_t)i * (ND + 1);
+    if (F32) {
+        ((float4*)sv)[s] = make_float4((float)vv[0], (float)vv[1], ND == 3 ? (float)vv[2] : 0.0f,
+                                       (float)(vv[ND] - rho0));
+        ((float*)sm)[s] = (float)m[i];
+    } else {
+#pragma unroll
+        for (int d = 0; d <= ND; ++d) ((double*)sv)[(size_t)s * (ND + 1) + d] = vv[d];
+        ((double*)sm)[s] = m[i];
+    }
+}
+
 __global__ void k_gate_init(unsigned* __restrict__ gate, float threshold, int force) {
     if (threadIdx.x == 0) {
         gate[0] = force ? 1u : 0u;
@@ -420,7 +444,7 @@ bool setup_grid(tp_handle* h, std::string& msg) {
 tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start,
                          const unsigned* gate = nullptr, int* maxcell = nullptr,
                          bool lex = false) {
-    if (!gate) h->kick_valid = false;  // an unconditional sort replaces the kick! path's lists
+    if (!gate) h->lists_owner = 0;  // an unconditional sort replaces the reusable lists
     if (n > 0) {
         if (lex) {
             if (h->cfg.ndims == 2)
@@ -500,7 +524,7 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
     const int cwf = cff;
     auto grow = [&](unsigned** buf, int* cap, int want, int n) -> cudaError_t {
         if (*cap >= want && *buf) return cudaSuccess;
-        h->kick_valid = false;  // the lists are re-allocated and must be rebuilt
+        h->lists_owner = 0;  // the lists are re-allocated and must be rebuilt
         if (*buf) cudaFree(*buf);
         *buf = nullptr;
         *cap = 0;
@@ -617,7 +641,7 @@ tp_status ensure_state(tp_handle* h) {
 // One RHS evaluation of the cell-sorted pipeline from caller-ordered device arrays:
 // sort + pack, exact lists (no skin), Adami.  The pair pass follows in the caller.
 tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
-    h->kick_valid = false;  // builds exact-radius lists, which the kick! path cannot reuse
+    h->lists_owner = 0;  // builds exact-radius lists, which no path can reuse
     const int nf = (int)h->cfg.n_fluid;
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
     tp_status st = h->lists_fixed ? TP_OK : ensure_lists(h, u);
@@ -657,7 +681,7 @@ tp_status rhs_kick(tp_handle* h, const double* u, const double* v) {
     tp_status st = h->lists_fixed ? TP_OK : ensure_lists(h, u);
     if (st != TP_OK) return st;
     if (!h->x_build) TP_CUDA(h, dalloc(&h->x_build, (size_t)std::max(nf, 1) * h->cfg.ndims));
-    const bool force = !h->kick_valid;
+    const bool force = h->lists_owner != 1;
     mark(h, 0);
     k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length),
                                          force ? 1 : 0);
@@ -681,7 +705,7 @@ tp_status rhs_kick(tp_handle* h, const double* u, const double* v) {
     h->launches += (nf > 0);
     st = build_lists(h, h->skin, h->gate);
     if (st != TP_OK) return st;
-    h->kick_valid = true;
+    h->lists_owner = 1;
     mark(h, 1);
     if (f32)
         fp32_adami(h);
@@ -1040,52 +1064,72 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
     if (nf == 0 || n_steps == 0) return TP_OK;
     if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: null array");
-    {
-        // Under stream capture nothing may synchronise or allocate: list capacities and the
-        // integrator state must have been set up by tp_prepare_lists, and timing must be off.
-        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-        TP_CUDA(h, cudaStreamIsCapturing(h->stream, &cap));
-        if (cap != cudaStreamCaptureStatusNone && (!h->lists_fixed || !h->st[0].u || h->timing))
-            return fail(h, TP_ERR_ARGUMENT,
-                        "tp_integrate_ck2n54: capturing needs tp_prepare_lists first and timing off");
-    }
+    // Under stream capture nothing may synchronise or allocate: list capacities and the
+    // integrator state must have been set up by tp_prepare_lists, and timing must be off.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    TP_CUDA(h, cudaStreamIsCapturing(h->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone && (!h->lists_fixed || !h->st[0].u || h->timing))
+        return fail(h, TP_ERR_ARGUMENT,
+                    "tp_integrate_ck2n54: capturing needs tp_prepare_lists first and timing off");
     st = ensure_state(h);
     if (st != TP_OK) return st;
-    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
-    begin_timing(h);
-
-    // Load the caller state into slot-ordered storage (identity order to begin with).
-    h->kick_valid = false;  // the integrator re-sorts its own slot-ordered state
-    PhysState& s0 = h->st[h->cur];
-    TP_CUDA(h, cudaMemcpyAsync(s0.u, u_ode, (size_t)nf * nd * sizeof(double),
-                               cudaMemcpyDeviceToDevice, h->stream));
-    if (f32) {
-        if (nd == 2)
-            k_load32<2><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, h->m_f,
-                                                              h->cfg.reference_density,
-                                                              (float4*)s0.v, (float*)s0.m, nf);
-        else
-            k_load32<3><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, h->m_f,
-                                                              h->cfg.reference_density,
-                                                              (float4*)s0.v, (float*)s0.m, nf);
-    } else {
-        TP_CUDA(h, cudaMemcpyAsync(s0.v, v_ode, (size_t)nf * (nd + 1) * sizeof(double),
-                                   cudaMemcpyDeviceToDevice, h->stream));
-        TP_CUDA(h, cudaMemcpyAsync(s0.m, h->m_f, (size_t)nf * sizeof(double),
-                                   cudaMemcpyDeviceToDevice, h->stream));
-    }
-    k_iota<<<nblk(nf, 256), 256, 0, h->stream>>>(s0.id, nf);
-    TP_LAUNCHED(h, "integrator load");
-    TP_DBG(h, "integrator load");
-    h->launches += f32 ? 2 : 1;
-
     if (!h->lists_fixed) {
         st = ensure_lists(h, u_ode);
         if (st != TP_OK) return st;
     }
-    // Rebuild gate: force the first rebuild of this call; threshold = skin * h.  Written by a
-    // kernel (not a host copy) so that a captured graph carries the values of capture time.
-    k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length), 1);
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    begin_timing(h);
+
+    // Load the caller state into slot-ordered storage.  Warm start: the lists still belong to
+    // the previous call of this integrator, so slot s takes caller particle id[s] of that call's
+    // final order and the displacement gate decides about a rebuild.  Cold start (or under
+    // capture, so that a graph does not depend on the history): identity order, forced rebuild.
+    const bool warm = h->lists_owner == 2 && cap == cudaStreamCaptureStatusNone;
+    h->lists_owner = 0;
+    PhysState& s0 = h->st[h->cur];
+    if (warm) {
+        auto load = [&](auto ndc, auto f32c) {
+            constexpr int ND = decltype(ndc)::value;
+            constexpr bool F32 = decltype(f32c)::value;
+            k_gather_load<ND, F32><<<nblk(nf, 256), 256, 0, h->stream>>>(
+                s0.id, u_ode, v_ode, h->m_f, h->cfg.reference_density, s0.u, s0.v, s0.m, nf);
+        };
+        if (nd == 2) {
+            if (f32) load(std::integral_constant<int, 2>{}, std::true_type{});
+            else load(std::integral_constant<int, 2>{}, std::false_type{});
+        } else {
+            if (f32) load(std::integral_constant<int, 3>{}, std::true_type{});
+            else load(std::integral_constant<int, 3>{}, std::false_type{});
+        }
+        h->launches += 1;
+    } else {
+        TP_CUDA(h, cudaMemcpyAsync(s0.u, u_ode, (size_t)nf * nd * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+        if (f32) {
+            if (nd == 2)
+                k_load32<2><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, h->m_f,
+                                                                  h->cfg.reference_density,
+                                                                  (float4*)s0.v, (float*)s0.m, nf);
+            else
+                k_load32<3><<<nblk(nf, 256), 256, 0, h->stream>>>(v_ode, h->m_f,
+                                                                  h->cfg.reference_density,
+                                                                  (float4*)s0.v, (float*)s0.m, nf);
+        } else {
+            TP_CUDA(h, cudaMemcpyAsync(s0.v, v_ode, (size_t)nf * (nd + 1) * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, h->stream));
+            TP_CUDA(h, cudaMemcpyAsync(s0.m, h->m_f, (size_t)nf * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, h->stream));
+        }
+        k_iota<<<nblk(nf, 256), 256, 0, h->stream>>>(s0.id, nf);
+        h->launches += f32 ? 2 : 1;
+    }
+    TP_LAUNCHED(h, "integrator load");
+    TP_DBG(h, "integrator load");
+
+    // Rebuild gate (threshold skin * h), forced on a cold start.  Written by a kernel (not a
+    // host copy) so that a captured graph carries the values of capture time.
+    k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length),
+                                         warm ? 0 : 1);
     TP_LAUNCHED(h, "gate init");
     h->launches += 1;
 
@@ -1156,6 +1200,8 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     TP_LAUNCHED(h, "integrator store");
     TP_DBG(h, "integrator store");
     h->launches += 1;
+    // a captured call has not run yet: the next eager call starts cold
+    h->lists_owner = cap == cudaStreamCaptureStatusNone ? 2 : 0;
     finish_timing(h);
     return TP_OK;
 }
@@ -1342,7 +1388,7 @@ tp_status tp_set_skin(tp_handle* h, double skin) {
     if (!(skin >= 0.0 && skin <= 1.0)) return fail(h, TP_ERR_ARGUMENT, "skin must be in [0, 1]");
     if (skin != h->skin) {
         h->lists_fixed = false;  // capacities were sized for the old skin
-        h->kick_valid = false;
+        h->lists_owner = 0;
     }
     h->skin = skin;
     return TP_OK;

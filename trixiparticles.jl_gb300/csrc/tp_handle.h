@@ -98,8 +98,11 @@ struct tp_handle {
     int* d_max = nullptr;       // scratch for the largest cell occupancy
     int maxcell_w = 0;          // largest wall cell occupancy (walls are static)
     bool lists_fixed = false;   // capacity fixed by tp_prepare_lists (no sizing sync per call)
-    bool kick_valid = false;    // kick! path: cell list, slot records and skin lists belong to the
-                                // caller's ordering (refresh in place until a rebuild is due)
+    // Which path the cell list, slot order and skin lists currently belong to: 0 none (next
+    // use rebuilds), 1 the kick! path (slots map to caller indices through f_perm), 2 the fused
+    // integrator (slots map to caller indices through its state's id array).  The owner reuses
+    // them across calls until a particle has moved more than skin * h.
+    int lists_owner = 0;
     int pair_block = 128;       // threads per block of the pair / Adami kernels (autotuned)
 
     // ---- integrator ping-pong state ----
