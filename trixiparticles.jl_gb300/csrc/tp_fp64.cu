@@ -240,13 +240,12 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
     // higher one when it is even; measured on GB300 this balances the lanes better than a hashed
     // owner, whose scattered accesses cost more than its balance gains)
     int n = 0;
-    for (int k = 0; k < cnt; ++k) {
-        const unsigned e = list[(size_t)k * n_rows + s];
+    auto test_one = [&](unsigned e, const float4& cb) {
         const int b = (int)(e & kSlotMask);
-        if (b == s && skip != 0) continue;
-        if (skip == 2 && ((b > s) != (((s ^ b) & 1) != 0))) continue;
+        if (b == s && skip != 0) return;
+        if (skip == 2 && ((b > s) != (((s ^ b) & 1) != 0))) return;
         float p0, p1, p2;
-        const float d2f = pair_diff<ND>(ta, cs, e, test[b], p0, p1, p2);
+        const float d2f = pair_diff<ND>(ta, cs, e, cb, p0, p1, p2);
         bool acc = d2f <= lo2;
         if ((!acc && d2f <= hi2) || (acc && d2f < zero2)) {
             // decided in FP64: the support bound, and the zero-distance skip of rhs.jl:27-28
@@ -256,6 +255,23 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
             acc = d2 <= sr2 && !(d2 < az2);
         }
         if (acc) out[(size_t)(n++) * n_rows + s] = b;
+    };
+    // four candidates' entries and records in flight at a time (the pass is gather-latency
+    // bound); tested in list order
+    int k = 0;
+    for (; k + 4 <= cnt; k += 4) {
+        unsigned e[4];
+        float4 cb[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) e[j] = list[(size_t)(k + j) * n_rows + s];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cb[j] = test[e[j] & kSlotMask];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) test_one(e[j], cb[j]);
+    }
+    for (; k < cnt; ++k) {
+        const unsigned e = list[(size_t)k * n_rows + s];
+        test_one(e, test[e & kSlotMask]);
     }
     return n;
 }
