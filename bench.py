@@ -38,7 +38,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = "particle-steps/s (3D WCSPH) FP32 vs FP64 at stated error; % of HBM roofline"
 UNIT = "particle-steps/s"
 
-# SURVEY-derived algorithmic byte model (compulsory unique bytes per RHS stage, 3D).
+# Algorithmic byte model: compulsory unique bytes per RHS stage in 3D, every array touched once
+# per pass (neighbour re-reads assumed on chip).  FP64 per fluid particle: NHS 32 (x read, key and
+# permutation written) + Adami-side read of x, rho 32 + pair 64 (x, v, rho, m) + fused 2N update
+# 224 (7 scalars, state and register read and written); per wall particle: Adami 40 + pair-side
+# read 48.  FP32 form: 32 + 20 + 36 + 160 per fluid, 56 per wall.
 BYTES_STAGE = {"float64": (352, 88), "float32": (248, 56)}   # (per fluid, per wall)
 BYTES_PAIR = {"float64": (288, 48), "float32": (196, 24)}    # pair kernel + fused update share
 
