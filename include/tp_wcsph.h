@@ -155,7 +155,11 @@ tp_status tp_drift(tp_handle* h, double* du_ode, const double* v_ode, const doub
 tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double t0,
                               double dt, int64_t n_steps);
 
-/* Fluid pressure (n_fluid) from the last kick, in caller order (system.jl:426-438). */
+/* Fluid pressure (n_fluid) of the last right-hand side evaluation, in caller order
+ * (system.jl:426-438): the last tp_kick, or the last stage of the last step of
+ * tp_integrate_ck2n54 / tp_integrate_spv, as the reference's pressure cache holds after solve.
+ * TP_ERR_NOT_READY when an unconditional reordering (tp_sort_particles, tp_interpolate_points
+ * without walls, tp_nhs_debug, the adjoint) came after it. */
 tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid);
 
 /* Wall pressure, density and kernel volume sum (n_wall each, caller order) from the last

@@ -48,6 +48,9 @@ static int run(int nd, int precision) {
     bad |= tp_wall_state(h, pw.data(), nullptr, nullptr) != TP_OK;
     bad |= tp_nhs_debug(h, u.data(), cell.data(), order.data(), nff.data(), nfw.data(),
                         nwf.data()) != TP_OK;
+    bad |= tp_fluid_pressure(h, pf.data()) != TP_ERR_NOT_READY;  // reordered since the kick
+    bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 1) != TP_OK;
+    bad |= tp_fluid_pressure(h, pf.data()) != TP_OK;
     double cons[5];
     bad |= tp_conservation(h, v.data(), cons) != TP_OK;
     double ms[8];

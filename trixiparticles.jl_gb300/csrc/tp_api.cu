@@ -444,7 +444,10 @@ bool setup_grid(tp_handle* h, std::string& msg) {
 tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tmp, int* start,
                          const unsigned* gate = nullptr, int* maxcell = nullptr,
                          bool lex = false) {
-    if (!gate) h->lists_owner = 0;  // an unconditional sort replaces the reusable lists
+    if (!gate) {
+        h->lists_owner = 0;  // an unconditional sort replaces the reusable lists
+        h->records_order = 0;
+    }
     if (n > 0) {
         if (lex) {
             if (h->cfg.ndims == 2)
@@ -658,6 +661,7 @@ tp_status rhs_from_caller(tp_handle* h, const double* u, const double* v) {
     h->launches += (nf > 0);
     st = build_lists(h, 0.0, nullptr);
     if (st != TP_OK) return st;
+    h->records_order = 1;
     mark(h, 1);
     if (f32)
         fp32_adami(h);
@@ -682,6 +686,7 @@ tp_status rhs_kick(tp_handle* h, const double* u, const double* v) {
     if (st != TP_OK) return st;
     if (!h->x_build) TP_CUDA(h, dalloc(&h->x_build, (size_t)std::max(nf, 1) * h->cfg.ndims));
     const bool force = h->lists_owner != 1;
+    h->records_order = 0;
     mark(h, 0);
     k_gate_init<<<1, 32, 0, h->stream>>>(h->gate, (float)(h->skin * h->cfg.smoothing_length),
                                          force ? 1 : 0);
@@ -706,6 +711,7 @@ tp_status rhs_kick(tp_handle* h, const double* u, const double* v) {
     st = build_lists(h, h->skin, h->gate);
     if (st != TP_OK) return st;
     h->lists_owner = 1;
+    h->records_order = 1;
     mark(h, 1);
     if (f32)
         fp32_adami(h);
@@ -1086,6 +1092,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     // capture, so that a graph does not depend on the history): identity order, forced rebuild.
     const bool warm = h->lists_owner == 2 && cap == cudaStreamCaptureStatusNone;
     h->lists_owner = 0;
+    h->records_order = 0;
     PhysState& s0 = h->st[h->cur];
     if (warm) {
         auto load = [&](auto ndc, auto f32c) {
@@ -1202,6 +1209,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     h->launches += 1;
     // a captured call has not run yet: the next eager call starts cold
     h->lists_owner = cap == cudaStreamCaptureStatusNone ? 2 : 0;
+    h->records_order = 2;  // records of the last stage, in the order of the final state
     finish_timing(h);
     return TP_OK;
 }
@@ -1211,12 +1219,17 @@ tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid) {
     const int nf = (int)h->cfg.n_fluid;
     if (nf == 0) return TP_OK;
     if (!p_fluid) return fail(h, TP_ERR_ARGUMENT, "tp_fluid_pressure: null array");
+    if (h->records_order == 0)
+        return fail(h, TP_ERR_NOT_READY,
+                    "tp_fluid_pressure: no right-hand side since the particles were last "
+                    "reordered (sort, interpolation, adjoint); call tp_kick first");
+    const int* ids = h->records_order == 2 ? h->st[h->cur].id : h->f_perm;
     if (h->cfg.precision == TP_PRECISION_FP32)
-        k_scatter_pressure<true><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_aux, h->f_perm,
-                                                                        p_fluid, nf);
+        k_scatter_pressure<true><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_aux, ids, p_fluid,
+                                                                        nf);
     else
-        k_scatter_pressure<false><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, h->f_perm,
-                                                                         p_fluid, nf);
+        k_scatter_pressure<false><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, ids, p_fluid,
+                                                                         nf);
     TP_LAUNCHED(h, "fluid pressure");
     return TP_OK;
 }

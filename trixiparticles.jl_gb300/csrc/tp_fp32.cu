@@ -119,6 +119,8 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4*
                                                  const float4* __restrict__ ftest,
                                                  const float4* __restrict__ fvel,
                                                  const float4* __restrict__ faux) {
+    __shared__ float4 off[kOffsetCodes];
+    fill_offset_table(off, P.cs);
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const float4 tw = wtest[w];
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4*
         const unsigned e = wf[(size_t)k * nw + w];
         const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(tw, P.cs, e, ftest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(tw, off, e, ftest[b], pd0, pd1, pd2);
         if (d2 > P.sr2) continue;
         const float r = sqrtf(d2);
         const float rho_f = P.rho0 + fvel[b].w;
@@ -187,6 +189,8 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
                                                 const float4* __restrict__ wtest,
                                                 const float4* __restrict__ wstate,
                                                 unsigned* __restrict__ gate, Update32 U) {
+    __shared__ float4 off[kOffsetCodes];
+    fill_offset_table(off, P.cs);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
         const unsigned e = ff[(size_t)k * nf + s];
         const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, P.cs, e, ftest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(ta, off, e, ftest[b], pd0, pd1, pd2);
         if (d2 > P.sr2 || d2 < P.az2) continue;
         const float r = d2 * rsqrtf(d2);
         const float4 vb = fvel[b];
@@ -241,7 +245,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
         const unsigned e = fw[(size_t)k * nf + s];
         const int b = (int)(e & kSlotMask);
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, P.cs, e, wtest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(ta, off, e, wtest[b], pd0, pd1, pd2);
         if (d2 > P.sr2 || d2 < P.az2) continue;
         const float r = d2 * rsqrtf(d2);
         const float4 sb = wstate[b];  // {p, rho - rho0, m, m / rho}

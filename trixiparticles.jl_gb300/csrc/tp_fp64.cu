@@ -228,7 +228,7 @@ __device__ __forceinline__ void stage_update(int s, const double4_32a& pa, const
 // arithmetic runs at 1/64 of the FP32 rate on this GPU, so removing the ~25 % of listed
 // candidates that lie in the skin shell from the FP64 pair loop is worth an extra pass.
 template <int ND>
-__device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float cs, float lo2,
+__device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const float4* off, float lo2,
                                            float hi2, float zero2, double sr2, double az2,
                                            const double4_32a& pa,
                                            const float4* __restrict__ test,
@@ -245,7 +245,7 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, float c
         if (b == s && skip != 0) return;
         if (skip == 2 && ((b > s) != (((s ^ b) & 1) != 0))) return;
         float p0, p1, p2;
-        const float d2f = pair_diff<ND>(ta, cs, e, cb, p0, p1, p2);
+        const float d2f = pair_diff<ND>(ta, off, e, cb, p0, p1, p2);
         bool acc = d2f <= lo2;
         if ((!acc && d2f <= hi2) || (acc && d2f < zero2)) {
             // decided in FP64: the support bound, and the zero-distance skip of rhs.jl:27-28
@@ -284,13 +284,15 @@ __global__ void __launch_bounds__(256) k_filter64(
     const int* __restrict__ ffc, const unsigned* __restrict__ fw, const int* __restrict__ fwc,
     const float4* __restrict__ wtest, const double4_32a* __restrict__ wpos, int* __restrict__ eff,
     int* __restrict__ effc, int* __restrict__ efw, int* __restrict__ efwc, int half) {
+    __shared__ float4 off[kOffsetCodes];
+    fill_offset_table(off, cs);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nf) return;
     const float4 ta = ftest[s];
     const double4_32a pa = fpos[s];
-    effc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, zero2, sr2, az2, pa, ftest, fpos, ff,
+    effc[s] = filter_list<ND>(s, nf, ta, off, lo2, hi2, zero2, sr2, az2, pa, ftest, fpos, ff,
                               ffc[s], half ? 2 : 1, eff);
-    efwc[s] = filter_list<ND>(s, nf, ta, cs, lo2, hi2, zero2, sr2, az2, pa, wtest, wpos, fw,
+    efwc[s] = filter_list<ND>(s, nf, ta, off, lo2, hi2, zero2, sr2, az2, pa, wtest, wpos, fw,
                               fwc[s], 0, efw);
 }
 

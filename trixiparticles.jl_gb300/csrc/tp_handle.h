@@ -103,7 +103,11 @@ struct tp_handle {
     // integrator (slots map to caller indices through its state's id array).  The owner reuses
     // them across calls until a particle has moved more than skin * h.
     int lists_owner = 0;
-    int pair_block = 128;       // threads per block of the pair / Adami kernels (autotuned)
+    // How the slot records (f_pos / f_aux, pressure of the last right-hand side) map to caller
+    // indices: 0 not at all (an unconditional sort replaced f_perm since), 1 through f_perm
+    // (kick! path), 2 through the integrator's final state id array.
+    int records_order = 0;
+    int pair_block = 128;      // threads per block of the pair / Adami kernels (autotuned)
 
     // ---- integrator ping-pong state ----
     tp::PhysState st[2];

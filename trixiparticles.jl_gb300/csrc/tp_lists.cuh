@@ -30,11 +30,18 @@ namespace tp {
 constexpr int kSlotBits = 25;  // slot field of a list entry: at most 2^25 particles per set
 constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;
 
-__device__ __forceinline__ void decode_cell_offset(unsigned e, int& dx, int& dy, int& dz) {
-    const int code = (int)(e >> kSlotBits);
-    dx = code % 5 - 2;
-    dy = (code / 5) % 5 - 2;
-    dz = code / 25 - 2;
+// Cell offsets of the 125 entry codes times the FP32 cell size, {dx cs, dy cs, dz cs, 0} at
+// code (dx+2) + 5 (dy+2) + 25 (dz+2), staged in shared memory by every kernel that reads lists:
+// one 16-byte shared load per candidate instead of an integer-division decode.  dx cs is exact
+// in FP32 for |dx| <= 2, so (o_a - dx cs) rounds exactly like fmaf(-dx, cs, o_a).
+constexpr int kOffsetCodes = 125;
+
+// Fills the block's table and synchronises the block: call before any thread returns.
+__device__ __forceinline__ void fill_offset_table(float4* tab, float cs) {
+    for (int i = threadIdx.x; i < kOffsetCodes; i += blockDim.x)
+        tab[i] = make_float4((float)(i % 5 - 2) * cs, (float)((i / 5) % 5 - 2) * cs,
+                             (float)(i / 25 - 2) * cs, 0.0f);
+    __syncthreads();
 }
 
 // Reach of the cell search of a query at offset o in its cell along one axis: 2 cells towards a
@@ -42,18 +49,18 @@ __device__ __forceinline__ void decode_cell_offset(unsigned e, int& dx, int& dy,
 __device__ __forceinline__ int reach_lo(float o, float m) { return o <= m ? 2 : 1; }
 __device__ __forceinline__ int reach_hi(float o, float cs, float m) { return o >= cs - m ? 2 : 1; }
 
-// o_a - o_b + (c_a - c_b) * cs from a list entry (same arithmetic as the list filter).
+// o_a - o_b + (c_a - c_b) * cs from a list entry and the block's offset table (same arithmetic
+// as the list filter).
 template <int ND>
-__device__ __forceinline__ float pair_diff(float4 ta, float cs, unsigned e, float4 cb, float& pdx,
-                                           float& pdy, float& pdz) {
-    int dx, dy, dz;
-    decode_cell_offset(e, dx, dy, dz);
-    pdx = fmaf(-(float)dx, cs, ta.x) - cb.x;
-    pdy = fmaf(-(float)dy, cs, ta.y) - cb.y;
+__device__ __forceinline__ float pair_diff(float4 ta, const float4* tab, unsigned e, float4 cb,
+                                           float& pdx, float& pdy, float& pdz) {
+    const float4 o = tab[e >> kSlotBits];
+    pdx = (ta.x - o.x) - cb.x;
+    pdy = (ta.y - o.y) - cb.y;
     float d2 = fmaf(pdy, pdy, pdx * pdx);
     pdz = 0.0f;
     if (ND == 3) {
-        pdz = fmaf(-(float)dz, cs, ta.z) - cb.z;
+        pdz = (ta.z - o.z) - cb.z;
         d2 = fmaf(pdz, pdz, d2);
     }
     return d2;
