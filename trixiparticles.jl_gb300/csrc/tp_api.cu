@@ -371,6 +371,7 @@ void setup_phys(tp_handle* h) {
     P.alpha_c = P.alpha * P.c;
     P.visc_k = P.alpha_c * P.visc_h;
     P.visc_k2 = 2.0 * P.visc_k;
+    P.visc_k2s = P.visc_k2 * P.sg_c;
     P.diff2 = 2.0 * P.diff_coef;
 
     Phys32& Q = h->phys32;

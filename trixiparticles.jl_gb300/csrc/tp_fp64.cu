@@ -4,9 +4,10 @@
 // reference writes as `div_fast` use its CUDA Float64 definition x * fast_inv(y)
 // (ext/TrixiParticlesCUDAExt.jl:12-32): approximate reciprocal `rcp.approx.ftz.f64` refined by
 // one cubic iteration e = 1 - a r; e = e + e^2; r = r + e r (the method the reference takes from
-// Oceananigans.jl PR 5140).  fast_inv(rho) of every particle is evaluated once in the pack pass
-// and reused for rho_a / rho_b and m_b / rho_b, which is bitwise the same as evaluating it per
-// pair.  Plain `/` in the reference stays IEEE division here.
+// Oceananigans.jl PR 5140).  fast_inv(rho) of every particle is evaluated once per pass (pack:
+// m_b / rho_b of the neighbour records; pair kernel: its own 1 / rho_a) and reused for every
+// pair, which is bitwise the same as evaluating it per pair.  Plain `/` in the reference stays
+// IEEE division here.
 //
 // Neighbour lists (tp_lists.cuh) are built with an FP32 distance on cell-relative offsets whose
 // bound is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative).  Before every pair
@@ -60,7 +61,12 @@ struct Pack64 {
     float4* test;    // offsets against the reference cell (the cell of the last rebuild)
     double4_32a* pos;
     double4_32a* vel;
-    double4_32a* aux;  // {m, m / rho, 1 / rho, 2 m alpha c h} with 1 / rho = fast_inv(rho)
+    // gather mode: {p S, S, A, 2 m alpha c h sg_c} with S = sg_c m / rho (the kernel
+    // gradient's constant folded into the per-particle factors) and A = p_off + p - rho g.x
+    // (the Adami sum term of a wall w is then A + rho g.x_w);
+    // symmetric mode: {m, m / rho, 1 / rho, 2 m alpha c h};  1 / rho = fast_inv(rho)
+    double4_32a* aux;
+    int symmetric;
     const int* src_perm;  // kick! path: without a rebuild, slot s packs caller particle perm[s]
     GridDesc g;
     double cs32;
@@ -79,7 +85,14 @@ struct Pack64 {
         pos[s] = make_double4_32a(x[0], x[1], ND == 3 ? x[2] : 0.0, p);
         vel[s] = make_double4_32a(w[0], w[1], ND == 3 ? w[2] : 0.0, rho);
         const double ir = fast_inv(rho);
-        aux[s] = make_double4_32a(mi, mi * ir, ir, mi * P.visc_k2);
+        if (symmetric) {
+            aux[s] = make_double4_32a(mi, mi * ir, ir, mi * P.visc_k2);
+        } else {
+            const double S = P.sg_c * (mi * ir);
+            double gx = P.g[0] * x[0] + P.g[1] * x[1];
+            if (ND == 3) gx += P.g[2] * x[2];
+            aux[s] = make_double4_32a(p * S, S, fma(-rho, gx, P.p_off + p), mi * P.visc_k2s);
+        }
         if (rebuild && xb_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
@@ -131,17 +144,23 @@ struct PackWall64 {
 // Adami pressure extrapolation (dummy_particles.jl:489-569, 586-606, 637-672): one lane per
 // wall slot gathers its fluid neighbours in PointNeighbors order.
 // ------------------------------------------------------------------------------------------
-template <int ND>
+// FOLD (gather pair mode): the fluid records carry A_f = p_off + p_f - rho_f g.x_f, so the sum
+// term p_off + p_f + g.(rho_f (x_w - x_f)) is fma(rho_f, g.x_w, A_f), and the kernel's norm is
+// applied once to the sums (their ratio does not depend on it).
+template <int ND, bool FOLD>
 __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
                                                  const unsigned* __restrict__ wf,
                                                  const int* __restrict__ wfc,
                                                  double4_32a* __restrict__ wstate,
                                                  double* __restrict__ wvol,
                                                  const double4_32a* __restrict__ fpos,
-                                                 const double4_32a* __restrict__ fvel) {
+                                                 const double4_32a* __restrict__ fvel,
+                                                 const double4_32a* __restrict__ faux) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const double4_32a xw = wpos[w];
+    double gxw = P.g[0] * xw.x + P.g[1] * xw.y;
+    if (ND == 3) gxw += P.g[2] * xw.z;
     double Ps = 0.0, V = 0.0;
     const int n = wfc[w];
     for (int k = 0; k < n; ++k) {
@@ -153,24 +172,41 @@ __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_3
         if (d2 > P.sr2) continue;
         const double r = d2 > 0.0 ? d2 * rsqrt(d2) : 0.0;
         const double rho_f = fvel[b].w;
-        double hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
-        if (ND == 3) hp += P.g[2] * (rho_f * pd2);
-        const double sum = (P.p_off + xb.w) + hp;
+        double sum;
+        if (FOLD) {
+            sum = fma(rho_f, gxw, faux[b].z);
+        } else {
+            double hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
+            if (ND == 3) hp += P.g[2] * (rho_f * pd2);
+            sum = (P.p_off + xb.w) + hp;
+        }
         double W = 0.0;
         if (r < P.two_h) {
             const double q = r * P.h_inv;
             const double t = fma(-0.5, q, 1.0);
             const double t2 = t * t;
-            W = (P.wc2_norm * (t2 * t2)) * fma(2.0, q, 1.0);
+            W = FOLD ? (t2 * t2) * fma(2.0, q, 1.0)
+                     : (P.wc2_norm * (t2 * t2)) * fma(2.0, q, 1.0);
         }
         Ps = fma(sum, W, Ps);
         V += W;
     }
-    if (V > 2.220446049250313e-16) Ps = Ps / V;
+    if (FOLD) {
+        const double Vn = P.wc2_norm * V;
+        Ps = Vn > 2.220446049250313e-16 ? Ps / V : P.wc2_norm * Ps;
+        V = Vn;
+    } else if (V > 2.220446049250313e-16) {
+        Ps = Ps / V;
+    }
     if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
     const double rho_w = eos_inverse(Ps, P);
     const double ir_w = fast_inv(rho_w);
-    wstate[w] = make_double4_32a(Ps, rho_w, ir_w, xw.w * ir_w);  // {p, rho, 1/rho, m/rho}
+    if (FOLD) {
+        const double S = P.sg_c * (xw.w * ir_w);
+        wstate[w] = make_double4_32a(Ps, rho_w, Ps * S, S);  // {p, rho, p S, S = sg_c m/rho}
+    } else {
+        wstate[w] = make_double4_32a(Ps, rho_w, ir_w, xw.w * ir_w);  // {p, rho, 1/rho, m/rho}
+    }
     wvol[w] = V;
 }
 
@@ -304,18 +340,20 @@ __global__ void __launch_bounds__(256) k_filter64(
 //   diffusion: psi_ab . grad W = 2 (rho_a - rho_b) / r^2 (x_ab . sg x_ab) = 2 (rho_a - rho_b) sg;
 //   Monaghan: mu / rho_mean from one reciprocal of (r^2 + eps h^2) rho_mean;
 //   1 / (rho_a rho_b) and m_b / rho_b from the per-particle fast_inv(rho) of the pack;
+//   the constant sg_c folded into the neighbour records (S_b = sg_c m_b / rho_b, p_b S_b,
+//   2 m_b alpha c h sg_c), so the pressure factor is one FMA and sg is t^3 alone;
 //   r = d^2 rsqrt(d^2); the zero-distance skip `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28)
 //   tested as d^2 < eps((2h)^2).
 // Each term equals the reference's expression up to a few ulp of rounding.
-__device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a& ab, double vr,
-                                                double d2, double rho_sum) {
-    // m_b (alpha c mu + beta mu^2) / rho_mean, mu = h vr / (r^2 + eps h^2), rho_mean = rho_sum / 2
-    // (vr < 0); ab.w = 2 m_b alpha c h
+__device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a& ab, double rho_b,
+                                                double vr, double d2, double rho_sum) {
+    // sg_c m_b (alpha c mu + beta mu^2) / rho_mean, mu = h vr / (r^2 + eps h^2),
+    // rho_mean = rho_sum / 2 (vr < 0); ab.w = 2 m_b alpha c h sg_c, ab.y rho_b = sg_c m_b
     const double den = d2 + P.visc_eps_h2;
     const double R = fast_inv(den * rho_sum);
     if (P.beta == 0.0) return ab.w * vr * R;
     const double mu = (P.visc_h * vr) * (rho_sum * R);
-    return (ab.x * mu) * (P.alpha_c + P.beta * mu) * (2.0 * den * R);
+    return ((ab.y * rho_b) * mu) * (P.alpha_c + P.beta * mu) * (2.0 * den * R);
 }
 
 template <int ND, bool INTEGRATE>
@@ -335,7 +373,7 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
-    const double p_a = pa.w, rho_a = va.w, ia = faux[s].z;
+    const double p_a = pa.w, rho_a = va.w, nia = -fast_inv(rho_a);  // the pack's 1 / rho
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
@@ -349,22 +387,23 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         if (ND == 3) d2 += pd2 * pd2;
         const double r = d2 * rsqrt(d2);  // d2 >= eps((2h)^2): the filter dropped closer pairs
         const double t = fma(-r, P.half_hinv, 1.0);
-        const double sg = P.sg_c * ((t * t) * t);
+        const double t3 = (t * t) * t;  // grad W_ab = sg_c t^3 x_ab, sg_c folded into ab
         const double4_32a vb = fvel[b];
-        const double4_32a ab = faux[b];  // {m_b, m_b / rho_b, 1 / rho_b, 2 m_b alpha c h}
+        const double4_32a ab = faux[b];  // {p_b S_b, S_b, A_b, 2 m_b alpha c h sg_c}
         const double vd0 = va.x - vb.x, vd1 = va.y - vb.y;
         const double vd2 = (ND == 3) ? va.z - vb.z : 0.0;
         double vr = vd0 * pd0 + vd1 * pd1;
         if (ND == 3) vr += vd2 * pd2;
-        double c = -(ab.y * ia) * (p_a + pb.w);
-        if (P.visc && vr < 0.0) c += monaghan_coef(P, ab, vr, d2, rho_a + vb.w);
-        c *= sg;
+        // -sg_c m_b (p_a + p_b) / (rho_a rho_b) = -(p_a S_b + p_b S_b) / rho_a
+        double c = nia * fma(p_a, ab.y, ab.x);
+        if (P.visc && vr < 0.0) c += monaghan_coef(P, ab, vb.w, vr, d2, rho_a + vb.w);
+        c *= t3;
         dv0 += c * pd0;
         dv1 += c * pd1;
         if (ND == 3) dv2 += c * pd2;
         // continuity (rho_a / rho_b) m_b v_ab . grad W  +  diffusion m_b / rho_b psi . grad W
         const double dd = P.diff ? P.diff2 * (rho_a - vb.w) : 0.0;
-        drho += (ab.y * sg) * fma(rho_a, vr, dd);
+        drho += (ab.y * t3) * fma(rho_a, vr, dd);
     }
 
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion, wall velocity 0) ----
@@ -379,15 +418,15 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         if (ND == 3) d2 += pd2 * pd2;
         const double r = d2 * rsqrt(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
-        const double sg = P.sg_c * ((t * t) * t);
-        const double4_32a sb = wstate[b];  // {p, rho, 1/rho, m/rho}
-        const double c = (-(sb.w * ia) * (p_a + sb.x)) * sg;
+        const double t3 = (t * t) * t;
+        const double4_32a sb = wstate[b];  // {p, rho, p S, S = sg_c m / rho}
+        const double c = (nia * fma(p_a, sb.w, sb.z)) * t3;
         ew0 += c * pd0;
         ew1 += c * pd1;
         if (ND == 3) ew2 += c * pd2;
         double vx = va.x * pd0 + va.y * pd1;
         if (ND == 3) vx += va.z * pd2;
-        erho += (rho_a * sb.w) * (sg * vx);
+        erho += (rho_a * sb.w) * (t3 * vx);
     }
 
     // dv = ((0 + S_ff) + S_fw) + g ;  drho = S_ff + S_fw
@@ -589,6 +628,7 @@ static void pack_fluid64(tp_handle* h, const double* u, const double* v, const d
     pk.pos = (double4_32a*)h->f_pos;
     pk.vel = (double4_32a*)h->f_vel;
     pk.aux = (double4_32a*)h->f_aux;
+    pk.symmetric = h->pair_mode == TP_PAIR_SYMMETRIC;
     pk.g = h->grid;
     pk.cs32 = (double)(float)h->grid.cs;
     pk.P = h->phys;
@@ -638,17 +678,22 @@ void fp64_pack_wall(tp_handle* h, const double* x, const double* m) {
 void fp64_adami(tp_handle* h) {
     const int nw = (int)h->cfg.n_wall;
     if (nw == 0) return;
-    auto run = [&](auto ndc) {
+    const bool fold = h->pair_mode != TP_PAIR_SYMMETRIC;
+    auto run = [&](auto ndc, auto foldc) {
         constexpr int ND = decltype(ndc)::value;
-        k_adami64<ND><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
+        k_adami64<ND, decltype(foldc)::value><<<nblk(nw, h->pair_block), h->pair_block, 0,
+                                                 h->stream>>>(
             h->phys, nw, (const double4_32a*)h->w_pos, h->l_wf, h->c_wf,
             (double4_32a*)h->w_state, h->w_vol, (const double4_32a*)h->f_pos,
-            (const double4_32a*)h->f_vel);
+            (const double4_32a*)h->f_vel, (const double4_32a*)h->f_aux);
     };
-    if (h->cfg.ndims == 2)
-        run(std::integral_constant<int, 2>{});
-    else
-        run(std::integral_constant<int, 3>{});
+    if (h->cfg.ndims == 2) {
+        if (fold) run(std::integral_constant<int, 2>{}, std::true_type{});
+        else run(std::integral_constant<int, 2>{}, std::false_type{});
+    } else {
+        if (fold) run(std::integral_constant<int, 3>{}, std::true_type{});
+        else run(std::integral_constant<int, 3>{}, std::false_type{});
+    }
 }
 
 template <int ND, bool INTEG>

@@ -64,6 +64,7 @@ struct Phys {
     double half_hinv;  // 0.5 * h_inv: 1 - q/2 = 1 - r * half_hinv
     double visc_k;     // alpha * c * visc_h (Monaghan with beta = 0)
     double visc_k2;    // 2 * visc_k (per-particle 2 m alpha c h of the pack)
+    double visc_k2s;   // visc_k2 * sg_c (gather-mode record: 2 m alpha c h sg_c)
     double alpha_c;    // alpha * c
     double diff2;      // 2 * diff_coef
 };
