@@ -356,28 +356,49 @@ __device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a
     return ((ab.y * rho_b) * mu) * (P.alpha_c + P.beta * mu) * (2.0 * den * R);
 }
 
+// Skin lists in, exact lists of this stage out (the filter fused into the gather pair kernel).
+struct Filter64 {
+    float cs, lo2, hi2, zero2;
+    const float4* ftest;
+    const float4* wtest;
+    const unsigned* ff;
+    const int* ffc;
+    const unsigned* fw;
+    const int* fwc;
+    int* eff;  // written and read back by the same thread: no restrict, no read-only path
+    int* efw;
+};
+
+// The gather pass first filters its slot's skin lists into exact lists (the same filter_list as
+// k_filter64), then walks them.  Fused, the filter's gathers and FP32 tests of some warps run
+// under the FP64 pair arithmetic of others instead of in a latency-bound pass of their own.
 template <int ND, bool INTEGRATE>
 __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
                                                 const double4_32a* __restrict__ fpos,
                                                 const double4_32a* __restrict__ fvel,
                                                 const double4_32a* __restrict__ faux,
-                                                const int* __restrict__ eff,
-                                                const int* __restrict__ effc,
-                                                const int* __restrict__ efw,
-                                                const int* __restrict__ efwc,
+                                                Filter64 F,
                                                 const double4_32a* __restrict__ wpos,
                                                 const double4_32a* __restrict__ wstate,
                                                 unsigned* __restrict__ gate, Update64 U) {
+    __shared__ float4 off[kOffsetCodes];
+    fill_offset_table(off, F.cs);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
+    const float4 ta = F.ftest[s];
+    const int nff = filter_list<ND>(s, nf, ta, off, F.lo2, F.hi2, F.zero2, P.sr2, P.az2, pa,
+                                    F.ftest, fpos, F.ff, F.ffc[s], 1, F.eff);
+    const int nfw = filter_list<ND>(s, nf, ta, off, F.lo2, F.hi2, F.zero2, P.sr2, P.az2, pa,
+                                    F.wtest, wpos, F.fw, F.fwc[s], 0, F.efw);
+    const int* eff = F.eff;
+    const int* efw = F.efw;
     const double p_a = pa.w, rho_a = va.w, nia = -fast_inv(rho_a);  // the pack's 1 / rho
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
-    const int nff = effc[s];
     for (int k = 0; k < nff; ++k) {
         const int b = eff[(size_t)k * nf + s];
         const double4_32a pb = fpos[b];
@@ -408,7 +429,6 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
 
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion, wall velocity 0) ----
     double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
-    const int nfw = efwc[s];
     for (int k = 0; k < nfw; ++k) {
         const int b = efw[(size_t)k * nf + s];
         const double4_32a pb = wpos[b];
@@ -701,12 +721,13 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
     const double sr2 = h->phys.sr2;
     const bool sym = h->pair_mode == TP_PAIR_SYMMETRIC;
-    k_filter64<ND><<<nblk(nf, 256), 256, 0, h->stream>>>(
-        sr2, h->phys.az2, (float)h->grid.cs, (float)(sr2 * (1.0 - 1e-5)),
-        (float)(sr2 * (1.0 + 1e-5)), (float)(sr2 * 1e-6), nf,
-        h->f_test, (const double4_32a*)h->f_pos, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test,
-        (const double4_32a*)h->w_pos, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw, sym ? 1 : 0);
+    const float lo2 = (float)(sr2 * (1.0 - 1e-5)), hi2 = (float)(sr2 * (1.0 + 1e-5));
+    const float zero2 = (float)(sr2 * 1e-6);
     if (sym) {
+        k_filter64<ND><<<nblk(nf, 256), 256, 0, h->stream>>>(
+            sr2, h->phys.az2, (float)h->grid.cs, lo2, hi2, zero2, nf, h->f_test,
+            (const double4_32a*)h->f_pos, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test,
+            (const double4_32a*)h->w_pos, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw, 1);
         k_pair64s<ND><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
             (const double4_32a*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
@@ -715,11 +736,12 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->acc, U);
         h->launches += 2;  // filter + update (the pair launch is counted by the caller)
     } else {
+        Filter64 F{(float)h->grid.cs, lo2, hi2, zero2, h->f_test, h->w_test, h->l_ff, h->c_ff,
+                   h->l_fw, h->c_fw, h->e_ff, h->e_fw};
         k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
-            (const double4_32a*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
-            (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, gate, U);
-        h->launches += 1;  // the filter
+            (const double4_32a*)h->f_aux, F, (const double4_32a*)h->w_pos,
+            (const double4_32a*)h->w_state, gate, U);
     }
 }
 
