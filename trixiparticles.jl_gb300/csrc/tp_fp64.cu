@@ -144,32 +144,47 @@ struct PackWall64 {
 // Adami pressure extrapolation (dummy_particles.jl:489-569, 586-606, 637-672): one lane per
 // wall slot gathers its fluid neighbours in PointNeighbors order.
 // ------------------------------------------------------------------------------------------
+// The support test is decided like the exact-list filter: an FP32 distance on the cell-relative
+// offsets outside a 1e-5 band around (2h)^2, the explicitly rounded FP64 distance inside it, so
+// the accepted pairs are the CPU's; the FP64 distance of an accepted pair is then formed with FMAs.
 // FOLD (gather pair mode): the fluid records carry A_f = p_off + p_f - rho_f g.x_f, so the sum
 // term p_off + p_f + g.(rho_f (x_w - x_f)) is fma(rho_f, g.x_w, A_f), and the kernel's norm is
 // applied once to the sums (their ratio does not depend on it).
 template <int ND, bool FOLD>
 __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
+                                                 const float4* __restrict__ wtest,
                                                  const unsigned* __restrict__ wf,
                                                  const int* __restrict__ wfc,
                                                  double4_32a* __restrict__ wstate,
                                                  double* __restrict__ wvol,
                                                  const double4_32a* __restrict__ fpos,
                                                  const double4_32a* __restrict__ fvel,
-                                                 const double4_32a* __restrict__ faux) {
+                                                 const double4_32a* __restrict__ faux,
+                                                 const float4* __restrict__ ftest, float cs,
+                                                 float lo2, float hi2) {
+    __shared__ float4 off[kOffsetCodes];
+    fill_offset_table(off, cs);
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const double4_32a xw = wpos[w];
+    const float4 tw = wtest[w];
     double gxw = P.g[0] * xw.x + P.g[1] * xw.y;
     if (ND == 3) gxw += P.g[2] * xw.z;
+    const double two_hinv = 2.0 * P.h_inv;
     double Ps = 0.0, V = 0.0;
     const int n = wfc[w];
     for (int k = 0; k < n; ++k) {
-        const int b = (int)(wf[(size_t)k * nw + w] & kSlotMask);
+        const unsigned e = wf[(size_t)k * nw + w];
+        const int b = (int)(e & kSlotMask);
+        float f0, f1, f2;
+        const float d2f = pair_diff<ND>(tw, off, e, ftest[b], f0, f1, f2);
+        if (d2f > hi2) continue;
         const double4_32a xb = fpos[b];
         const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
         const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
-        const double d2 = dist2_rn<ND>(pd0, pd1, pd2);  // exact support test, as the CPU
-        if (d2 > P.sr2) continue;
+        if (d2f > lo2 && dist2_rn<ND>(pd0, pd1, pd2) > P.sr2) continue;  // the CPU's test
+        double d2 = pd0 * pd0 + pd1 * pd1;
+        if (ND == 3) d2 += pd2 * pd2;
         const double r = d2 > 0.0 ? d2 * rsqrt(d2) : 0.0;
         const double rho_f = fvel[b].w;
         double sum;
@@ -181,12 +196,11 @@ __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_3
             sum = (P.p_off + xb.w) + hp;
         }
         double W = 0.0;
-        if (r < P.two_h) {
-            const double q = r * P.h_inv;
-            const double t = fma(-0.5, q, 1.0);
+        if (r < P.two_h) {  // (1 - q/2)^4 (2q + 1), q = r / h
+            const double t = fma(-r, P.half_hinv, 1.0);
             const double t2 = t * t;
-            W = FOLD ? (t2 * t2) * fma(2.0, q, 1.0)
-                     : (P.wc2_norm * (t2 * t2)) * fma(2.0, q, 1.0);
+            W = FOLD ? (t2 * t2) * fma(r, two_hinv, 1.0)
+                     : (P.wc2_norm * (t2 * t2)) * fma(r, two_hinv, 1.0);
         }
         Ps = fma(sum, W, Ps);
         V += W;
@@ -699,13 +713,16 @@ void fp64_adami(tp_handle* h) {
     const int nw = (int)h->cfg.n_wall;
     if (nw == 0) return;
     const bool fold = h->pair_mode != TP_PAIR_SYMMETRIC;
+    const double sr2 = h->phys.sr2;
+    const float cs = (float)h->grid.cs, lo2 = (float)(sr2 * (1.0 - 1e-5)),
+                hi2 = (float)(sr2 * (1.0 + 1e-5));
     auto run = [&](auto ndc, auto foldc) {
         constexpr int ND = decltype(ndc)::value;
         k_adami64<ND, decltype(foldc)::value><<<nblk(nw, h->pair_block), h->pair_block, 0,
                                                  h->stream>>>(
-            h->phys, nw, (const double4_32a*)h->w_pos, h->l_wf, h->c_wf,
+            h->phys, nw, (const double4_32a*)h->w_pos, h->w_test, h->l_wf, h->c_wf,
             (double4_32a*)h->w_state, h->w_vol, (const double4_32a*)h->f_pos,
-            (const double4_32a*)h->f_vel, (const double4_32a*)h->f_aux);
+            (const double4_32a*)h->f_vel, (const double4_32a*)h->f_aux, h->f_test, cs, lo2, hi2);
     };
     if (h->cfg.ndims == 2) {
         if (fold) run(std::integral_constant<int, 2>{}, std::true_type{});
