@@ -93,9 +93,17 @@ __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__
 
 // Warp-cooperative candidate search: lanes are grouped by their (cy, cz) row; for each searched
 // row the group's candidates form one contiguous slot range (cells are linearised x fastest),
-// which the warp streams through shared memory 32 test records at a time; every lane tests every
-// staged record against its own cell range and radius and appends hits to its list column.
+// which the warp streams through shared memory 32 test records at a time, and every lane tests
+// the staged records against its own cell range and radius and appends hits to its list column.
 // m = r_list - cs (plus a rounding margin) decides where the search reaches two cells.
+//
+// Because a cell's particles fill it, some lane of a group is nearly always close to each face,
+// so the union of the lanes' ranges is about 5 x 5 rows of 5 cells.  The group's lanes are
+// therefore bounded by a box (relative to the group's first cell), rows farther than r_list from
+// the box are skipped, and each staged record is first tested against the box inflated by
+// r_list (by the lane that staged it); only records that pass are tested by every lane.  The box
+// tests are conservative (inflated radius and margins), so the lists -- entries and order -- are
+// the ones the plain union search produces.
 template <int ND>
 __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m, bool active,
                                             const int c[3], float4 oa,
@@ -110,20 +118,40 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
     const int yl = reach_lo(oa.y, m), yh = reach_hi(oa.y, cs, m);
     const int zl = (ND == 3) ? reach_lo(oa.z, m) : 0, zh = (ND == 3) ? reach_hi(oa.z, cs, m) : 0;
     const int yz = active ? (c[1] + g.n[1] * c[2]) : -1;
+    const float margin = 1e-3f * cs;
+    const float rbox = sqrtf(r2f) * 1.0001f + margin;
+    const float r2box = rbox * rbox;
     unsigned todo = __ballot_sync(FULL, active);
     while (todo) {
         const int leader = __ffs(todo) - 1;
         const int yz0 = __shfl_sync(FULL, yz, leader);
+        const int cx0 = __shfl_sync(FULL, c[0], leader);
         const bool ing = active && (yz == yz0);
         const unsigned grp = __ballot_sync(FULL, ing);
         todo &= ~grp;
         const int cy = yz0 % g.n[1], cz = yz0 / g.n[1];
         const float cxa = (float)c[0];
+        // box of the group's lanes relative to cell (cx0, cy, cz); the group's cells are
+        // cx >= cx0 (slot order), offsets are clamped at 0 so that float bits order as ints
+        const float ax = fmaxf(fmaf((float)(c[0] - cx0), cs, oa.x), 0.0f);
+        const float ay = fmaxf(oa.y, 0.0f), az = fmaxf(oa.z, 0.0f);
+        const float bx0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(ax) : INT_MAX)) - margin;
+        const float bx1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(ax) : 0)) + margin;
+        const float by0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(ay) : INT_MAX)) - margin;
+        const float by1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(ay) : 0)) + margin;
+        float bz0 = 0.0f, bz1 = 0.0f;
+        if (ND == 3) {
+            bz0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(az) : INT_MAX)) - margin;
+            bz1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(az) : 0)) + margin;
+        }
         const int zr = (ND == 3) ? 2 : 0;
         for (int dz = -zr; dz <= zr; ++dz) {
             if (cz + dz < 0 || cz + dz >= g.n[2]) continue;
+            const float ez = (ND == 3) ? fmaxf(fmaxf((float)dz * cs - bz1, bz0 - (float)(dz + 1) * cs), 0.0f) : 0.0f;
             for (int dy = -2; dy <= 2; ++dy) {
                 if (cy + dy < 0 || cy + dy >= g.n[1]) continue;
+                const float ey = fmaxf(fmaxf((float)dy * cs - by1, by0 - (float)(dy + 1) * cs), 0.0f);
+                if (fmaf(ey, ey, ez * ez) > r2box) continue;  // the whole row is out of reach
                 const bool need = ing && dy >= -yl && dy <= yh && dz >= -zl && dz <= zh;
                 if (!__ballot_sync(FULL, need)) continue;
                 const int xa = need ? max(c[0] - xl, 0) : INT_MAX;
@@ -141,13 +169,32 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                 }
                 const float sy = fmaf(-(float)dy, cs, oa.y);
                 const float sz = fmaf(-(float)dz, cs, oa.z);
+                const float ryz = fmaf(ey, ey, ez * ez);
                 const unsigned rowcode = 5u * (unsigned)(dy + 2) + 25u * (unsigned)(dz + 2);
                 for (int base = lo; base < hi; base += 32) {
                     const int j = base + lane;
-                    if (j < hi) cand[lane] = test[j];
+                    bool rel = false;
+                    if (j < hi) {
+                        const float4 cb = test[j];
+                        cand[lane] = cb;
+                        // box distance of the staged record (its row distance is ey, ez at least)
+                        const float X = fmaf(cb.w - (float)cx0, cs, cb.x);
+                        const float Y = fmaf((float)dy, cs, cb.y);
+                        const float ex = fmaxf(fmaxf(bx0 - X, X - bx1), 0.0f);
+                        const float eyc = fmaxf(fmaxf(by0 - Y, Y - by1), 0.0f);
+                        float d2b = fmaf(ex, ex, eyc * eyc);
+                        if (ND == 3) {
+                            const float Z = fmaf((float)dz, cs, cb.z);
+                            const float ezc = fmaxf(fmaxf(bz0 - Z, Z - bz1), 0.0f);
+                            d2b = fmaf(ezc, ezc, d2b);
+                        }
+                        rel = fmaxf(d2b, ryz) <= r2box;
+                    }
+                    unsigned hits = __ballot_sync(FULL, rel);
                     __syncwarp();
-                    const int nc = min(32, hi - base);
-                    for (int k = 0; k < nc; ++k) {
+                    while (hits) {
+                        const int k = __ffs(hits) - 1;
+                        hits &= hits - 1;
                         const float4 cb = cand[k];
                         const int jj = base + k;
                         const float pdx = fmaf(cxa - cb.w, cs, oa.x) - cb.x;
