@@ -109,8 +109,9 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                                             const int c[3], float4 oa,
                                             const int* __restrict__ start,
                                             const float4* __restrict__ test, float r2f,
-                                            float4* cand, unsigned* __restrict__ list,
-                                            int stride, int cap, int s) {
+                                            float4* cand, int* cidx,
+                                            unsigned* __restrict__ list, int stride, int cap,
+                                            int s) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int cnt = 0;
@@ -174,9 +175,9 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                 for (int base = lo; base < hi; base += 32) {
                     const int j = base + lane;
                     bool rel = false;
+                    float4 cb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (j < hi) {
-                        const float4 cb = test[j];
-                        cand[lane] = cb;
+                        cb = test[j];
                         // box distance of the staged record (its row distance is ey, ez at least)
                         const float X = fmaf(cb.w - (float)cx0, cs, cb.x);
                         const float Y = fmaf((float)dy, cs, cb.y);
@@ -190,13 +191,19 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                         }
                         rel = fmaxf(d2b, ryz) <= r2box;
                     }
-                    unsigned hits = __ballot_sync(FULL, rel);
+                    // the records that pass are compacted in staging order (ballot prefix), so the
+                    // test loop below reads them at consecutive shared addresses
+                    const unsigned hits = __ballot_sync(FULL, rel);
+                    if (rel) {
+                        const int pos = __popc(hits & ((1u << lane) - 1u));
+                        cand[pos] = cb;
+                        cidx[pos] = j;
+                    }
                     __syncwarp();
-                    while (hits) {
-                        const int k = __ffs(hits) - 1;
-                        hits &= hits - 1;
-                        const float4 cb = cand[k];
-                        const int jj = base + k;
+                    const int nrel = __popc(hits);
+                    for (int i = 0; i < nrel; ++i) {
+                        const float4 cb = cand[i];
+                        const int jj = cidx[i];
                         const float pdx = fmaf(cxa - cb.w, cs, oa.x) - cb.x;
                         const float pdy = sy - cb.y;
                         float d2 = fmaf(pdy, pdy, pdx * pdx);
@@ -220,7 +227,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
 
 // Fluid slots: fluid-fluid and fluid-wall lists.
 template <int ND>
-__global__ void __launch_bounds__(128) k_build_fluid_lists(
+__global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     GridDesc g, float cs, float m, float r2f, int nf, const float4* __restrict__ ftest,
     const int* __restrict__ fskey, const int* __restrict__ fstart,
     const float4* __restrict__ wtest, const int* __restrict__ wstart, unsigned* __restrict__ ff,
@@ -228,17 +235,19 @@ __global__ void __launch_bounds__(128) k_build_fluid_lists(
     int cap_fw, int* __restrict__ err, const unsigned* __restrict__ gate) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
+    __shared__ int cidx_all[4][32];
     float4* cand = cand_all[threadIdx.x >> 5];
+    int* cidx = cidx_all[threadIdx.x >> 5];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = s < nf;
     const int si = active ? s : 0;
     const float4 ta = ftest[si];
     int c[3];
     key_to_coords(fskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, ff, nf,
-                                    cap_ff, s);
-    const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wtest, r2f, cand, fw, nf,
-                                    cap_fw, s);
+    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, cidx, ff,
+                                    nf, cap_ff, s);
+    const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wtest, r2f, cand, cidx, fw,
+                                    nf, cap_fw, s);
     if (!active) return;
     ffc[s] = min(n1, cap_ff);
     fwc[s] = min(n2, cap_fw);
@@ -247,22 +256,24 @@ __global__ void __launch_bounds__(128) k_build_fluid_lists(
 
 // Wall slots: wall-fluid lists (the Adami gather).
 template <int ND>
-__global__ void __launch_bounds__(128) k_build_wall_lists(
+__global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     GridDesc g, float cs, float m, float r2f, int nw, const float4* __restrict__ wtest,
     const int* __restrict__ wskey, const float4* __restrict__ ftest,
     const int* __restrict__ fstart, unsigned* __restrict__ wf, int* __restrict__ wfc, int cap_wf,
     int* __restrict__ err, const unsigned* __restrict__ gate) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
+    __shared__ int cidx_all[4][32];
     float4* cand = cand_all[threadIdx.x >> 5];
+    int* cidx = cidx_all[threadIdx.x >> 5];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = s < nw;
     const int si = active ? s : 0;
     const float4 ta = wtest[si];
     int c[3];
     key_to_coords(wskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, wf, nw,
-                                    cap_wf, s);
+    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, cidx, wf,
+                                    nw, cap_wf, s);
     if (!active) return;
     wfc[s] = min(n1, cap_wf);
     if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
