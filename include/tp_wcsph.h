@@ -204,7 +204,7 @@ int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n);
 tp_status tp_enable_timing(tp_handle* h, int32_t enable);
 
 /*
- * Neighbour-list skin of tp_integrate_ck2n54 (default 0.1): candidate lists are built at radius
+ * Neighbour-list skin of tp_integrate_ck2n54 (default 0.05): candidate lists are built at radius
  * 2h (1 + skin) and reused across Runge-Kutta stages until some particle has moved more than
  * skin * h since the last rebuild (checked on the device every stage); pairs are still decided
  * exactly with |x_a - x_b|^2 <= (2h)^2 at each stage, so the skin changes speed, not results.

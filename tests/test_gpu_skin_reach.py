@@ -29,20 +29,23 @@ def _config(pkg, precision):
     return c
 
 
-def _state():
+def _state(skin):
     h = 0.035
-    xa = 0.07 * 10 + 0.003          # 0.086 h inside cell 10
-    xb = xa - 2.1 * h               # cell 8: two cells to the left, 2.1 h away
+    xa = 0.07 * 10 + 0.001           # 0.029 h inside cell 10
+    xb = xa - 2.0 * h * (1.0 + 0.5 * skin)  # cell 8: two cells to the left, inside the list radius
     u = np.array([[xa, 0.5], [xb, 0.5]])
     v = np.array([[-1.0, 0.0, 1000.0], [1.0, 0.0, 1000.0]])
     return v, u
 
 
+@pytest.mark.parametrize("skin", [0.05, 0.1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_pair_two_cells_apart_is_not_missed(lib, pkg, orc, cuda, precision):
+def test_pair_two_cells_apart_is_not_missed(lib, pkg, orc, cuda, precision, skin):
     c = _config(pkg, precision)
-    v0, u0 = _state()
-    n, dt = 30, 1e-4  # contact (r < 2h) from step 18; first rebuild by displacement at step 35
+    v0, u0 = _state(skin)
+    assert int(u0[0, 0] // 0.07) - int(u0[1, 0] // 0.07) == 2
+    # contact (r < 2h) after 175 skin steps, first rebuild by displacement after 350 skin steps
+    n, dt = 30, 1e-4
     model = orc.Model(c, np.zeros((0, 2)), np.zeros(0), np.full(2, 1.2))
     v_ref, u_ref, st = model.integrate(v0, u0, dt, n)
     assert st == 0
@@ -51,6 +54,7 @@ def test_pair_two_cells_apart_is_not_missed(lib, pkg, orc, cuda, precision):
 
     h = ctypes.c_void_p()
     assert lib.tp_create(ctypes.byref(c), ctypes.byref(h)) == 0
+    assert lib.tp_set_skin(h, ctypes.c_double(skin)) == 0
     dummy = torch.zeros(2, dtype=torch.float64, device="cuda")
     mf = torch.full((2,), 1.2, dtype=torch.float64, device="cuda")
     p = lambda t: ctypes.c_void_p(t.data_ptr())

@@ -790,6 +790,8 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
         return TP_ERR_CUDA;
     }
     h->cfg = *cfg;
+    // measured on GB300 (3D dam break): the FP32 pair kernel runs best with 256-thread blocks
+    if (cfg->precision == TP_PRECISION_FP32) h->pair_block = 256;
     if (!setup_grid(h, msg)) {
         g_create_error = msg;
         delete h;

@@ -25,7 +25,7 @@ struct tp_batch {
         cudaStream_t stream = nullptr;
         cudaEvent_t join = nullptr;
         int pair_block = 128;
-        double skin = 0.1;
+        double skin = 0.05;
         double trial_ms = 0.0;
     };
     std::vector<Member> m;
