@@ -230,7 +230,7 @@ __global__ void k_scatter_pressure(const void* __restrict__ rec, const int* __re
                                    double* __restrict__ p, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    p[perm[s]] = F32 ? (double)((const float4*)rec)[s].x : ((const double4_32a*)rec)[s].w;
+    p[perm[s]] = F32 ? (double)((const float*)rec)[s] : ((const double4_32a*)rec)[s].w;
 }
 
 template <bool F32>
@@ -568,11 +568,13 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
         constexpr int ND = decltype(ndc)::value;
         if (nf > 0)
             k_build_fluid_lists<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
-                h->grid, cs, m, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_start,
+                h->grid, cs, m, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_skey,
+                h->w_start,
                 h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate);
         if (nw > 0)
             k_build_wall_lists<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
-                h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_start, h->l_wf,
+                h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_skey, h->f_start,
+                h->l_wf,
                 h->c_wf, h->cap_wf, h->d_err, gate);
     };
     if (h->cfg.ndims == 2)
@@ -826,6 +828,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc((double4_32a**)&h->w_pos, nw));
     A(dalloc(&h->w_test, nw));
     A(dalloc((double4_32a**)&h->w_state, nw));
+    A(dalloc(&h->w_p32, nw));
     A(dalloc(&h->w_vol, nw));
     A(dalloc(&h->c_ff, nf));
     A(dalloc(&h->c_fw, nf));
@@ -860,7 +863,7 @@ tp_status tp_destroy(tp_handle* h) {
                     h->f_start, h->f_cursor, h->scan_partial, h->f_test, h->f_pos,
                     h->f_vel,   h->f_aux,   h->m_f,     h->w_key,         h->w_tmp,
                     h->w_perm,  h->w_skey,  h->w_start, h->w_pos,         h->w_test,
-                    h->w_state, h->w_vol,   h->red_partial, h->d_err};
+                    h->w_state, h->w_p32,   h->w_vol,   h->red_partial, h->d_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,

@@ -56,9 +56,9 @@ struct Pack32 {
     int* id_out;
     float* m_out;
     double* xb_out;
-    float4* test;
-    float4* vel;
-    float4* aux;  // {p, m, m / rho, 1 / rho}
+    float4* test;  // {ox, oy, oz, rho - rho0}
+    float4* vel;   // {vx, vy, vz, m / rho}
+    float* pres;   // p
     const int* src_perm;  // kick! path: without a rebuild, slot s packs caller particle perm[s]
     GridDesc g;
     double cs32, rho0;
@@ -81,11 +81,14 @@ struct Pack32 {
             w.w = (float)(vv[ND] - rho0);
             mi = (float)((const double*)m)[i];
         }
-        // offsets against the reference cell `key` (the cell of the last rebuild)
-        test[s] = test_record_in<ND>(x, g, cs32, key);
-        vel[s] = w;
+        // offsets against the reference cell `key` (the cell of the last rebuild); the records
+        // hold what a neighbour gather needs and nothing else: 36 bytes per pair
+        float4 t = test_record_in<ND>(x, g, cs32, key);
+        t.w = w.w;
+        test[s] = t;
         const float irho = __frcp_rn(P.rho0 + w.w);
-        aux[s] = make_float4(eos32(w.w, P, P.fluid_clip), mi, mi * irho, irho);
+        vel[s] = make_float4(w.x, w.y, w.z, mi * irho);
+        pres[s] = eos32(w.w, P, P.fluid_clip);
         if (rebuild && xb_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
@@ -110,15 +113,19 @@ __global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4
     if (s < n) st[s] = make_float4(0.0f, 0.0f, (float)wpos[s].w, 0.0f);
 }
 
+// Per wall slot over its fluid list: the fluid neighbour's offsets and rho - rho0 come with its
+// test record, its pressure from the dense pressure array (20 bytes per pair).  Besides the wall
+// state, the pass leaves m / rho of the wall in the fourth slot of its test record and its
+// pressure in a dense array, which is what the fluid pair pass gathers.
 template <int ND>
-__global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4* __restrict__ wtest,
+__global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __restrict__ wtest,
                                                  const unsigned* __restrict__ wf,
                                                  const int* __restrict__ wfc,
                                                  float4* __restrict__ wstate,
+                                                 float* __restrict__ wpres,
                                                  double* __restrict__ wvol,
                                                  const float4* __restrict__ ftest,
-                                                 const float4* __restrict__ fvel,
-                                                 const float4* __restrict__ faux) {
+                                                 const float* __restrict__ fpres) {
     __shared__ float4 off[kOffsetCodes];
     fill_offset_table(off, P.cs);
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -129,14 +136,15 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4*
     for (int k = 0; k < n; ++k) {
         const unsigned e = wf[(size_t)k * nw + w];
         const int b = (int)(e & kSlotMask);
+        const float4 cb = ftest[b];
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(tw, off, e, ftest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(tw, off, e, cb, pd0, pd1, pd2);
         if (d2 > P.sr2) continue;
         const float r = sqrtf(d2);
-        const float rho_f = P.rho0 + fvel[b].w;
+        const float rho_f = P.rho0 + cb.w;
         float hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
         if (ND == 3) hp += P.g[2] * (rho_f * pd2);
-        const float sum = (P.p_off + faux[b].x) + hp;
+        const float sum = (P.p_off + fpres[b]) + hp;
         float W = 0.0f;
         if (r < P.two_h) {
             const float q = r * P.h_inv;
@@ -153,7 +161,10 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, const float4*
     if (P.wall_clip) pw = (pw != pw || pw > 0.0f) ? pw : 0.0f;
     const float m = wstate[w].z;
     const float dr = eos32_inverse_dev(pw, P);
-    wstate[w] = make_float4(pw, dr, m, m * __frcp_rn(P.rho0 + dr));  // {p, rho - rho0, m, m/rho}
+    const float vol = m * __frcp_rn(P.rho0 + dr);
+    wstate[w] = make_float4(pw, dr, m, vol);  // {p, rho - rho0, m, m/rho}
+    wpres[w] = pw;
+    wtest[w].w = vol;
     wvol[w] = (double)vw;
 }
 
@@ -181,61 +192,65 @@ struct Update32 {
 template <int ND, bool INTEGRATE>
 __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
-                                                const float4* __restrict__ faux,
+                                                const float* __restrict__ fpres,
                                                 const unsigned* __restrict__ ff,
                                                 const int* __restrict__ ffc,
                                                 const unsigned* __restrict__ fw,
                                                 const int* __restrict__ fwc,
                                                 const float4* __restrict__ wtest,
-                                                const float4* __restrict__ wstate,
+                                                const float* __restrict__ wpres,
                                                 unsigned* __restrict__ gate, Update32 U) {
     __shared__ float4 off[kOffsetCodes];
     fill_offset_table(off, P.cs);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
-    const float4 ta = ftest[s];
-    const float4 va = fvel[s];
-    const float4 aa = faux[s];  // {p, m, m/rho, 1/rho}
-    const float p_a = aa.x, ia = aa.w;
-    const float drho_a = va.w;
+    const float4 ta = ftest[s];  // {offsets, rho - rho0}
+    const float4 va = fvel[s];   // {v, m / rho}
+    const float p_a = fpres[s];
+    const float drho_a = ta.w;
     const float rho_a = P.rho0 + drho_a;
+    const float ia = __frcp_rn(rho_a);  // the pack's 1 / rho
 
     Kahan a0, a1, a2, ar;
     const int nff = ffc[s];
     for (int k = 0; k < nff; ++k) {
         const unsigned e = ff[(size_t)k * nf + s];
         const int b = (int)(e & kSlotMask);
+        const float4 cb = ftest[b];  // {offsets, rho_b - rho0}
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, off, e, ftest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(ta, off, e, cb, pd0, pd1, pd2);
         if (d2 > P.sr2 || d2 < P.az2) continue;
         const float r = d2 * rsqrtf(d2);
-        const float4 vb = fvel[b];
-        const float4 ab = faux[b];  // {p_b, m_b, m_b / rho_b, 1 / rho_b}
+        const float4 vb = fvel[b];  // {v_b, m_b / rho_b}
+        const float p_b = fpres[b];
+        const float vol_b = vb.w;
         const float t = fmaf(-r, P.half_hinv, 1.0f);
         const float sg = P.sg_c * ((t * t) * t);
         const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
         const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
         float vr = vd0 * pd0 + vd1 * pd1;
         if (ND == 3) vr += vd2 * pd2;
-        float c = -(ab.z * ia) * (p_a + ab.x);
+        float c = -(vol_b * ia) * (p_a + p_b);
         if (P.visc && vr < 0.0f) {
+            const float rho_b = P.rho0 + cb.w;
+            const float m_b = vol_b * rho_b;
             const float den = d2 + P.visc_eps_h2;
-            const float rm = 0.5f * (rho_a + P.rho0 + vb.w);
+            const float rm = 0.5f * (rho_a + rho_b);
             const float R = __fdividef(1.0f, den * rm);
             if (P.beta == 0.0f) {
-                c += (ab.y * P.visc_k) * vr * R;
+                c += (m_b * P.visc_k) * vr * R;
             } else {
                 const float mu = (P.visc_h * vr) * (rm * R);
-                c += (ab.y * mu) * (P.visc_ac + P.beta * mu) * (den * R);
+                c += (m_b * mu) * (P.visc_ac + P.beta * mu) * (den * R);
             }
         }
         c *= sg;
         a0.add(c * pd0);
         a1.add(c * pd1);
         if (ND == 3) a2.add(c * pd2);
-        float er = (rho_a * ab.z) * (sg * vr);
-        if (P.diff) er += (ab.z * (drho_a - vb.w)) * (sg * P.diff2);
+        float er = (rho_a * vol_b) * (sg * vr);
+        if (P.diff) er += (vol_b * (drho_a - cb.w)) * (sg * P.diff2);
         ar.add(er);
     }
 
@@ -244,15 +259,15 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
     for (int k = 0; k < nfw; ++k) {
         const unsigned e = fw[(size_t)k * nf + s];
         const int b = (int)(e & kSlotMask);
+        const float4 tb = wtest[b];  // {offsets, m_w / rho_w of the last Adami pass}
         float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, off, e, wtest[b], pd0, pd1, pd2);
+        const float d2 = pair_diff<ND>(ta, off, e, tb, pd0, pd1, pd2);
         if (d2 > P.sr2 || d2 < P.az2) continue;
         const float r = d2 * rsqrtf(d2);
-        const float4 sb = wstate[b];  // {p, rho - rho0, m, m / rho}
-        const float vol_b = sb.w;
+        const float vol_b = tb.w;
         const float t = fmaf(-r, P.half_hinv, 1.0f);
         const float sg = P.sg_c * ((t * t) * t);
-        const float c = (-(vol_b * ia) * (p_a + sb.x)) * sg;
+        const float c = (-(vol_b * ia) * (p_a + wpres[b])) * sg;
         w0.add(c * pd0);
         w1.add(c * pd1);
         if (ND == 3) w2.add(c * pd2);
@@ -275,7 +290,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
         // float4 slots: velocity components 0..ND-1 and the density deviation in slot 3
         const float kv[4] = {(float)k[0], (float)k[1], ND == 3 ? (float)k[2] : 0.0f,
                              (float)k[ND]};
-        const float vin[4] = {va.x, va.y, va.z, va.w};
+        const float vin[4] = {va.x, va.y, va.z, drho_a};
         const float4 tv = U.tv[s];
         const float tin[4] = {tv.x, tv.y, tv.z, tv.w};
         float tout[4], vout[4];
@@ -331,7 +346,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         pk.xb_out = h->x_build;
         pk.test = h->f_test;
         pk.vel = (float4*)h->f_vel;
-        pk.aux = (float4*)h->f_aux;
+        pk.pres = (float*)h->f_aux;
         pk.g = h->grid;
         pk.cs32 = cs32;
         pk.rho0 = h->cfg.reference_density;
@@ -363,20 +378,20 @@ void fp32_adami(tp_handle* h) {
     if (nw == 0) return;
     if (h->cfg.ndims == 2)
         k_adami32<2><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
-            h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
-            h->f_test, (const float4*)h->f_vel, (const float4*)h->f_aux);
+            h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_p32, h->w_vol,
+            h->f_test, (const float*)h->f_aux);
     else
         k_adami32<3><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
-            h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_vol,
-            h->f_test, (const float4*)h->f_vel, (const float4*)h->f_aux);
+            h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_p32, h->w_vol,
+            h->f_test, (const float*)h->f_aux);
 }
 
 template <int ND, bool INTEG>
 static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
     const int nf = (int)h->cfg.n_fluid;
     k_pair32<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
-        h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float4*)h->f_aux, h->l_ff,
-        h->c_ff, h->l_fw, h->c_fw, h->w_test, (const float4*)h->w_state, gate, U);
+        h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux, h->l_ff,
+        h->c_ff, h->l_fw, h->c_fw, h->w_test, h->w_p32, gate, U);
 }
 
 void fp32_pair_kick(tp_handle* h, double* dv) {

@@ -55,10 +55,12 @@ struct tp_handle {
     int scan_blocks = 0;
 
     // ---- fluid records (slot order) ----
-    float4* f_test = nullptr;  // {ox, oy, oz, cx}: FP32 neighbour filter (both forms)
+    // f_test: {ox, oy, oz, w}: offsets in the reference cell (FP32 neighbour tests, both forms);
+    // w = x cell index (FP64) or rho - rho0 (FP32, rewritten every stage)
+    float4* f_test = nullptr;
     void* f_pos = nullptr;     // FP64 form / diagnostics: double4 {x, y, z, p}
-    void* f_vel = nullptr;     // FP64: double4 {v, rho};  FP32: float4 {v, rho - rho0}
-    void* f_aux = nullptr;     // FP64: double2 {m, 1/rho}; FP32: float2 {p, m}
+    void* f_vel = nullptr;     // FP64: double4 {v, rho};  FP32: float4 {v, m / rho}
+    void* f_aux = nullptr;     // FP64: double4 (see the pack);  FP32: float p
 
     // ---- fluid masses in caller order (FP64) ----
     double* m_f = nullptr;
@@ -70,8 +72,9 @@ struct tp_handle {
     int* w_skey = nullptr;
     int* w_start = nullptr;  // ncells + 1
     void* w_pos = nullptr;    // double4 {x, y, z, m} (both forms)
-    float4* w_test = nullptr; // {ox, oy, oz, cx}
-    void* w_state = nullptr;  // FP64: double4 {p, rho, 1/rho, 0}; FP32: float4 {p, rho-rho0, m, 0}
+    float4* w_test = nullptr; // {ox, oy, oz, w}: w = x cell (FP64) or m / rho (FP32, Adami)
+    void* w_state = nullptr;  // FP64: double4 (see the Adami pass); FP32: float4 {p, rho-rho0, m, m/rho}
+    float* w_p32 = nullptr;   // FP32: wall pressure of the last Adami pass (dense, for gathers)
     double* w_vol = nullptr;
 
     // ---- neighbour lists (tp_lists.cuh): entry k of slot s at list[k * n + s] ----

@@ -108,6 +108,7 @@ template <int ND>
 __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m, bool active,
                                             const int c[3], float4 oa,
                                             const int* __restrict__ start,
+                                            const int* __restrict__ skey,
                                             const float4* __restrict__ test, float r2f,
                                             float4* cand, int* cidx,
                                             unsigned* __restrict__ list, int stride, int cap,
@@ -177,7 +178,10 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                     bool rel = false;
                     float4 cb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (j < hi) {
+                        // offsets from the test record, the x cell from the sorted cell key
+                        // (the record's fourth slot carries per-stage data in the FP32 form)
                         cb = test[j];
+                        cb.w = (float)(skey[j] - rb);
                         // box distance of the staged record (its row distance is ey, ez at least)
                         const float X = fmaf(cb.w - (float)cx0, cs, cb.x);
                         const float Y = fmaf((float)dy, cs, cb.y);
@@ -230,7 +234,8 @@ template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     GridDesc g, float cs, float m, float r2f, int nf, const float4* __restrict__ ftest,
     const int* __restrict__ fskey, const int* __restrict__ fstart,
-    const float4* __restrict__ wtest, const int* __restrict__ wstart, unsigned* __restrict__ ff,
+    const float4* __restrict__ wtest, const int* __restrict__ wskey,
+    const int* __restrict__ wstart, unsigned* __restrict__ ff,
     int* __restrict__ ffc, int cap_ff, unsigned* __restrict__ fw, int* __restrict__ fwc,
     int cap_fw, int* __restrict__ err, const unsigned* __restrict__ gate) {
     if (!gate_open(gate)) return;
@@ -244,10 +249,10 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     const float4 ta = ftest[si];
     int c[3];
     key_to_coords(fskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, cidx, ff,
-                                    nf, cap_ff, s);
-    const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wtest, r2f, cand, cidx, fw,
-                                    nf, cap_fw, s);
+    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
+                                    cidx, ff, nf, cap_ff, s);
+    const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, cand,
+                                    cidx, fw, nf, cap_fw, s);
     if (!active) return;
     ffc[s] = min(n1, cap_ff);
     fwc[s] = min(n2, cap_fw);
@@ -259,7 +264,8 @@ template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     GridDesc g, float cs, float m, float r2f, int nw, const float4* __restrict__ wtest,
     const int* __restrict__ wskey, const float4* __restrict__ ftest,
-    const int* __restrict__ fstart, unsigned* __restrict__ wf, int* __restrict__ wfc, int cap_wf,
+    const int* __restrict__ fskey, const int* __restrict__ fstart, unsigned* __restrict__ wf,
+    int* __restrict__ wfc, int cap_wf,
     int* __restrict__ err, const unsigned* __restrict__ gate) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
@@ -272,8 +278,8 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     const float4 ta = wtest[si];
     int c[3];
     key_to_coords(wskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, ftest, r2f, cand, cidx, wf,
-                                    nw, cap_wf, s);
+    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
+                                    cidx, wf, nw, cap_wf, s);
     if (!active) return;
     wfc[s] = min(n1, cap_wf);
     if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
