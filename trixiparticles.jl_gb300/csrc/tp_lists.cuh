@@ -173,15 +173,26 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                 const float sz = fmaf(-(float)dz, cs, oa.z);
                 const float ryz = fmaf(ey, ey, ez * ez);
                 const unsigned rowcode = 5u * (unsigned)(dy + 2) + 25u * (unsigned)(dz + 2);
+                // the next chunk's records are loaded while the current one is tested
+                float4 nxt = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                int nkey = 0;
+                if (lo + lane < hi) {
+                    nxt = test[lo + lane];
+                    nkey = skey[lo + lane];
+                }
                 for (int base = lo; base < hi; base += 32) {
                     const int j = base + lane;
                     bool rel = false;
-                    float4 cb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    float4 cb = nxt;
+                    const int key = nkey;
+                    if (j + 32 < hi) {
+                        nxt = test[j + 32];
+                        nkey = skey[j + 32];
+                    }
                     if (j < hi) {
                         // offsets from the test record, the x cell from the sorted cell key
                         // (the record's fourth slot carries per-stage data in the FP32 form)
-                        cb = test[j];
-                        cb.w = (float)(skey[j] - rb);
+                        cb.w = (float)(key - rb);
                         // box distance of the staged record (its row distance is ey, ez at least)
                         const float X = fmaf(cb.w - (float)cx0, cs, cb.x);
                         const float Y = fmaf((float)dy, cs, cb.y);
