@@ -110,7 +110,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                                             const int* __restrict__ start,
                                             const int* __restrict__ skey,
                                             const float4* __restrict__ test, float r2f,
-                                            float4* cand, int* cidx,
+                                            float4* cand, int2* cidx,
                                             unsigned* __restrict__ list, int stride, int cap,
                                             int s) {
     const unsigned FULL = 0xffffffffu;
@@ -132,10 +132,11 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
         const unsigned grp = __ballot_sync(FULL, ing);
         todo &= ~grp;
         const int cy = yz0 % g.n[1], cz = yz0 / g.n[1];
-        const float cxa = (float)c[0];
+        // x of the lane relative to the group's first cell cx0 (staged records carry the same)
+        const float xlane = fmaf((float)(c[0] - cx0), cs, oa.x);
         // box of the group's lanes relative to cell (cx0, cy, cz); the group's cells are
         // cx >= cx0 (slot order), offsets are clamped at 0 so that float bits order as ints
-        const float ax = fmaxf(fmaf((float)(c[0] - cx0), cs, oa.x), 0.0f);
+        const float ax = fmaxf(xlane, 0.0f);
         const float ay = fmaxf(oa.y, 0.0f), az = fmaxf(oa.z, 0.0f);
         const float bx0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(ax) : INT_MAX)) - margin;
         const float bx1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(ax) : 0)) + margin;
@@ -185,16 +186,20 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                     bool rel = false;
                     float4 cb = nxt;
                     const int key = nkey;
+                    int cxb = 0;
                     if (j + 32 < hi) {
                         nxt = test[j + 32];
                         nkey = skey[j + 32];
                     }
                     if (j < hi) {
                         // offsets from the test record, the x cell from the sorted cell key
-                        // (the record's fourth slot carries per-stage data in the FP32 form)
-                        cb.w = (float)(key - rb);
+                        // (the record's fourth slot carries per-stage data in the FP32 form);
+                        // staged as {x relative to cx0, oy, oz} and {slot, x cell} so that the
+                        // lanes' tests below need no conversions
+                        cxb = key - rb;
+                        const float X = fmaf((float)(cxb - cx0), cs, cb.x);
+                        cb.x = X;
                         // box distance of the staged record (its row distance is ey, ez at least)
-                        const float X = fmaf(cb.w - (float)cx0, cs, cb.x);
                         const float Y = fmaf((float)dy, cs, cb.y);
                         const float ex = fmaxf(fmaxf(bx0 - X, X - bx1), 0.0f);
                         const float eyc = fmaxf(fmaxf(by0 - Y, Y - by1), 0.0f);
@@ -212,14 +217,15 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                     if (rel) {
                         const int pos = __popc(hits & ((1u << lane) - 1u));
                         cand[pos] = cb;
-                        cidx[pos] = j;
+                        cidx[pos] = make_int2(j, cxb);
                     }
                     __syncwarp();
                     const int nrel = __popc(hits);
                     for (int i = 0; i < nrel; ++i) {
                         const float4 cb = cand[i];
-                        const int jj = cidx[i];
-                        const float pdx = fmaf(cxa - cb.w, cs, oa.x) - cb.x;
+                        const int2 jc = cidx[i];
+                        const int jj = jc.x;
+                        const float pdx = xlane - cb.x;
                         const float pdy = sy - cb.y;
                         float d2 = fmaf(pdy, pdy, pdx * pdx);
                         if (ND == 3) {
@@ -227,7 +233,8 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                             d2 = fmaf(pdz, pdz, d2);
                         }
                         if (jj >= mlo && jj < mhi && d2 <= r2f) {
-                            const unsigned code = rowcode + (unsigned)((int)(cb.w - cxa) + 2);
+                            const unsigned code =
+                                rowcode + (unsigned)(jc.y - c[0] + 2);
                             if (cnt < cap) list[(size_t)cnt * stride + s] = (unsigned)jj | (code << kSlotBits);
                             ++cnt;
                         }
@@ -251,9 +258,9 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     int cap_fw, int* __restrict__ err, const unsigned* __restrict__ gate) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
-    __shared__ int cidx_all[4][32];
+    __shared__ int2 cidx_all[4][32];
     float4* cand = cand_all[threadIdx.x >> 5];
-    int* cidx = cidx_all[threadIdx.x >> 5];
+    int2* cidx = cidx_all[threadIdx.x >> 5];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = s < nf;
     const int si = active ? s : 0;
@@ -280,9 +287,9 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     int* __restrict__ err, const unsigned* __restrict__ gate) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
-    __shared__ int cidx_all[4][32];
+    __shared__ int2 cidx_all[4][32];
     float4* cand = cand_all[threadIdx.x >> 5];
-    int* cidx = cidx_all[threadIdx.x >> 5];
+    int2* cidx = cidx_all[threadIdx.x >> 5];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = s < nw;
     const int si = active ? s : 0;
