@@ -133,8 +133,9 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __res
     const float4 tw = wtest[w];
     Kahan Ps, V;
     const int n = wfc[w];
+    uint4 lq;  // the list quad holding entry k
     for (int k = 0; k < n; ++k) {
-        const unsigned e = wf[(size_t)k * nw + w];
+        const unsigned e = list_next(wf, k, nw, w, lq);
         const int b = (int)(e & kSlotMask);
         const float4 cb = ftest[b];
         float pd0, pd1, pd2;
@@ -214,8 +215,9 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
 
     Kahan a0, a1, a2, ar;
     const int nff = ffc[s];
+    uint4 lq;  // the list quad holding entry k
     for (int k = 0; k < nff; ++k) {
-        const unsigned e = ff[(size_t)k * nf + s];
+        const unsigned e = list_next(ff, k, nf, s, lq);
         const int b = (int)(e & kSlotMask);
         const float4 cb = ftest[b];  // {offsets, rho_b - rho0}
         float pd0, pd1, pd2;
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
     Kahan w0, w1, w2, wr;
     const int nfw = fwc[s];
     for (int k = 0; k < nfw; ++k) {
-        const unsigned e = fw[(size_t)k * nf + s];
+        const unsigned e = list_next(fw, k, nf, s, lq);
         const int b = (int)(e & kSlotMask);
         const float4 tb = wtest[b];  // {offsets, m_w / rho_w of the last Adami pass}
         float pd0, pd1, pd2;

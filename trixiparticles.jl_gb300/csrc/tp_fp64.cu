@@ -173,8 +173,9 @@ __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_3
     const double two_hinv = 2.0 * P.h_inv;
     double Ps = 0.0, V = 0.0;
     const int n = wfc[w];
+    uint4 lq;  // the list quad holding entry k
     for (int k = 0; k < n; ++k) {
-        const unsigned e = wf[(size_t)k * nw + w];
+        const unsigned e = list_next(wf, k, nw, w, lq);
         const int b = (int)(e & kSlotMask);
         float f0, f1, f2;
         const float d2f = pair_diff<ND>(tw, off, e, ftest[b], f0, f1, f2);
@@ -310,17 +311,16 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const f
     // bound); tested in list order
     int k = 0;
     for (; k + 4 <= cnt; k += 4) {
-        unsigned e[4];
+        const uint4 q = list_quad(list, k, n_rows, s);
+        const unsigned e[4] = {q.x, q.y, q.z, q.w};
         float4 cb[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) e[j] = list[(size_t)(k + j) * n_rows + s];
 #pragma unroll
         for (int j = 0; j < 4; ++j) cb[j] = test[e[j] & kSlotMask];
 #pragma unroll
         for (int j = 0; j < 4; ++j) test_one(e[j], cb[j]);
     }
     for (; k < cnt; ++k) {
-        const unsigned e = list[(size_t)k * n_rows + s];
+        const unsigned e = list[list_at(k, n_rows, s)];
         test_one(e, test[e & kSlotMask]);
     }
     return n;

@@ -6,9 +6,13 @@
 // as no particle has moved more than skin * h since the rebuild; the displacement check below
 // reopens the rebuild gate before that can happen (see tp_nhs.cuh for the gate).
 //
-// Layout: entry k of slot s at list[k * stride + s] (stride = number of query slots), so the 32
-// lanes of a warp read one 128-byte line per k.  An entry is the candidate slot (25 bits) and
-// the candidate's cell offset code (dx+2) + 5(dy+2) + 25(dz+2) relative to the query's cell at
+// Layout: a slot's entries come in chunks of eight, chunk q of slot s at entries
+// [(q * stride + s) * 8, + 8) (stride = number of query slots): a builder lane writes one whole
+// 32-byte sector per chunk (scattered 4-byte appends into a slot-interleaved layout cost the
+// builder 3.4x its time in partial-sector writes), and a reader lane fetches four consecutive
+// entries with one 16-byte load (a warp's quad read covers half of 32 adjacent sectors, whose
+// other halves the next quad reads).  An entry is the candidate slot (25 bits) and the
+// candidate's cell offset code (dx+2) + 5(dy+2) + 25(dz+2) relative to the query's cell at
 // build time (top 7 bits), which the FP32 form needs to form cell-relative differences.
 //
 // Cells are 2h wide (the reference's grid) and the list radius 2h (1 + skin) is larger, so a
@@ -28,6 +32,25 @@ namespace tp {
 #define TP_ERRBIT_CAPACITY 4
 
 constexpr int kSlotBits = 25;  // slot field of a list entry: at most 2^25 particles per set
+constexpr int kListChunk = 8;  // entries per chunk; list capacities are multiples of it
+
+__host__ __device__ __forceinline__ size_t list_at(int k, int stride, int s) {
+    return ((size_t)(k >> 3) * (size_t)stride + (size_t)s) * kListChunk + (size_t)(k & 7);
+}
+
+// Entries k .. k+3 of slot s (k a multiple of 4).
+__device__ __forceinline__ uint4 list_quad(const unsigned* __restrict__ list, int k, int stride,
+                                           int s) {
+    return *reinterpret_cast<const uint4*>(list + list_at(k, stride, s));
+}
+
+// Entry k of slot s from the quad q that holds it, loading the next quad when k reaches it.
+__device__ __forceinline__ unsigned list_next(const unsigned* __restrict__ list, int k,
+                                              int stride, int s, uint4& q) {
+    if ((k & 3) == 0) q = list_quad(list, k, stride, s);
+    const int r = k & 3;
+    return r == 0 ? q.x : r == 1 ? q.y : r == 2 ? q.z : q.w;
+}
 constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;
 
 // Cell offsets of the 125 entry codes times the FP32 cell size, {dx cs, dy cs, dz cs, 0} at
@@ -110,12 +133,20 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                                             const int* __restrict__ start,
                                             const int* __restrict__ skey,
                                             const float4* __restrict__ test, float r2f,
-                                            float4* cand, int2* cidx,
+                                            float4* cand, int2* cidx, unsigned* lbuf,
                                             unsigned* __restrict__ list, int stride, int cap,
                                             int s) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int cnt = 0;
+    // a lane's entries are collected in its column of the block's buffer (entry r of the open
+    // chunk at lbuf[r * blockDim.x]) and written out a whole chunk at a time
+    const int bs = blockDim.x;
+    auto flush = [&](int q) {
+        uint4* dst = reinterpret_cast<uint4*>(list + list_at(q * kListChunk, stride, s));
+        dst[0] = make_uint4(lbuf[0], lbuf[bs], lbuf[2 * bs], lbuf[3 * bs]);
+        dst[1] = make_uint4(lbuf[4 * bs], lbuf[5 * bs], lbuf[6 * bs], lbuf[7 * bs]);
+    };
     const int xl = reach_lo(oa.x, m), xh = reach_hi(oa.x, cs, m);
     const int yl = reach_lo(oa.y, m), yh = reach_hi(oa.y, cs, m);
     const int zl = (ND == 3) ? reach_lo(oa.z, m) : 0, zh = (ND == 3) ? reach_hi(oa.z, cs, m) : 0;
@@ -235,7 +266,10 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                         if (jj >= mlo && jj < mhi && d2 <= r2f) {
                             const unsigned code =
                                 rowcode + (unsigned)(jc.y - c[0] + 2);
-                            if (cnt < cap) list[(size_t)cnt * stride + s] = (unsigned)jj | (code << kSlotBits);
+                            if (cnt < cap) {
+                                lbuf[(cnt & 7) * bs] = (unsigned)jj | (code << kSlotBits);
+                                if ((cnt & 7) == 7) flush(cnt >> 3);
+                            }
                             ++cnt;
                         }
                     }
@@ -244,6 +278,8 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
             }
         }
     }
+    const int stored = min(cnt, cap);
+    if (active && (stored & 7)) flush(stored >> 3);  // the open chunk (tail entries unused)
     return cnt;
 }
 
@@ -259,8 +295,10 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
     __shared__ int2 cidx_all[4][32];
+    __shared__ unsigned lbuf_all[kListChunk][128];
     float4* cand = cand_all[threadIdx.x >> 5];
     int2* cidx = cidx_all[threadIdx.x >> 5];
+    unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = s < nf;
     const int si = active ? s : 0;
@@ -268,9 +306,9 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     int c[3];
     key_to_coords(fskey[si], g, c);
     const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
-                                    cidx, ff, nf, cap_ff, s);
+                                    cidx, lbuf, ff, nf, cap_ff, s);
     const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, cand,
-                                    cidx, fw, nf, cap_fw, s);
+                                    cidx, lbuf, fw, nf, cap_fw, s);
     if (!active) return;
     ffc[s] = min(n1, cap_ff);
     fwc[s] = min(n2, cap_fw);
@@ -288,8 +326,10 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
     __shared__ int2 cidx_all[4][32];
+    __shared__ unsigned lbuf_all[kListChunk][128];
     float4* cand = cand_all[threadIdx.x >> 5];
     int2* cidx = cidx_all[threadIdx.x >> 5];
+    unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = s < nw;
     const int si = active ? s : 0;
@@ -297,7 +337,7 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     int c[3];
     key_to_coords(wskey[si], g, c);
     const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
-                                    cidx, wf, nw, cap_wf, s);
+                                    cidx, lbuf, wf, nw, cap_wf, s);
     if (!active) return;
     wfc[s] = min(n1, cap_wf);
     if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
