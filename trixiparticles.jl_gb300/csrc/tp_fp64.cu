@@ -285,12 +285,21 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const f
                                            const float4* __restrict__ test,
                                            const double4_32a* __restrict__ pos,
                                            const unsigned* __restrict__ list,
-                                           int cnt, int skip, int* __restrict__ out) {
+                                           int cnt, int skip, unsigned* out,
+                                           unsigned* lbuf) {
     // skip: 0 keep all (walls), 1 drop self (fluid, gather mode), 2 keep the pairs that s owns
     // (fluid, symmetric mode: the owner of {s, b} is the lower slot when s + b is odd and the
     // higher one when it is even; measured on GB300 this balances the lanes better than a hashed
     // owner, whose scattered accesses cost more than its balance gains)
     int n = 0;
+    // exact list in the chunked layout of the skin lists, whole chunks written from the lane's
+    // column of the block buffer (entry r of the open chunk at lbuf[r * blockDim.x])
+    const int bs = blockDim.x;
+    auto flush = [&](int q) {
+        uint4* dst = reinterpret_cast<uint4*>(out + list_at(q * kListChunk, n_rows, s));
+        dst[0] = make_uint4(lbuf[0], lbuf[bs], lbuf[2 * bs], lbuf[3 * bs]);
+        dst[1] = make_uint4(lbuf[4 * bs], lbuf[5 * bs], lbuf[6 * bs], lbuf[7 * bs]);
+    };
     auto test_one = [&](unsigned e, const float4& cb) {
         const int b = (int)(e & kSlotMask);
         if (b == s && skip != 0) return;
@@ -305,7 +314,11 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const f
             const double d2 = dist2_rn<ND>(pa.x - pb.x, pa.y - pb.y, ND == 3 ? pa.z - pb.z : 0.0);
             acc = d2 <= sr2 && !(d2 < az2);
         }
-        if (acc) out[(size_t)(n++) * n_rows + s] = b;
+        if (acc) {
+            lbuf[(n & 7) * bs] = (unsigned)b;
+            if ((n & 7) == 7) flush(n >> 3);
+            ++n;
+        }
     };
     // four candidates' entries and records in flight at a time (the pass is gather-latency
     // bound); tested in list order
@@ -323,6 +336,7 @@ __device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const f
         const unsigned e = list[list_at(k, n_rows, s)];
         test_one(e, test[e & kSlotMask]);
     }
+    if (n & 7) flush(n >> 3);  // the open chunk (tail entries unused)
     return n;
 }
 
@@ -335,15 +349,17 @@ __global__ void __launch_bounds__(256) k_filter64(
     const float4* __restrict__ wtest, const double4_32a* __restrict__ wpos, int* __restrict__ eff,
     int* __restrict__ effc, int* __restrict__ efw, int* __restrict__ efwc, int half) {
     __shared__ float4 off[kOffsetCodes];
+    __shared__ unsigned lbuf_all[kListChunk][256];
     fill_offset_table(off, cs);
+    unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nf) return;
     const float4 ta = ftest[s];
     const double4_32a pa = fpos[s];
     effc[s] = filter_list<ND>(s, nf, ta, off, lo2, hi2, zero2, sr2, az2, pa, ftest, fpos, ff,
-                              ffc[s], half ? 2 : 1, eff);
+                              ffc[s], half ? 2 : 1, (unsigned*)eff, lbuf);
     efwc[s] = filter_list<ND>(s, nf, ta, off, lo2, hi2, zero2, sr2, az2, pa, wtest, wpos, fw,
-                              fwc[s], 0, efw);
+                              fwc[s], 0, (unsigned*)efw, lbuf);
 }
 
 // Pair terms of rhs.jl:81-117 (pressure, Monaghan viscosity, continuity, Molteni-Colagrossi
@@ -396,7 +412,9 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
                                                 const double4_32a* __restrict__ wstate,
                                                 unsigned* __restrict__ gate, Update64 U) {
     __shared__ float4 off[kOffsetCodes];
+    __shared__ unsigned lbuf_all[kListChunk][256];
     fill_offset_table(off, F.cs);
+    unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
@@ -404,17 +422,18 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     const double4_32a va = fvel[s];
     const float4 ta = F.ftest[s];
     const int nff = filter_list<ND>(s, nf, ta, off, F.lo2, F.hi2, F.zero2, P.sr2, P.az2, pa,
-                                    F.ftest, fpos, F.ff, F.ffc[s], 1, F.eff);
+                                    F.ftest, fpos, F.ff, F.ffc[s], 1, (unsigned*)F.eff, lbuf);
     const int nfw = filter_list<ND>(s, nf, ta, off, F.lo2, F.hi2, F.zero2, P.sr2, P.az2, pa,
-                                    F.wtest, wpos, F.fw, F.fwc[s], 0, F.efw);
-    const int* eff = F.eff;
-    const int* efw = F.efw;
+                                    F.wtest, wpos, F.fw, F.fwc[s], 0, (unsigned*)F.efw, lbuf);
+    const unsigned* eff = (const unsigned*)F.eff;
+    const unsigned* efw = (const unsigned*)F.efw;
+    uint4 lq;  // the exact-list quad holding entry k
     const double p_a = pa.w, rho_a = va.w, nia = -fast_inv(rho_a);  // the pack's 1 / rho
 
     // ---- fluid-fluid ----
     double dv0 = 0.0, dv1 = 0.0, dv2 = 0.0, drho = 0.0;
     for (int k = 0; k < nff; ++k) {
-        const int b = eff[(size_t)k * nf + s];
+        const int b = (int)list_next_rw(eff, k, nf, s, lq);
         const double4_32a pb = fpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
@@ -444,7 +463,7 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
     // ---- fluid-wall (wall viscosity = nothing, no density diffusion, wall velocity 0) ----
     double ew0 = 0.0, ew1 = 0.0, ew2 = 0.0, erho = 0.0;
     for (int k = 0; k < nfw; ++k) {
-        const int b = efw[(size_t)k * nf + s];
+        const int b = (int)list_next_rw(efw, k, nf, s, lq);
         const double4_32a pb = wpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
@@ -506,7 +525,7 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
     int k = (int)(((unsigned)(threadIdx.x & 31) * (unsigned)nff) >> 5);
     for (int it = 0; it < nff; ++it, ++k) {
         if (k == nff) k = 0;
-        const int b = eff[(size_t)k * nf + s];
+        const int b = eff[list_at(k, nf, s)];
         const double4_32a pb = fpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
@@ -563,7 +582,7 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
 
     const int nfw = efwc[s];
     for (int kw = 0; kw < nfw; ++kw) {
-        const int b = efw[(size_t)kw * nf + s];
+        const int b = efw[list_at(kw, nf, s)];
         const double4_32a pb = wpos[b];
         const double pd0 = pa.x - pb.x, pd1 = pa.y - pb.y;
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;

@@ -44,6 +44,15 @@ __device__ __forceinline__ uint4 list_quad(const unsigned* __restrict__ list, in
     return *reinterpret_cast<const uint4*>(list + list_at(k, stride, s));
 }
 
+// The same for a list written earlier in the same kernel by the reading thread (the exact pair
+// lists of the fused FP64 pass): plain loads, never the read-only data path.
+__device__ __forceinline__ unsigned list_next_rw(const unsigned* list, int k, int stride, int s,
+                                                 uint4& q) {
+    if ((k & 3) == 0) q = *reinterpret_cast<const uint4*>(list + list_at(k, stride, s));
+    const int r = k & 3;
+    return r == 0 ? q.x : r == 1 ? q.y : r == 2 ? q.z : q.w;
+}
+
 // Entry k of slot s from the quad q that holds it, loading the next quad when k reaches it.
 __device__ __forceinline__ unsigned list_next(const unsigned* __restrict__ list, int k,
                                               int stride, int s, uint4& q) {
