@@ -77,7 +77,7 @@ struct tp_handle {
     float* w_p32 = nullptr;   // FP32: wall pressure of the last Adami pass (dense, for gathers)
     double* w_vol = nullptr;
 
-    // ---- neighbour lists (tp_lists.cuh): entry k of slot s at list[k * n + s] ----
+    // ---- neighbour lists (tp_lists.cuh): entry k of slot s at list_at(k, n, s), chunks of 8 ----
     unsigned* l_ff = nullptr;  // fluid -> fluid candidates
     unsigned* l_fw = nullptr;  // fluid -> wall
     unsigned* l_wf = nullptr;  // wall -> fluid (Adami)
@@ -86,7 +86,8 @@ struct tp_handle {
     int* c_wf = nullptr;
     int cap_ff = 0, cap_fw = 0, cap_wf = 0;
     // FP64 form: the exact pair lists of the current stage (|x_a - x_b| <= 2h, self excluded),
-    // filtered from l_ff / l_fw before every pair pass; plain slot indices, same layout
+    // filtered from l_ff / l_fw at the start of every pair pass; plain slot indices, same layout
+    // (ec_ff / ec_fw: their counts, kept by the separate filter pass of the symmetric mode)
     int* e_ff = nullptr;
     int* e_fw = nullptr;
     int* ec_ff = nullptr;
