@@ -187,9 +187,10 @@ struct Update32 {
 // pressure + viscosity, continuity through sg (v_ab . x_ab), diffusion as 2 (rho_a - rho_b) sg,
 // one reciprocal for the Monaghan mu / rho_mean), in FP32 on the cell-relative differences, with
 // Kahan-compensated per-particle sums.
-// Five 256-thread blocks per SM cap the kernel at 48 registers without spills: the pass is bound
-// by the latency of its neighbour gathers, and the extra resident warps (66 % occupancy instead
-// of 53 %) hide more of it (measured 3.05 -> 2.85 ms per launch at dx = 0.0064 in 3D).
+// Five 256-thread blocks per SM cap the kernel at 48 registers: the pass is bound by the L1 data
+// pipe serving its neighbour gathers and by their latency, and the extra resident warps (66 %
+// occupancy instead of 53 % at 56 registers) hide more of it (8 % faster at dx = 0.0064 in 3D).
+// The list is read four entries per 16-byte load (the chunked layout of tp_lists.cuh).
 template <int ND, bool INTEGRATE>
 __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
