@@ -176,11 +176,13 @@ __global__ void k_gather_load(const int* __restrict__ id, const double* __restri
     }
 }
 
+// Rebuild gate {forced, largest squared displacement, squared threshold} for a displacement
+// threshold (skin * h); k_displacement fills gate[1].
 __global__ void k_gate_init(unsigned* __restrict__ gate, float threshold, int force) {
     if (threadIdx.x == 0) {
         gate[0] = force ? 1u : 0u;
         gate[1] = 0u;
-        gate[2] = __float_as_uint(threshold);
+        gate[2] = __float_as_uint((threshold * threshold) * (1.0f - 1e-5f));
     }
 }
 

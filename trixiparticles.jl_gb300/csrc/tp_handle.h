@@ -100,7 +100,7 @@ struct tp_handle {
     // GB300 in both forms, at rest and in a 3 m/s flow (shorter lists outweigh the rebuilds).
     double skin = 0.05;
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
-    unsigned* gate = nullptr;   // {force, max displacement bits, half-skin bits}
+    unsigned* gate = nullptr;   // {force, max squared displacement bits, squared threshold bits}
     int* d_max = nullptr;       // scratch for the largest cell occupancy
     int maxcell_w = 0;          // largest wall cell occupancy (walls are static)
     bool lists_fixed = false;   // capacity fixed by tp_prepare_lists (no sizing sync per call)

@@ -98,7 +98,11 @@ __device__ __forceinline__ float pair_diff(float4 ta, const float4* tab, unsigne
     return d2;
 }
 
-// Largest displacement since the last rebuild -> gate[1] (float bits, atomicMax on unsigned).
+// Largest squared displacement since the last rebuild -> gate[1] (float bits, atomicMax on
+// unsigned), compared with the squared threshold in gate[2].  Only the differences are FP64 (the
+// positions are); squares and sum are FP32 and there is no square root: the pass was bound by
+// the FP64 pipe (sqrt of the FP64 distance).  The threshold is lowered by 1e-5 relative to cover
+// the FP32 rounding, so a rebuild never comes later than the exact test would have it.
 // `perm` (optional): slot -> index into u (caller-ordered positions of the kick! path).
 template <int ND>
 __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__ u,
@@ -106,21 +110,19 @@ __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__
                                                       unsigned* __restrict__ gate,
                                                       const int* __restrict__ perm = nullptr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    float d = 0.0f;
+    float d2 = 0.0f;
     if (s < n) {
         const int i = perm ? perm[s] : s;
-        double d2 = 0.0;
 #pragma unroll
         for (int k = 0; k < ND; ++k) {
-            const double e = u[(size_t)i * ND + k] - xb[(size_t)s * ND + k];
-            d2 += e * e;
+            const float e = (float)(u[(size_t)i * ND + k] - xb[(size_t)s * ND + k]);
+            d2 = fmaf(e, e, d2);
         }
-        d = (float)sqrt(d2);
-        if (!(d == d)) d = 3.0e38f;  // NaN positions force a rebuild (and are reported there)
+        if (!(d2 == d2)) d2 = 3.0e38f;  // NaN positions force a rebuild (and are reported there)
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, off));
-    if ((threadIdx.x & 31) == 0 && d > 0.0f) atomicMax(&gate[1], __float_as_uint(d));
+    for (int off = 16; off > 0; off >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, off));
+    if ((threadIdx.x & 31) == 0 && d2 > 0.0f) atomicMax(&gate[1], __float_as_uint(d2));
 }
 
 // Warp-cooperative candidate search: lanes are grouped by their (cy, cz) row; for each searched
