@@ -544,6 +544,7 @@ tp_status ensure_lists(tp_handle* h, const double* u) {
     if (h->cfg.precision == TP_PRECISION_FP64) {
         TP_CUDA(h, grow((unsigned**)&h->e_ff, &h->ecap_ff, cff, nf));
         TP_CUDA(h, grow((unsigned**)&h->e_fw, &h->ecap_fw, cfw, nf));
+        TP_CUDA(h, grow((unsigned**)&h->e_wf, &h->ecap_wf, cwf, nw));
         if (!h->ec_ff) TP_CUDA(h, dalloc(&h->ec_ff, (size_t)std::max(nf, 1)));
         if (!h->ec_fw) TP_CUDA(h, dalloc(&h->ec_fw, (size_t)std::max(nf, 1)));
         if (!h->acc) {
@@ -869,7 +870,7 @@ tp_status tp_destroy(tp_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
-                    h->d_max, h->e_ff, h->e_fw, h->ec_ff, h->ec_fw, h->acc, h->spv};
+                    h->d_max, h->e_ff, h->e_fw, h->e_wf, h->ec_ff, h->ec_fw, h->acc, h->spv};
     for (void* p : more)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {

@@ -144,87 +144,6 @@ struct PackWall64 {
 // Adami pressure extrapolation (dummy_particles.jl:489-569, 586-606, 637-672): one lane per
 // wall slot gathers its fluid neighbours in PointNeighbors order.
 // ------------------------------------------------------------------------------------------
-// The support test is decided like the exact-list filter: an FP32 distance on the cell-relative
-// offsets outside a 1e-5 band around (2h)^2, the explicitly rounded FP64 distance inside it, so
-// the accepted pairs are the CPU's; the FP64 distance of an accepted pair is then formed with FMAs.
-// FOLD (gather pair mode): the fluid records carry A_f = p_off + p_f - rho_f g.x_f, so the sum
-// term p_off + p_f + g.(rho_f (x_w - x_f)) is fma(rho_f, g.x_w, A_f), and the kernel's norm is
-// applied once to the sums (their ratio does not depend on it).
-template <int ND, bool FOLD>
-__global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
-                                                 const float4* __restrict__ wtest,
-                                                 const unsigned* __restrict__ wf,
-                                                 const int* __restrict__ wfc,
-                                                 double4_32a* __restrict__ wstate,
-                                                 double* __restrict__ wvol,
-                                                 const double4_32a* __restrict__ fpos,
-                                                 const double4_32a* __restrict__ fvel,
-                                                 const double4_32a* __restrict__ faux,
-                                                 const float4* __restrict__ ftest, float cs,
-                                                 float lo2, float hi2) {
-    __shared__ float4 off[kOffsetCodes];
-    fill_offset_table(off, cs);
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nw) return;
-    const double4_32a xw = wpos[w];
-    const float4 tw = wtest[w];
-    double gxw = P.g[0] * xw.x + P.g[1] * xw.y;
-    if (ND == 3) gxw += P.g[2] * xw.z;
-    const double two_hinv = 2.0 * P.h_inv;
-    double Ps = 0.0, V = 0.0;
-    const int n = wfc[w];
-    uint4 lq;  // the list quad holding entry k
-    for (int k = 0; k < n; ++k) {
-        const unsigned e = list_next(wf, k, nw, w, lq);
-        const int b = (int)(e & kSlotMask);
-        float f0, f1, f2;
-        const float d2f = pair_diff<ND>(tw, off, e, ftest[b], f0, f1, f2);
-        if (d2f > hi2) continue;
-        const double4_32a xb = fpos[b];
-        const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
-        const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
-        if (d2f > lo2 && dist2_rn<ND>(pd0, pd1, pd2) > P.sr2) continue;  // the CPU's test
-        double d2 = pd0 * pd0 + pd1 * pd1;
-        if (ND == 3) d2 += pd2 * pd2;
-        const double r = d2 > 0.0 ? d2 * rsqrt(d2) : 0.0;
-        const double rho_f = fvel[b].w;
-        double sum;
-        if (FOLD) {
-            sum = fma(rho_f, gxw, faux[b].z);
-        } else {
-            double hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
-            if (ND == 3) hp += P.g[2] * (rho_f * pd2);
-            sum = (P.p_off + xb.w) + hp;
-        }
-        double W = 0.0;
-        if (r < P.two_h) {  // (1 - q/2)^4 (2q + 1), q = r / h
-            const double t = fma(-r, P.half_hinv, 1.0);
-            const double t2 = t * t;
-            W = FOLD ? (t2 * t2) * fma(r, two_hinv, 1.0)
-                     : (P.wc2_norm * (t2 * t2)) * fma(r, two_hinv, 1.0);
-        }
-        Ps = fma(sum, W, Ps);
-        V += W;
-    }
-    if (FOLD) {
-        const double Vn = P.wc2_norm * V;
-        Ps = Vn > 2.220446049250313e-16 ? Ps / V : P.wc2_norm * Ps;
-        V = Vn;
-    } else if (V > 2.220446049250313e-16) {
-        Ps = Ps / V;
-    }
-    if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
-    const double rho_w = eos_inverse(Ps, P);
-    const double ir_w = fast_inv(rho_w);
-    if (FOLD) {
-        const double S = P.sg_c * (xw.w * ir_w);
-        wstate[w] = make_double4_32a(Ps, rho_w, Ps * S, S);  // {p, rho, p S, S = sg_c m/rho}
-    } else {
-        wstate[w] = make_double4_32a(Ps, rho_w, ir_w, xw.w * ir_w);  // {p, rho, 1/rho, m/rho}
-    }
-    wvol[w] = V;
-}
-
 // ------------------------------------------------------------------------------------------
 // Fused fluid pair kernel: fluid-fluid then fluid-wall interactions of one fluid slot
 // (weakly_compressible_sph/rhs.jl:30-124), plus gravity (semidiscretization.jl:701-731), then
@@ -385,6 +304,90 @@ __device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a
     const double mu = (P.visc_h * vr) * (rho_sum * R);
     return ((ab.y * rho_b) * mu) * (P.alpha_c + P.beta * mu) * (2.0 * den * R);
 }
+
+// The support test is the exact-list filter's (FP32 on the cell-relative offsets outside a 1e-5
+// band around (2h)^2, the CPU's explicitly rounded FP64 test inside it), run first over the whole
+// skin list: the accepted fluid neighbours are compacted into the wall's exact list (chunked
+// layout, written and read back by the same thread) and the FP64 loop walks only those, so the
+// lanes of a warp stay busy on the FP64 pipe (wall particles deep in the wall layers have few
+// fluid neighbours).  Distances of accepted pairs are formed with FMAs.
+// FOLD (gather pair mode): the fluid records carry A_f = p_off + p_f - rho_f g.x_f, so the sum
+// term p_off + p_f + g.(rho_f (x_w - x_f)) is fma(rho_f, g.x_w, A_f), and the kernel's norm is
+// applied once to the sums (their ratio does not depend on it).
+template <int ND, bool FOLD>
+__global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
+                                                 const float4* __restrict__ wtest,
+                                                 const unsigned* __restrict__ wf,
+                                                 const int* __restrict__ wfc,
+                                                 double4_32a* __restrict__ wstate,
+                                                 double* __restrict__ wvol,
+                                                 const double4_32a* __restrict__ fpos,
+                                                 const double4_32a* __restrict__ fvel,
+                                                 const double4_32a* __restrict__ faux,
+                                                 const float4* __restrict__ ftest, float cs,
+                                                 float lo2, float hi2, unsigned* ewf) {
+    __shared__ float4 off[kOffsetCodes];
+    __shared__ unsigned lbuf_all[kListChunk][256];
+    fill_offset_table(off, cs);
+    unsigned* lbuf = &lbuf_all[0][threadIdx.x];
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    const double4_32a xw = wpos[w];
+    const float4 tw = wtest[w];
+    // exact list of the wall: d^2 <= (2h)^2, zero distance included (no skip in the Adami sum)
+    const int n = filter_list<ND>(w, nw, tw, off, lo2, hi2, -1.0f, P.sr2, -1.0, xw, ftest, fpos,
+                                  wf, wfc[w], 0, ewf, lbuf);
+    double gxw = P.g[0] * xw.x + P.g[1] * xw.y;
+    if (ND == 3) gxw += P.g[2] * xw.z;
+    const double two_hinv = 2.0 * P.h_inv;
+    double Ps = 0.0, V = 0.0;
+    uint4 lq;  // the exact-list quad holding entry k
+    for (int k = 0; k < n; ++k) {
+        const int b = (int)list_next_rw(ewf, k, nw, w, lq);
+        const double4_32a xb = fpos[b];
+        const double pd0 = xw.x - xb.x, pd1 = xw.y - xb.y;
+        const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
+        double d2 = pd0 * pd0 + pd1 * pd1;
+        if (ND == 3) d2 += pd2 * pd2;
+        const double r = d2 > 0.0 ? d2 * rsqrt(d2) : 0.0;
+        const double rho_f = fvel[b].w;
+        double sum;
+        if (FOLD) {
+            sum = fma(rho_f, gxw, faux[b].z);
+        } else {
+            double hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
+            if (ND == 3) hp += P.g[2] * (rho_f * pd2);
+            sum = (P.p_off + xb.w) + hp;
+        }
+        double W = 0.0;
+        if (r < P.two_h) {  // (1 - q/2)^4 (2q + 1), q = r / h
+            const double t = fma(-r, P.half_hinv, 1.0);
+            const double t2 = t * t;
+            W = FOLD ? (t2 * t2) * fma(r, two_hinv, 1.0)
+                     : (P.wc2_norm * (t2 * t2)) * fma(r, two_hinv, 1.0);
+        }
+        Ps = fma(sum, W, Ps);
+        V += W;
+    }
+    if (FOLD) {
+        const double Vn = P.wc2_norm * V;
+        Ps = Vn > 2.220446049250313e-16 ? Ps / V : P.wc2_norm * Ps;
+        V = Vn;
+    } else if (V > 2.220446049250313e-16) {
+        Ps = Ps / V;
+    }
+    if (P.wall_clip) Ps = (Ps != Ps || Ps > 0.0) ? Ps : 0.0;
+    const double rho_w = eos_inverse(Ps, P);
+    const double ir_w = fast_inv(rho_w);
+    if (FOLD) {
+        const double S = P.sg_c * (xw.w * ir_w);
+        wstate[w] = make_double4_32a(Ps, rho_w, Ps * S, S);  // {p, rho, p S, S = sg_c m/rho}
+    } else {
+        wstate[w] = make_double4_32a(Ps, rho_w, ir_w, xw.w * ir_w);  // {p, rho, 1/rho, m/rho}
+    }
+    wvol[w] = V;
+}
+
 
 // Skin lists in, exact lists of this stage out (the filter fused into the gather pair kernel).
 struct Filter64 {
@@ -741,7 +744,8 @@ void fp64_adami(tp_handle* h) {
                                                  h->stream>>>(
             h->phys, nw, (const double4_32a*)h->w_pos, h->w_test, h->l_wf, h->c_wf,
             (double4_32a*)h->w_state, h->w_vol, (const double4_32a*)h->f_pos,
-            (const double4_32a*)h->f_vel, (const double4_32a*)h->f_aux, h->f_test, cs, lo2, hi2);
+            (const double4_32a*)h->f_vel, (const double4_32a*)h->f_aux, h->f_test, cs, lo2, hi2,
+            (unsigned*)h->e_wf);
     };
     if (h->cfg.ndims == 2) {
         if (fold) run(std::integral_constant<int, 2>{}, std::true_type{});

@@ -90,9 +90,10 @@ struct tp_handle {
     // (ec_ff / ec_fw: their counts, kept by the separate filter pass of the symmetric mode)
     int* e_ff = nullptr;
     int* e_fw = nullptr;
+    int* e_wf = nullptr;  // the walls' exact fluid lists of the Adami pass (FP64 form)
     int* ec_ff = nullptr;
     int* ec_fw = nullptr;
-    int ecap_ff = 0, ecap_fw = 0;
+    int ecap_ff = 0, ecap_fw = 0, ecap_wf = 0;
     // FP64 form, symmetric pair mode: per-slot accumulator {dv (3), drho} of the pair pass
     double* acc = nullptr;
     int pair_mode = 0;  // TP_PAIR_GATHER (default) or TP_PAIR_SYMMETRIC
