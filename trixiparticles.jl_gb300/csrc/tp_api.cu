@@ -351,6 +351,8 @@ void setup_phys(tp_handle* h) {
     P.rho0 = c.reference_density;
     P.c = c.sound_speed;
     P.gamma = c.exponent;
+    P.gamma_int = (c.exponent >= 1.0 && c.exponent <= 16.0 && c.exponent == std::floor(c.exponent))
+                      ? (int)c.exponent : 0;
     P.p_bg = c.background_pressure;
     P.B = (P.rho0 * (P.c * P.c)) / P.gamma;
     P.inv_gamma = 1.0 / P.gamma;

@@ -48,6 +48,7 @@ struct Phys {
     double wc2_dnorm;  // -5 * wc2_norm (kernel_deriv_div_r_unsafe prefactor)
     double hi2;        // h_inv * h_inv
     double rho0, c, gamma, p_bg, B, inv_gamma;
+    int gamma_int;     // the exponent when it is an integer in [1, 16], else 0
     int fluid_clip, wall_clip;
     int visc;
     double alpha, beta, eps_visc;
@@ -123,9 +124,25 @@ __device__ __forceinline__ void key_to_coords(int key, const GridDesc& g, int c[
     c[2] = r / g.n[1];
 }
 
-// StateEquationCole pressure (state_equations.jl:117-129), FP64.
+// x^n for a small positive integer n by squaring (x^7: four multiplications, a few ulp of the
+// correctly rounded power).  FP64 runs at 1/64 of the FP32 rate on this GPU, and pow's
+// logarithm and exponential cost tens of FP64 instructions per call.
+__device__ __forceinline__ double ipow(double x, int n) {
+    double r = 1.0, b = x;
+    while (n) {
+        if (n & 1) r *= b;
+        n >>= 1;
+        if (n) b *= b;
+    }
+    return r;
+}
+
+// StateEquationCole pressure (state_equations.jl:117-129), FP64; an integer exponent (the usual
+// 7) by repeated multiplication.
 __device__ __forceinline__ double eos_pressure(double rho, const Phys& P, int clip) {
-    double p = P.B * (pow(rho / P.rho0, P.gamma) - 1.0) + P.p_bg;
+    const double x = rho / P.rho0;
+    const double xg = P.gamma_int ? ipow(x, P.gamma_int) : pow(x, P.gamma);
+    double p = P.B * (xg - 1.0) + P.p_bg;
     if (clip) p = (p != p || p > 0.0) ? p : 0.0;
     return p;
 }
