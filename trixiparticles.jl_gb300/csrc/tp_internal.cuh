@@ -147,10 +147,20 @@ __device__ __forceinline__ double eos_pressure(double rho, const Phys& P, int cl
     return p;
 }
 
-// inverse_state_equation (state_equations.jl:131-139), FP64.
+// a^(1/n) for a > 0 and a small positive integer n: an FP32 seed and two Newton steps
+// y <- y + y (a / y^n - 1) / n in FP64 (the error squares from 1e-7 to rounding level, a few ulp
+// of the correctly rounded root), a third of FP64 pow's cost; a = y^n exactly stays exact.
+__device__ __forceinline__ double iroot(double a, int n) {
+    double y = (double)powf((float)a, 1.0f / (float)n);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) y = fma(y, (a / ipow(y, n) - 1.0) / (double)n, y);
+    return y;
+}
+
+// inverse_state_equation (state_equations.jl:131-139), FP64; an integer exponent by iroot.
 __device__ __forceinline__ double eos_inverse(double p, const Phys& P) {
     double tmp = (p - P.p_bg) / P.B + 1.0;
-    return P.rho0 * pow(tmp, P.inv_gamma);
+    return P.rho0 * (P.gamma_int && tmp > 0.0 ? iroot(tmp, P.gamma_int) : pow(tmp, P.inv_gamma));
 }
 
 }  // namespace tp
