@@ -517,6 +517,41 @@ def run_profile_form(args):
     return 0
 
 
+def run_profile_ensemble(args, n_instances=512, seed=0, steps_per_replay=5):
+    """Profiling mode of the batching form: the 512-instance ensemble with the library's default
+    launch shape and skin (no autotuning trials), one warm-up replay of the CUDA graph and then
+    `--steps` replays; one summary line.  Used under ncu for the launch list of the graph."""
+    import torch
+
+    import __graft_entry__ as g
+
+    pkg = g.load_package()
+    pkg.load_library()
+    e = pkg.ensemble
+    groups = e.build_ensemble(e.ensemble_specs(n_instances, seed))
+    eg = e.EnsembleGraph(groups, steps_per_replay)
+    eg.reset()
+    eg.replay()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launch = torch.cuda.current_stream()
+    ev0.record(launch)
+    for _ in range(max(1, args.steps)):
+        eg.replay()
+    ev1.record(launch)
+    torch.cuda.synchronize()
+    eg.check()
+    steps = max(1, args.steps) * steps_per_replay
+    ms = ev0.elapsed_time(ev1)
+    print(json.dumps({"profile_ensemble": n_instances, "particles": eg.n_particles,
+                      "groups": [{"dx": gr.dx, "particles": gr.n_particles} for gr in groups],
+                      "steps": steps, "ms_per_step": ms / steps,
+                      "value": eg.n_particles * steps / (ms / 1e3)}), flush=True)
+    for gr in groups:
+        gr.semi.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -532,6 +567,9 @@ def main():
     ap.add_argument("--profile-form", default=None, metavar="PRECISION:WORKLOAD",
                     help="profiling mode (e.g. float32:cfg2): only warm-up + timed steps of that "
                          "form, one summary line; used under ncu")
+    ap.add_argument("--profile-ensemble", action="store_true",
+                    help="profiling mode of the batching form: default launch shape, one warm-up "
+                         "replay and --steps replays of the ensemble graph; used under ncu")
     ap.add_argument("--pair-mode", type=int, default=None, choices=[0, 1],
                     help="FP64 pair pass of --profile-form: 0 gather, 1 symmetric")
     ap.add_argument("--precision-study", action="store_true",
@@ -551,6 +589,8 @@ def main():
         return 0
     if args.profile_form:
         return run_profile_form(args)
+    if args.profile_ensemble:
+        return run_profile_ensemble(args)
 
     import torch
 
