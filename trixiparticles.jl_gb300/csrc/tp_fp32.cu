@@ -191,7 +191,10 @@ struct Update32 {
 // pipe serving its neighbour gathers and by their latency, and the extra resident warps (66 %
 // occupancy instead of 53 % at 56 registers) hide more of it (8 % faster at dx = 0.0064 in 3D).
 // The list is read four entries per 16-byte load (the chunked layout of tp_lists.cuh).
-template <int ND, bool INTEGRATE>
+// STD: the configuration of the dam-break setups (Monaghan viscosity with beta = 0, Molteni-
+// Colagrossi diffusion) with the model switches resolved at compile time; the pass is issue
+// bound, and the per-pair tests of the runtime switches are instructions of their own.
+template <int ND, bool INTEGRATE, bool STD>
 __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float* __restrict__ fpres,
@@ -235,13 +238,13 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
         float vr = vd0 * pd0 + vd1 * pd1;
         if (ND == 3) vr += vd2 * pd2;
         float c = -(vol_b * ia) * (p_a + p_b);
-        if (P.visc && vr < 0.0f) {
+        if ((STD || P.visc) && vr < 0.0f) {
             const float rho_b = P.rho0 + cb.w;
             const float m_b = vol_b * rho_b;
             const float den = d2 + P.visc_eps_h2;
             const float rm = 0.5f * (rho_a + rho_b);
             const float R = __fdividef(1.0f, den * rm);
-            if (P.beta == 0.0f) {
+            if (STD || P.beta == 0.0f) {
                 c += (m_b * P.visc_k) * vr * R;
             } else {
                 const float mu = (P.visc_h * vr) * (rm * R);
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float
         a1.add(c * pd1);
         if (ND == 3) a2.add(c * pd2);
         float er = (rho_a * vol_b) * (sg * vr);
-        if (P.diff) er += (vol_b * (drho_a - cb.w)) * (sg * P.diff2);
+        if (STD || P.diff) er += (vol_b * (drho_a - cb.w)) * (sg * P.diff2);
         ar.add(er);
     }
 
@@ -392,9 +395,18 @@ void fp32_adami(tp_handle* h) {
 template <int ND, bool INTEG>
 static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
     const int nf = (int)h->cfg.n_fluid;
-    k_pair32<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
-        h->phys32, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux, h->l_ff,
-        h->c_ff, h->l_fw, h->c_fw, h->w_test, h->w_p32, gate, U);
+    const Phys32& P = h->phys32;
+    const bool std_cfg = P.visc && P.beta == 0.0f && P.diff;
+    auto run = [&](auto stdc) {
+        k_pair32<ND, INTEG, decltype(stdc)::value><<<nblk(nf, h->pair_block), h->pair_block, 0,
+                                                     h->stream>>>(
+            P, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux, h->l_ff, h->c_ff,
+            h->l_fw, h->c_fw, h->w_test, h->w_p32, gate, U);
+    };
+    if (std_cfg)
+        run(std::true_type{});
+    else
+        run(std::false_type{});
 }
 
 void fp32_pair_kick(tp_handle* h, double* dv) {
