@@ -5,9 +5,10 @@ candidates against the group's bounding box, reaches a second cell along an axis
 near a cell face, and writes each slot's list in eight-entry chunks.  The dam-break tests place
 particles on a (jittered) lattice; here the fluid is a dense clump (half the lattice spacing), a
 sparse random scatter (cells with zero to a few particles, so a warp's lanes span many cells)
-and particles pinned within 0.02 h of cell faces, with random velocities.  One kick and a few
-fused CarpenterKennedy2N54 steps must match the oracle, which searches exactly at every stage:
-a missed or misplaced list entry shows as an O(1) error.
+and particles pinned within 0.02 h of cell faces, with random velocities.  One kick (both FP64
+pair modes and the FP32 form), a few fused CarpenterKennedy2N54 steps and a few
+SymplecticPositionVerlet steps (the kick! path with list reuse) must match the oracle, which
+searches exactly at every stage: a missed or misplaced list entry shows as an O(1) error.
 """
 import ctypes
 
@@ -59,11 +60,13 @@ def _uneven_case(pkg, nd, precision, seed):
 
 
 @pytest.mark.parametrize("nd", [2, 3])
-@pytest.mark.parametrize("precision", ["float64", "float32"])
-def test_uneven_kick_matches_oracle(pkg, orc, cuda, nd, precision):
+@pytest.mark.parametrize("precision,pair_mode", [("float64", 0), ("float64", 1), ("float32", 0)],
+                         ids=["fp64-gather", "fp64-symmetric", "fp32"])
+def test_uneven_kick_matches_oracle(pkg, orc, cuda, nd, precision, pair_mode):
     torch = cuda
     semi, tank, v, u = _uneven_case(pkg, nd, precision, seed=21 + nd)
     ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    semi._call("tp_set_pair_mode", pair_mode)
     v_t = torch.as_tensor(v.ravel(), device=semi.device)
     u_t = torch.as_tensor(u.ravel(), device=semi.device)
     dv = torch.full_like(v_t, float("nan"))
@@ -103,4 +106,32 @@ def test_uneven_integration_matches_oracle(pkg, orc, cuda, nd):
     ug = u_t.view(-1, nd).cpu().numpy()
     assert rel_l2(ug, u_ref.reshape(-1, nd)) <= 1e-12
     assert rel_l2(vg, v_ref.reshape(-1, nd + 1)) <= 1e-9
+    semi.close()
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_uneven_spv_matches_oracle(pkg, orc, cuda, nd):
+    """SymplecticPositionVerlet: two kicks per step through the kick! path, whose lists are
+    reused across kicks (records refreshed through the last permutation) and rebuilt on
+    displacement."""
+    torch = cuda
+    semi, tank, v, u = _uneven_case(pkg, nd, "float64", seed=41 + nd)
+    pkg.semidiscretize(semi, (0.0, 1.0))
+    dt, n = 2e-4, 8
+    v_t = torch.as_tensor(v.ravel(), device=semi.device).contiguous()
+    u_t = torch.as_tensor(u.ravel(), device=semi.device).contiguous()
+    semi._call("tp_integrate_spv", v_t.data_ptr(), u_t.data_ptr(), ctypes.c_double(0.0),
+               ctypes.c_double(dt), ctypes.c_int64(n))
+    semi.sync()
+    model = oracle_model(orc, semi, tank)
+    v_ref, u_ref, st = model.integrate_spv(v, u, dt, n)
+    assert st == 0
+    vg = v_t.view(-1, nd + 1).cpu().numpy()
+    ug = u_t.view(-1, nd).cpu().numpy()
+    vr = v_ref.reshape(-1, nd + 1)
+    assert rel_l2(ug, u_ref.reshape(-1, nd)) <= 1e-12
+    assert rel_l2(vg[:, :nd], vr[:, :nd]) <= 1e-9
+    # the clump's large density rates and the scheme's multiplicative density update amplify the
+    # ulp-level differences (FMA contraction, the EOS power) to ~2e-12; a list error is O(1)
+    assert rel_l2(vg[:, nd], vr[:, nd]) <= 1e-11
     semi.close()
