@@ -195,7 +195,8 @@ struct Update32 {
 // Colagrossi diffusion) with the model switches resolved at compile time; the pass is issue
 // bound, and the per-pair tests of the runtime switches are instructions of their own.
 template <int ND, bool INTEGRATE, bool STD>
-__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf, const float4* __restrict__ ftest,
+__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
+                                                const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float* __restrict__ fpres,
                                                 const unsigned* __restrict__ ff,

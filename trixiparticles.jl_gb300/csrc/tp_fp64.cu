@@ -198,9 +198,9 @@ __device__ __forceinline__ void stage_update(int s, const double4_32a& pa, const
 // arithmetic runs at 1/64 of the FP32 rate on this GPU, so removing the ~25 % of listed
 // candidates that lie in the skin shell from the FP64 pair loop is worth an extra pass.
 template <int ND>
-__device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const float4* off, float lo2,
-                                           float hi2, float zero2, double sr2, double az2,
-                                           const double4_32a& pa,
+__device__ __forceinline__ int filter_list(int s, int n_rows, float4 ta, const float4* off,
+                                           float lo2, float hi2, float zero2, double sr2,
+                                           double az2, const double4_32a& pa,
                                            const float4* __restrict__ test,
                                            const double4_32a* __restrict__ pos,
                                            const unsigned* __restrict__ list,
@@ -315,7 +315,8 @@ __device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a
 // term p_off + p_f + g.(rho_f (x_w - x_f)) is fma(rho_f, g.x_w, A_f), and the kernel's norm is
 // applied once to the sums (their ratio does not depend on it).
 template <int ND, bool FOLD>
-__global__ void __launch_bounds__(256) k_adami64(Phys P, int nw, const double4_32a* __restrict__ wpos,
+__global__ void __launch_bounds__(256) k_adami64(Phys P, int nw,
+                                                 const double4_32a* __restrict__ wpos,
                                                  const float4* __restrict__ wtest,
                                                  const unsigned* __restrict__ wf,
                                                  const int* __restrict__ wfc,

@@ -73,7 +73,8 @@ struct tp_handle {
     int* w_start = nullptr;  // ncells + 1
     void* w_pos = nullptr;    // double4 {x, y, z, m} (both forms)
     float4* w_test = nullptr; // {ox, oy, oz, w}: w = x cell (FP64) or m / rho (FP32, Adami)
-    void* w_state = nullptr;  // FP64: double4 (see the Adami pass); FP32: float4 {p, rho-rho0, m, m/rho}
+    // FP64: double4 (see the Adami pass); FP32: float4 {p, rho - rho0, m, m / rho}
+    void* w_state = nullptr;
     float* w_p32 = nullptr;   // FP32: wall pressure of the last Adami pass (dense, for gathers)
     double* w_vol = nullptr;
 

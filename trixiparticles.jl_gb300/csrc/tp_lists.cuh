@@ -180,22 +180,31 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
         // cx >= cx0 (slot order), offsets are clamped at 0 so that float bits order as ints
         const float ax = fmaxf(xlane, 0.0f);
         const float ay = fmaxf(oa.y, 0.0f), az = fmaxf(oa.z, 0.0f);
-        const float bx0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(ax) : INT_MAX)) - margin;
-        const float bx1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(ax) : 0)) + margin;
-        const float by0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(ay) : INT_MAX)) - margin;
-        const float by1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(ay) : 0)) + margin;
+        // min / max over the group's lanes of non-negative floats, as ints
+        auto gmin = [&](float x) {
+            return __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(x) : INT_MAX));
+        };
+        auto gmax = [&](float x) {
+            return __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(x) : 0));
+        };
+        const float bx0 = gmin(ax) - margin, bx1 = gmax(ax) + margin;
+        const float by0 = gmin(ay) - margin, by1 = gmax(ay) + margin;
         float bz0 = 0.0f, bz1 = 0.0f;
         if (ND == 3) {
-            bz0 = __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(az) : INT_MAX)) - margin;
-            bz1 = __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(az) : 0)) + margin;
+            bz0 = gmin(az) - margin;
+            bz1 = gmax(az) + margin;
         }
+        // distance of a row's slab [d cs, (d + 1) cs] from the box [b0, b1] along one axis
+        auto slab = [&](int d, float b0, float b1) {
+            return fmaxf(fmaxf((float)d * cs - b1, b0 - (float)(d + 1) * cs), 0.0f);
+        };
         const int zr = (ND == 3) ? 2 : 0;
         for (int dz = -zr; dz <= zr; ++dz) {
             if (cz + dz < 0 || cz + dz >= g.n[2]) continue;
-            const float ez = (ND == 3) ? fmaxf(fmaxf((float)dz * cs - bz1, bz0 - (float)(dz + 1) * cs), 0.0f) : 0.0f;
+            const float ez = (ND == 3) ? slab(dz, bz0, bz1) : 0.0f;
             for (int dy = -2; dy <= 2; ++dy) {
                 if (cy + dy < 0 || cy + dy >= g.n[1]) continue;
-                const float ey = fmaxf(fmaxf((float)dy * cs - by1, by0 - (float)(dy + 1) * cs), 0.0f);
+                const float ey = slab(dy, by0, by1);
                 if (fmaf(ey, ey, ez * ez) > r2box) continue;  // the whole row is out of reach
                 const bool need = ing && dy >= -yl && dy <= yh && dz >= -zl && dz <= zh;
                 if (!__ballot_sync(FULL, need)) continue;
