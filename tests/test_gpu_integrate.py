@@ -41,6 +41,26 @@ def test_integrate_fp64_2d(pkg, orc, cuda, mode):
     semi.close()
 
 
+def test_integrate_2d_dam_break_200_steps(pkg, orc, cuda):
+    """The 2D dam break (5000 fluid particles, 3 wall layers, dx = 0.02) over its full 200 steps
+    at dt = 1e-4 from rest, FP64 drop-in and FP32 form against the oracle."""
+    nd = 2
+    v, u, v_ref, u_ref, semi = _integrate(pkg, orc, cuda, 2, 0.02, (2.0, 1.0), (5.366, 4.0),
+                                          200, 1e-4, "float64")
+    vr, vg = v_ref.reshape(-1, nd + 1), v.reshape(-1, nd + 1)
+    assert rel_l2(u, u_ref) <= 1e-11
+    assert rel_l2(vg[:, :nd], vr[:, :nd]) <= 1e-8
+    assert rel_l2(vg[:, nd], vr[:, nd]) <= 1e-11
+    semi.close()
+    v, u, _, _, semi = _integrate(pkg, orc, cuda, 2, 0.02, (2.0, 1.0), (5.366, 4.0), 200, 1e-4,
+                                  "float32")
+    vg = v.reshape(-1, nd + 1)
+    assert rel_l2(u, u_ref) <= 1e-7
+    assert rel_l2(vg[:, :nd], vr[:, :nd]) <= 1e-4
+    assert rel_l2(vg[:, nd], vr[:, nd]) <= 1e-7
+    semi.close()
+
+
 def test_integrate_fp64_3d_jittered(pkg, orc, cuda):
     v, u, v_ref, u_ref, semi = _integrate(pkg, orc, cuda, 3, 0.05, (1.0, 0.5, 1.0),
                                           (3.2, 1.0, 1.4), 10, 2e-4, "float64", jitter=0.1)
