@@ -12,10 +12,12 @@ CASES = [
     dict(ndims=2, dx=0.02, fluid=(2.0, 1.0), tank=(5.366, 4.0), jitter=0.3),
     dict(ndims=3, dx=0.05, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.0),
     dict(ndims=3, dx=0.05, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.45),
+    # the full 3D workload of the benchmark: 968 750 fluid + 876 666 wall particles
+    dict(ndims=3, dx=0.008, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.2),
 ]
 
 
-@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c['ndims']}d-j{c['jitter']}")
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c['ndims']}d-dx{c['dx']}-j{c['jitter']}")
 def test_nhs_bit_exact(pkg, orc, cuda, case):
     semi, tank = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"],
                                 jitter=case["jitter"], seed=7)
