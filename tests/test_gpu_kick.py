@@ -86,6 +86,24 @@ def test_kick_fp32_form_matches_oracle(pkg, orc, cuda, case):
     assert rel_l2(out["p_w"], ref["p_w"]) <= 1e-5
 
 
+FULL = dict(ndims=3, dx=0.008, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.2, vel=0.5)
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_kick_full_3d_workload(pkg, orc, cuda, precision):
+    """One right-hand side of the full 3D benchmark workload (968 750 fluid + 876 666 wall
+    particles, jittered, random velocities) against the oracle."""
+    out, dv_ref, ref, nd = _run(pkg, orc, cuda, FULL, precision)
+    g = out["dv"].reshape(-1, nd + 1)
+    r = dv_ref.reshape(-1, nd + 1)
+    if precision == "float64":
+        assert rel_l2(out["dv"], dv_ref) <= 1e-11
+        assert rel_l2(out["p_w"], ref["p_w"]) <= 1e-12
+    else:
+        assert rel_l2(g[:, :nd], r[:, :nd]) <= 2e-5
+        assert np.abs(g[:, nd] - r[:, nd]).max() <= 1e-4 * max(np.abs(r[:, nd]).max(), 1.0)
+
+
 def test_drift_copies_velocity(pkg, cuda):
     # test/general/semidiscretization.jl:608-631
     torch = cuda
