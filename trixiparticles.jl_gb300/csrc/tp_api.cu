@@ -1156,8 +1156,11 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
             PhysState& src = h->st[h->cur];
             PhysState& dst = h->st[1 - h->cur];
             mark(h, 0);
-            // displacement since the last rebuild (slot order of src = order of x_build)
-            TP_CUDA(h, cudaMemsetAsync(h->gate + 1, 0, sizeof(unsigned), h->stream));
+            // displacement since the last rebuild (slot order of src = order of x_build); after
+            // the first stage of the call the forced flag is consumed as well (the pair kernels
+            // read the gate to know whether this stage moved the state, so none writes it)
+            TP_CUDA(h, cudaMemsetAsync(step + stage > 0 ? h->gate : h->gate + 1, 0,
+                                       (step + stage > 0 ? 2 : 1) * sizeof(unsigned), h->stream));
             if (nd == 2)
                 k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build, nf,
                                                                          h->gate);
@@ -1187,7 +1190,7 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
             TP_DBG(h, "adami");
             mark(h, 2);
             if (f32)
-                fp32_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
+                fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0);
             else
                 fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
             TP_LAUNCHED(h, "pair stage");

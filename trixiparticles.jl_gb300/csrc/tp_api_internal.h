@@ -23,7 +23,9 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
 void fp32_init_wall_state(tp_handle* h);
 void fp32_adami(tp_handle* h);
 void fp32_pair_kick(tp_handle* h, double* dv);
-void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first);
+// src: the stage's source state (read in place when the stage did not rebuild); st: destination
+void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
+                     double dt, int first);
 
 // API layer services used by the differentiation form (tp_api.cu)
 tp_status api_fail(tp_handle* h, tp_status st, const std::string& msg);

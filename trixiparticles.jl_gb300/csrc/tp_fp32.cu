@@ -94,12 +94,16 @@ struct Pack32 {
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
         }
         if (u_out) {
+            // the integrator state moves with a rebuild; without one the pair pass reads the
+            // source state in place and writes the destination, so only ids and masses follow
+            if (rebuild) {
 #pragma unroll
-            for (int d = 0; d < ND; ++d) {
-                u_out[(size_t)s * ND + d] = x[d];
-                tu_out[(size_t)s * ND + d] = tu[(size_t)i * ND + d];
+                for (int d = 0; d < ND; ++d) {
+                    u_out[(size_t)s * ND + d] = x[d];
+                    tu_out[(size_t)s * ND + d] = tu[(size_t)i * ND + d];
+                }
+                tv_out[s] = tv[i];
             }
-            tv_out[s] = tv[i];
             id_out[s] = id_in[i];
             m_out[s] = mi;
         }
@@ -173,11 +177,16 @@ struct Update32 {
     double* dv;       // kick: dv_ode (caller order, FP64) indexed by perm
     const int* perm;
     double g[3];
-    // integrator (slot order, in place on the state written by this stage's pack)
+    // integrator (slot order): the destination state; the pass reads the positions and
+    // registers from it when this stage's pack moved the state there (a rebuild), else from the
+    // source state in place
     double* u;
     double* tu;
     float4* v_out;
     float4* tv;
+    const double* u_in;
+    const double* tu_in;
+    const float4* tv_in;
     double A, B, dt;
     float Af, Bf, dtf;
     int first;
@@ -209,7 +218,6 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
     __shared__ float4 off[kOffsetCodes];
     fill_offset_table(off, P.cs);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
     const float4 ta = ftest[s];  // {offsets, rho - rho0}
     const float4 va = fvel[s];   // {v, m / rho}
@@ -298,7 +306,10 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
         const float kv[4] = {(float)k[0], (float)k[1], ND == 3 ? (float)k[2] : 0.0f,
                              (float)k[ND]};
         const float vin[4] = {va.x, va.y, va.z, drho_a};
-        const float4 tv = U.tv[s];
+        const bool moved = gate_open(gate);  // this stage rebuilt (gate words are not written here)
+        const double* u_in = moved ? U.u : U.u_in;
+        const double* tu_in = moved ? U.tu : U.tu_in;
+        const float4 tv = (moved ? U.tv : U.tv_in)[s];
         const float tin[4] = {tv.x, tv.y, tv.z, tv.w};
         float tout[4], vout[4];
 #pragma unroll
@@ -313,9 +324,9 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
             const double ku = (double)vin[d];
-            const double t = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
+            const double t = U.first ? U.dt * ku : fma(U.dt, ku, U.A * tu_in[(size_t)s * ND + d]);
             U.tu[(size_t)s * ND + d] = t;
-            U.u[(size_t)s * ND + d] = fma(U.B, t, U.u[(size_t)s * ND + d]);
+            U.u[(size_t)s * ND + d] = fma(U.B, t, u_in[(size_t)s * ND + d]);
         }
     }
 }
@@ -422,7 +433,8 @@ void fp32_pair_kick(tp_handle* h, double* dv) {
         launch_pair32<3, false>(h, nullptr, U);
 }
 
-void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first) {
+void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
+                     double dt, int first) {
     if (h->cfg.n_fluid == 0) return;
     Update32 U{};
     U.perm = h->f_perm;
@@ -431,6 +443,9 @@ void fp32_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt,
     U.tu = st.tu;
     U.v_out = (float4*)st.v;
     U.tv = (float4*)st.tv;
+    U.u_in = src.u;
+    U.tu_in = src.tu;
+    U.tv_in = (const float4*)src.tv;
     U.A = A;
     U.B = B;
     U.dt = dt;

@@ -414,13 +414,12 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
                                                 Filter64 F,
                                                 const double4_32a* __restrict__ wpos,
                                                 const double4_32a* __restrict__ wstate,
-                                                unsigned* __restrict__ gate, Update64 U) {
+                                                Update64 U) {
     __shared__ float4 off[kOffsetCodes];
     __shared__ unsigned lbuf_all[kListChunk][256];
     fill_offset_table(off, F.cs);
     unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
@@ -514,10 +513,8 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
                                                  const int* __restrict__ efwc,
                                                  const double4_32a* __restrict__ wpos,
                                                  const double4_32a* __restrict__ wstate,
-                                                 double* __restrict__ acc,
-                                                 unsigned* __restrict__ gate) {
+                                                 double* __restrict__ acc) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gate && blockIdx.x == 0 && threadIdx.x == 0) gate[0] = 0u;  // forced rebuild consumed
     if (s >= nf) return;
     const double4_32a pa = fpos[s];
     const double4_32a va = fvel[s];
@@ -758,7 +755,7 @@ void fp64_adami(tp_handle* h) {
 }
 
 template <int ND, bool INTEG>
-static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
+static void launch_pair64(tp_handle* h, const Update64& U) {
     const int nf = (int)h->cfg.n_fluid;
     const double sr2 = h->phys.sr2;
     const bool sym = h->pair_mode == TP_PAIR_SYMMETRIC;
@@ -772,7 +769,7 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
         k_pair64s<ND><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
             (const double4_32a*)h->f_aux, h->e_ff, h->ec_ff, h->e_fw, h->ec_fw,
-            (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, h->acc, gate);
+            (const double4_32a*)h->w_pos, (const double4_32a*)h->w_state, h->acc);
         k_update64<ND, INTEG><<<nblk(nf, 256), 256, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel, h->acc, U);
         h->launches += 2;  // filter + update (the pair launch is counted by the caller)
@@ -782,7 +779,7 @@ static void launch_pair64(tp_handle* h, unsigned* gate, const Update64& U) {
         k_pair64<ND, INTEG><<<nblk(nf, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys, nf, (const double4_32a*)h->f_pos, (const double4_32a*)h->f_vel,
             (const double4_32a*)h->f_aux, F, (const double4_32a*)h->w_pos,
-            (const double4_32a*)h->w_state, gate, U);
+            (const double4_32a*)h->w_state, U);
     }
 }
 
@@ -792,9 +789,9 @@ void fp64_pair_kick(tp_handle* h, double* dv) {
     U.dv = dv;
     U.perm = h->f_perm;
     if (h->cfg.ndims == 2)
-        launch_pair64<2, false>(h, nullptr, U);
+        launch_pair64<2, false>(h, U);
     else
-        launch_pair64<3, false>(h, nullptr, U);
+        launch_pair64<3, false>(h, U);
 }
 
 // Stage update in place on the slot-ordered state `out` written by the pack of this stage.
@@ -811,9 +808,9 @@ void fp64_pair_stage(tp_handle* h, PhysState& out, double A, double B, double dt
     U.dt = dt;
     U.first = first;
     if (h->cfg.ndims == 2)
-        launch_pair64<2, true>(h, h->gate, U);
+        launch_pair64<2, true>(h, U);
     else
-        launch_pair64<3, true>(h, h->gate, U);
+        launch_pair64<3, true>(h, U);
 }
 
 void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf) {
