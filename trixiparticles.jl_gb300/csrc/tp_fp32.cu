@@ -14,6 +14,9 @@
 //   * positions and their Runge-Kutta register stay FP64 (the drift! accumulation); velocity
 //     and density registers are FP32.
 // The neighbour set is the FP32 one: |o_a - o_b + shift|^2 <= (2h)^2 evaluated in FP32.
+// A neighbour gather is 36 bytes from three slot-ordered arrays (test {offsets, rho - rho0},
+// velocity {v, m / rho}, pressure): neighbouring lanes gather nearby slots, so small records keep
+// many of them in one cache line.
 #include "tp_api_internal.h"
 #include "tp_lists.cuh"
 

@@ -10,11 +10,13 @@
 // IEEE division here.
 //
 // Neighbour lists (tp_lists.cuh) are built with an FP32 distance on cell-relative offsets whose
-// bound is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative).  Before every pair
-// pass the exact-list filter reduces them to the pairs with |x_a - x_b|^2 <= (2h)^2 decided in
-// FP64 with explicitly rounded products and sums (no FMA contraction) wherever the FP32 test is
-// not conclusive; the Adami kernel decides its listed pairs the same way.  The neighbour set is
-// therefore the one the CPU computes, visited in the CPU's order.
+// bound is widened by 1e-5 (FP32 rounding of d^2 is below 1e-6 relative).  At the start of every
+// pair pass (fused into the pair kernel) the exact-list filter reduces them to the pairs with
+// |x_a - x_b|^2 <= (2h)^2 decided in FP64 with explicitly rounded products and sums (no FMA
+// contraction) wherever the FP32 test is not conclusive; the Adami kernel compacts its wall
+// lists the same way.  The neighbour set is therefore the one the CPU computes, visited in the
+// CPU's order.  The Cole EOS power and its inverse use repeated multiplication and Newton's
+// method for the usual integer exponent (a few ulp of the correctly rounded values).
 //
 // On GB300 an FP64 FMA issues at 1/64 of the FP32 rate (about 20 SM cycles per warp
 // instruction), so the pair kernel is FP64-throughput bound and the code spends FP32 and
