@@ -76,3 +76,37 @@ def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64).ravel()
     b = np.asarray(b, dtype=np.float64).ravel()
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def adami_tank_case(pkg, density, gravity, precision="float64", n_layers=2):
+    """The static tank of the reference's Adami pressure-extrapolation tests
+    (test/schemes/boundary/dummy_particles/dummy_particles.jl:308-333): a 10 x 10 fluid block at
+    dx = 0.1 filling the tank, `n_layers` of wall particles on the bottom and sides (no lid),
+    Cole EOS with c = 10, rho0 = 257, exponent 7, smoothing length 1.5 dx; `density` is the fluid
+    density (hydrostatic from the EOS when `gravity` is set)."""
+    dx = 0.1
+    eos = pkg.StateEquationCole(sound_speed=10.0, reference_density=257.0, exponent=7.0)
+    acc = (0.0, -gravity) if gravity else None
+    tank = pkg.RectangularTank(dx, (1.0, 1.0), (1.0, 1.0), density, n_layers=n_layers,
+                               acceleration=acc, state_equation=eos if gravity else None,
+                               faces=(True, True, True, False))
+    semi = pkg.dam_break_semidiscretization(tank, eos, 1.5 * dx, precision=precision,
+                                            gravity=gravity)
+    return semi, tank, eos
+
+
+def hydrostatic_fields(pkg, tank, eos, p_f, p_w, n_layers=2, n=10, dx=0.1):
+    """Pressure of the tank's fluid and walls on one integer grid, and that of a fluid-only tank
+    covering the same area (test/schemes/boundary/dummy_particles/dummy_particles.jl:646-694)."""
+    got = np.zeros((n + 2 * n_layers, n + n_layers))
+    for coords, p in ((tank.boundary.coordinates, p_w), (tank.fluid.coordinates, p_f)):
+        idx = np.rint(coords / dx + n_layers + 0.5).astype(int) - 1
+        got[idx[:, 0], idx[:, 1]] = p
+    ref_tank = pkg.RectangularTank(dx, (dx * (n + 2 * n_layers), dx * (n + n_layers)),
+                                   (dx * (n + 2 * n_layers), dx * (n + n_layers)), 257.0,
+                                   n_layers=0, acceleration=(0.0, -9.81), state_equation=eos,
+                                   faces=(True, True, True, False))
+    ref = np.zeros_like(got)
+    idx = np.rint(ref_tank.fluid.coordinates / dx + 0.5).astype(int) - 1
+    ref[idx[:, 0], idx[:, 1]] = ref_tank.fluid.pressure
+    return got, ref
