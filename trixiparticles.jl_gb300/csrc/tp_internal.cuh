@@ -1,17 +1,22 @@
 // tp_internal.cuh — shared device-side definitions of the sm_103a WCSPH library.
 //
-// Data layout in HBM (all particle arrays are cell-sorted "slots" unless noted):
-//   fluid records, rebuilt once per RHS evaluation by the pack pass of the neighbour search:
-//     FP64 form:  fpos[s] = double4_32a {x, y, z, p}      fvel[s] = double4_32a {vx, vy, vz, rho}
-//                 fmass[s] = double m
-//     FP32 form:  fpos[s] = float4  {ox, oy, oz, p}   (ox.. = offset inside the cell, metres)
-//                 fvel[s] = float4  {vx, vy, vz, rho - rho0}
-//                 fmass[s] = float m
-//   wall records, sorted once (walls are static), pressure/density rewritten by the Adami pass:
-//     FP64:  wpos[s] = double4_32a {x, y, z, m}   wstate[s] = double2 {p, rho}
-//     FP32:  wpos[s] = float4  {ox, oy, oz, m} wstate[s] = float2 {p, rho - rho0}
+// Data layout in HBM (all particle arrays are cell-sorted "slots" unless noted; o = offset of
+// the particle inside its reference cell in FP32 metres, cx = its x cell index):
+//   fluid records, written by the pack pass of every right-hand side:
+//     both forms: ftest[s] = float4 {ox, oy, oz, cx} (FP64) / {ox, oy, oz, rho - rho0} (FP32)
+//     FP64 form:  fpos[s] = double4_32a {x, y, z, p}   fvel[s] = double4_32a {vx, vy, vz, rho}
+//                 faux[s] = double4_32a {p S, S, p_off + p - rho g.x, 2 m alpha c h sg_c} with
+//                 S = sg_c m / rho (gather pair mode; the symmetric mode keeps {m, m/rho, 1/rho,
+//                 2 m alpha c h})
+//     FP32 form:  fvel[s] = float4 {vx, vy, vz, m / rho}   faux[s] = float p
+//   wall records, sorted once (walls are static), the state rewritten by the Adami pass:
+//     wpos[s] = double4_32a {x, y, z, m}, wtest[s] = float4 {ox, oy, oz, cx} (FP32 form: the
+//     fourth slot is m / rho of the last Adami pass)
+//     FP64:  wstate[s] = double4_32a {p, rho, p S, S}  (symmetric mode: {p, rho, 1/rho, m/rho})
+//     FP32:  wstate[s] = float4 {p, rho - rho0, m, m / rho} and a dense float pressure array
 //   cell list: start[c] = first slot of cell c (ncells + 1 entries), cells linearised x fastest,
-//   so the three cells (cx-1, cx, cx+1) of one (cy, cz) row are one contiguous slot range.
+//   so the three cells (cx-1, cx, cx+1) of one (cy, cz) row are one contiguous slot range;
+//   neighbour lists in the chunked layout of tp_lists.cuh.
 // In 2D the z components are unused.
 #pragma once
 
