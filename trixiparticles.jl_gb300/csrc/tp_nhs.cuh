@@ -16,10 +16,12 @@
 //
 // Gate: inside the integrator the cell list is rebuilt only when some particle has moved more
 // than half the neighbour-list skin since the last rebuild (or a rebuild is forced).  The
-// decision is taken on the device: gate[0] = force flag, gate[1] = largest displacement since
-// the last rebuild (non-negative float bits, so unsigned order = float order), gate[2] = half
-// skin (float bits).  A null gate means "always rebuild".  When the gate is closed the kernels
-// return at once and the rank pass packs every slot in place.
+// decision is taken on the device: gate[0] = force flag, gate[1] = largest squared displacement
+// since the last rebuild (non-negative float bits, so unsigned order = float order), gate[2] =
+// the squared half skin (skin * h)^2, lowered by 1e-5 relative so that FP32 rounding of the
+// displacement never lets a particle past the margin unseen (float bits).  A null gate means
+// "always rebuild".  When the gate is closed the kernels return at once and the rank pass packs
+// every slot in place.
 #pragma once
 
 #include "tp_internal.cuh"
