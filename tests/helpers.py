@@ -78,7 +78,7 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def adami_tank_case(pkg, density, gravity, precision="float64", n_layers=2):
+def adami_tank_case(pkg, density, gravity, precision="float64", n_layers=2, wall_clip=True):
     """The static tank of the reference's Adami pressure-extrapolation tests
     (test/schemes/boundary/dummy_particles/dummy_particles.jl:308-333): a 10 x 10 fluid block at
     dx = 0.1 filling the tank, `n_layers` of wall particles on the bottom and sides (no lid),
@@ -91,7 +91,7 @@ def adami_tank_case(pkg, density, gravity, precision="float64", n_layers=2):
                                acceleration=acc, state_equation=eos if gravity else None,
                                faces=(True, True, True, False))
     semi = pkg.dam_break_semidiscretization(tank, eos, 1.5 * dx, precision=precision,
-                                            gravity=gravity)
+                                            gravity=gravity, wall_clip=wall_clip)
     return semi, tank, eos
 
 
@@ -110,3 +110,61 @@ def hydrostatic_fields(pkg, tank, eos, p_f, p_w, n_layers=2, n=10, dx=0.1):
     idx = np.rint(ref_tank.fluid.coordinates / dx + 0.5).astype(int) - 1
     ref[idx[:, 0], idx[:, 1]] = ref_tank.fluid.pressure
     return got, ref
+
+
+def random_fluid_case(pkg, nd, seed, n=6, viscosity=True, diffusion=True, precision="float64"):
+    """Fluid-only semidiscretization of n^nd particles on a lattice of spacing 0.1 jittered by
+    +-0.3 dx, densities 1000 (1 +- 1 %), random velocities, no walls and no gravity: the
+    setting of the reference's conservation tests (test/schemes/fluid/rhs.jl:115-264), with the
+    path's WendlandC2 kernel at h = 1.2 dx.  Returns (semi, x, v, m)."""
+    rng = np.random.default_rng(seed)
+    dx = 0.1
+    g = np.stack(np.meshgrid(*[np.arange(n)] * nd, indexing="ij"), -1).reshape(-1, nd)
+    x = (g + 0.5) * dx + rng.uniform(-0.3 * dx, 0.3 * dx, g.shape)
+    rho = 1000.0 * (1 + rng.uniform(-0.01, 0.01, len(x)))
+    m = dx ** nd * rho
+    v = np.zeros((len(x), nd + 1))
+    v[:, :nd] = rng.normal(0, 0.3, (len(x), nd))
+    v[:, nd] = rho
+    eos = pkg.StateEquationCole(sound_speed=20.0, reference_density=1000.0, exponent=7.0)
+    ic = pkg.InitialCondition(x, v[:, :nd], m, rho, np.zeros(len(x)), dx)
+    wic = pkg.InitialCondition(np.zeros((0, nd)), np.zeros((0, nd)), np.zeros(0), np.zeros(0),
+                               np.zeros(0), dx)
+    k = pkg.WendlandC2Kernel(nd)
+    fluid = pkg.WeaklyCompressibleSPHSystem(
+        ic, smoothing_kernel=k, smoothing_length=1.2 * dx,
+        density_calculator=pkg.ContinuityDensity(), state_equation=eos,
+        acceleration=(0.0,) * nd,
+        viscosity=pkg.ArtificialViscosityMonaghan(alpha=0.02) if viscosity else None,
+        density_diffusion=pkg.DensityDiffusionMolteniColagrossi(delta=0.1) if diffusion else None)
+    wall = pkg.WallBoundarySystem(wic, pkg.BoundaryModelDummyParticles(
+        np.zeros(0), np.zeros(0), pkg.AdamiPressureExtrapolation(), k, 1.2 * dx,
+        state_equation=eos))
+    cl = pkg.FullGridCellList(tuple(x.min(0) - dx), tuple(x.max(0) + dx))
+    semi = pkg.Semidiscretization(fluid, wall,
+                                  neighborhood_search=pkg.GridNeighborhoodSearch(nd, cl),
+                                  parallelization_backend=pkg.GB300Backend(precision=precision))
+    return semi, x, v, m
+
+
+def conservation_residuals(x, v, m, dv, p):
+    """Rates of the conserved quantities of the pair terms and their scales (sums of the
+    magnitudes of the summands): linear momentum sum_a m_a dv_a, angular momentum
+    sum_a m_a x_a x dv_a, total energy sum_a m_a (v_a . dv_a + p_a / rho_a^2 drho_a)
+    (test/schemes/fluid/rhs.jl:192-260)."""
+    nd = x.shape[1]
+    a, drho = dv[:, :nd], dv[:, nd]
+    rho = v[:, nd]
+    mom = (m[:, None] * a).sum(0)
+    mom_scale = (m[:, None] * np.abs(a)).sum()
+    x3 = np.zeros((len(x), 3))
+    a3 = np.zeros((len(x), 3))
+    x3[:, :nd], a3[:, :nd] = x, a
+    ang = (m[:, None] * np.cross(x3, a3)).sum(0)
+    ang_scale = (m[:, None] * np.linalg.norm(x3, axis=1)[:, None] * np.abs(a3)).sum()
+    work = m * (v[:, :nd] * a).sum(1)
+    heat = m * p / rho ** 2 * drho
+    energy = (work + heat).sum()
+    energy_scale = (np.abs(work) + np.abs(heat)).sum()
+    return dict(mom=mom, mom_scale=mom_scale, ang=ang, ang_scale=ang_scale, energy=energy,
+                energy_scale=energy_scale)

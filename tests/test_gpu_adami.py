@@ -5,7 +5,9 @@ support 3 dx, through tp_kick and the pressure / wall-state accessors, in both p
 * fluid at the reference density: fluid and wall pressures exactly zero, wall density rho0;
 * fluid at another constant density: every wall pressure equals the fluid pressure;
 * hydrostatic fluid: the walls continue the fluid's hydrostatic gradient (atol 4 Pa against a
-  fluid-only tank covering fluid and walls), and the wall state matches the oracle's.
+  fluid-only tank covering fluid and walls), and the wall state matches the oracle's;
+* fluid below the reference density: clipped walls get p = 0 and rho = rho0 exactly, unclipped
+  walls the fluid's negative pressure and its density (dummy_particles.jl:13-68).
 """
 import numpy as np
 import pytest
@@ -17,9 +19,10 @@ pytestmark = pytest.mark.gpu
 PRECISIONS = ["float64", "float32"]
 
 
-def _device_state(pkg, cuda, density, gravity, precision):
+def _device_state(pkg, cuda, density, gravity, precision, wall_clip=True):
     torch = cuda
-    semi, tank, eos = adami_tank_case(pkg, density, gravity, precision=precision)
+    semi, tank, eos = adami_tank_case(pkg, density, gravity, precision=precision,
+                                      wall_clip=wall_clip)
     ode = pkg.semidiscretize(semi, (0.0, 1.0))
     v = np.zeros((tank.fluid.n_particles, 3))
     v[:, 2] = tank.fluid.density
@@ -72,3 +75,18 @@ def test_hydrostatic_pressure_gradient(pkg, orc, cuda, precision):
     else:
         assert np.abs(s["p_w"] - o["p_w"]).max() <= 1e-5 * np.abs(o["p_w"]).max()
         assert np.abs(s["rho_w"] - o["rho_w"]).max() <= 1e-6 * 257.0
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_negative_pressure_clipping(pkg, cuda, precision):
+    s, _, _, eos, _ = _device_state(pkg, cuda, 250.0, 0.0, precision, wall_clip=True)
+    p0 = eos(250.0)
+    assert p0 < 0.0
+    assert np.all(s["p_w"] == 0.0) and np.all(s["rho_w"] == 257.0)
+    s, *_ = _device_state(pkg, cuda, 250.0, 0.0, precision, wall_clip=False)
+    # FP32 form: float EOS, its inverse and sums (a few ulp of |p0| ~ 750 and of rho)
+    tol_p = 1e-12 if precision == "float64" else 1e-5 * abs(p0)
+    tol_rho = 1e-12 * 250.0 if precision == "float64" else 1e-6 * 250.0
+    assert np.abs(s["p_f"] - p0).max() <= tol_p
+    assert np.abs(s["p_w"] - p0).max() <= tol_p
+    assert np.abs(s["rho_w"] - 250.0).max() <= tol_rho
