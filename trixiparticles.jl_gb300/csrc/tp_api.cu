@@ -176,13 +176,25 @@ __global__ void k_gather_load(const int* __restrict__ id, const double* __restri
     }
 }
 
-// Rebuild gate {forced, largest squared displacement, squared threshold} for a displacement
-// threshold (skin * h); k_displacement fills gate[1].
+// Rebuild gate {forced, largest squared displacement, squared threshold, largest squared
+// displacement of the next stage} for a displacement threshold (skin * h); k_displacement fills
+// gate[1], the integrator's pair stage gate[3].
 __global__ void k_gate_init(unsigned* __restrict__ gate, float threshold, int force) {
     if (threadIdx.x == 0) {
         gate[0] = force ? 1u : 0u;
         gate[1] = 0u;
         gate[2] = __float_as_uint((threshold * threshold) * (1.0f - 1e-5f));
+        gate[3] = 0u;
+    }
+}
+
+// Integrator, between stages: the forced flag is consumed, the displacement the last pair stage
+// collected becomes this stage's, and the next stage's word starts from zero.
+__global__ void k_gate_advance(unsigned* __restrict__ gate) {
+    if (threadIdx.x == 0) {
+        gate[0] = 0u;
+        gate[1] = gate[3];
+        gate[3] = 0u;
     }
 }
 
@@ -1156,17 +1168,21 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
             PhysState& src = h->st[h->cur];
             PhysState& dst = h->st[1 - h->cur];
             mark(h, 0);
-            // displacement since the last rebuild (slot order of src = order of x_build); after
-            // the first stage of the call the forced flag is consumed as well (the pair kernels
-            // read the gate to know whether this stage moved the state, so none writes it)
-            TP_CUDA(h, cudaMemsetAsync(step + stage > 0 ? h->gate : h->gate + 1, 0,
-                                       (step + stage > 0 ? 2 : 1) * sizeof(unsigned), h->stream));
-            if (nd == 2)
-                k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build, nf,
-                                                                         h->gate);
-            else
-                k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build, nf,
-                                                                         h->gate);
+            // displacement since the last rebuild (slot order of src = order of x_build): at the
+            // first stage of the call a pass over the loaded state; later the previous pair
+            // stage has collected it from the positions it wrote (gate[3]), and the advance
+            // also consumes the forced flag (the pair kernels read gate[0..2] to know whether
+            // this stage moved the state, so none writes them)
+            if (step + stage == 0) {
+                if (nd == 2)
+                    k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build,
+                                                                             nf, h->gate);
+                else
+                    k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build,
+                                                                             nf, h->gate);
+            } else {
+                k_gate_advance<<<1, 32, 0, h->stream>>>(h->gate);
+            }
             h->launches += 1;
             TP_DBG(h, "displacement");
             st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);

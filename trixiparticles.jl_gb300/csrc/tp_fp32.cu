@@ -190,6 +190,10 @@ struct Update32 {
     const double* u_in;
     const double* tu_in;
     const float4* tv_in;
+    // displacement check of the next stage (optional): positions of the last rebuild (slot
+    // order) and the gate word that collects the largest squared displacement
+    const double* xb;
+    unsigned* gate_next;
     double A, B, dt;
     float Af, Bf, dtf;
     int first;
@@ -324,13 +328,17 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
         }
         U.tv[s] = make_float4(tout[0], tout[1], tout[2], tout[3]);
         U.v_out[s] = make_float4(vout[0], vout[1], vout[2], vout[3]);
+        double un[ND];
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
             const double ku = (double)vin[d];
             const double t = U.first ? U.dt * ku : fma(U.dt, ku, U.A * tu_in[(size_t)s * ND + d]);
             U.tu[(size_t)s * ND + d] = t;
-            U.u[(size_t)s * ND + d] = fma(U.B, t, u_in[(size_t)s * ND + d]);
+            un[d] = fma(U.B, t, u_in[(size_t)s * ND + d]);
+            U.u[(size_t)s * ND + d] = un[d];
         }
+        if (U.gate_next)
+            gate_max_displacement(U.gate_next, displacement2<ND>(un, U.xb + (size_t)s * ND));
     }
 }
 
@@ -449,6 +457,8 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
     U.u_in = src.u;
     U.tu_in = src.tu;
     U.tv_in = (const float4*)src.tv;
+    U.xb = h->x_build;
+    U.gate_next = h->gate + 3;
     U.A = A;
     U.B = B;
     U.dt = dt;

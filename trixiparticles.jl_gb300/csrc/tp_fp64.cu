@@ -159,6 +159,10 @@ struct Update64 {
     double* v_out;
     double* tu;
     double* tv;
+    // displacement check of the next stage (optional): positions of the last rebuild (slot
+    // order) and the gate word that collects the largest squared displacement
+    const double* xb;
+    unsigned* gate_next;
     double A, B, dt;
     int first;
 };
@@ -182,13 +186,17 @@ __device__ __forceinline__ void stage_update(int s, const double4_32a& pa, const
             U.tv[(size_t)s * (ND + 1) + d] = tv;
             U.v_out[(size_t)s * (ND + 1) + d] = fma(U.B, tv, va_arr[d]);
         }
+        double un[ND];
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
             const double ku = va_arr[d];
             double tu = U.first ? U.dt * ku : fma(U.dt, ku, U.A * U.tu[(size_t)s * ND + d]);
             U.tu[(size_t)s * ND + d] = tu;
-            U.u_out[(size_t)s * ND + d] = fma(U.B, tu, xa_arr[d]);
+            un[d] = fma(U.B, tu, xa_arr[d]);
+            U.u_out[(size_t)s * ND + d] = un[d];
         }
+        if (U.gate_next)
+            gate_max_displacement(U.gate_next, displacement2<ND>(un, U.xb + (size_t)s * ND));
     }
 }
 
@@ -805,6 +813,8 @@ void fp64_pair_stage(tp_handle* h, PhysState& out, double A, double B, double dt
     U.v_out = (double*)out.v;
     U.tu = out.tu;
     U.tv = (double*)out.tv;
+    U.xb = h->x_build;
+    U.gate_next = h->gate + 3;
     U.A = A;
     U.B = B;
     U.dt = dt;

@@ -98,6 +98,29 @@ __device__ __forceinline__ float pair_diff(float4 ta, const float4* tab, unsigne
     return d2;
 }
 
+// Squared displacement of one particle, the same arithmetic as k_displacement: FP64 differences
+// rounded to FP32, FP32 sum of squares.
+template <int ND>
+__device__ __forceinline__ float displacement2(const double* x, const double* __restrict__ xb) {
+    float d2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        const float e = (float)(x[k] - xb[k]);
+        d2 = fmaf(e, e, d2);
+    }
+    return (d2 == d2) ? d2 : 3.0e38f;  // NaN positions force a rebuild (and are reported there)
+}
+
+// The integrator's pair stage already holds every particle's next position: it folds the
+// displacement check of the next stage into its update, each converged group of lanes taking
+// the maximum of its squared displacements into `word` (float bits, atomicMax on unsigned);
+// lanes that returned early take no part.
+__device__ __forceinline__ void gate_max_displacement(unsigned* word, float d2) {
+    const unsigned m = __activemask();
+    const unsigned mx = __reduce_max_sync(m, __float_as_uint(d2));
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1 && mx > 0u) atomicMax(word, mx);
+}
+
 // Largest squared displacement since the last rebuild -> gate[1] (float bits, atomicMax on
 // unsigned), compared with the squared threshold in gate[2].  Only the differences are FP64 (the
 // positions are); squares and sum are FP32 and there is no square root: the pass was bound by
@@ -113,12 +136,7 @@ __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__
     float d2 = 0.0f;
     if (s < n) {
         const int i = perm ? perm[s] : s;
-#pragma unroll
-        for (int k = 0; k < ND; ++k) {
-            const float e = (float)(u[(size_t)i * ND + k] - xb[(size_t)s * ND + k]);
-            d2 = fmaf(e, e, d2);
-        }
-        if (!(d2 == d2)) d2 = 3.0e38f;  // NaN positions force a rebuild (and are reported there)
+        d2 = displacement2<ND>(u + (size_t)i * ND, xb + (size_t)s * ND);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, off));
