@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
         const float kv[4] = {(float)k[0], (float)k[1], ND == 3 ? (float)k[2] : 0.0f,
                              (float)k[ND]};
         const float vin[4] = {va.x, va.y, va.z, drho_a};
-        const bool moved = gate_open(gate);  // this stage rebuilt (gate words are not written here)
+        const bool moved = gate_open(gate);  // this stage rebuilt (gate[0..2] are read-only here)
         const double* u_in = moved ? U.u : U.u_in;
         const double* tu_in = moved ? U.tu : U.tu_in;
         const float4 tv = (moved ? U.tv : U.tv_in)[s];
