@@ -168,3 +168,60 @@ def conservation_residuals(x, v, m, dv, p):
     energy_scale = (np.abs(work) + np.abs(heat)).sum()
     return dict(mom=mom, mom_scale=mom_scale, ang=ang, ang_scale=ang_scale, energy=energy,
                 energy_scale=energy_scale)
+
+
+def gpu_example_dam_break(pkg, precision="float64"):
+    """examples/fluid/dam_break_2d.jl as examples/fluid/dam_break_2d_gpu.jl includes it, at the
+    fluid particle spacing 0.05 of the reference's GPU interpolation test
+    (test/examples/gpu.jl:833-841): H = 0.6, W = 2H, tank length floor(5.366 H / dx) dx by 4,
+    4 wall layers, Cole EOS with exponent 1 and c = 20 sqrt(g H), h = 2 dx, Monaghan alpha 0.02,
+    Molteni-Colagrossi delta 0.1, clipped wall pressure.  Returns (semi, tank)."""
+    H, dx, grav = 0.6, 0.05, 9.81
+    eos = pkg.StateEquationCole(sound_speed=20 * math.sqrt(grav * H), reference_density=1000.0,
+                                exponent=1.0)
+    tank_x = math.floor(5.366 * H / dx) * dx
+    tank = pkg.RectangularTank(dx, (2 * H, H), (tank_x, 4.0), 1000.0, n_layers=4,
+                               acceleration=(0.0, -grav), state_equation=eos)
+    semi = pkg.dam_break_semidiscretization(tank, eos, 2 * dx, precision=precision, alpha=0.02,
+                                            delta=0.1, gravity=grav, wall_clip=True)
+    return semi, tank
+
+
+# Fields interpolated by the reference's Float32 GPU run of that setup at t = 0.01
+# (StepsizeCallback(cfl=0.9), CarpenterKennedy2N54), test/examples/gpu.jl:843-916, compared
+# there with isapprox, i.e. |got - ref| <= sqrt(eps(Float32)) |ref| in the 2-norm.
+INTERP_GOLDEN = {
+    "line": dict(  # interpolate_line (0.5, 0) -> (0.5, 0.5), 10 points, cut_off_bnd=false
+        computed_density=[500.96387, 859.06744, 989.0479, 1001.3735, 1001.30927, 1001.0831,
+                          1000.7325, 1000.3575, 999.8011, 975.98553],
+        density=[1002.1891, 1002.0748, 1001.8913, 1001.67126, 1001.4529, 1001.2382, 1001.0298,
+                 1000.81964, 1000.594, 1000.3878],
+        pressure=[5154.1177, 4885.1, 4452.6533, 3934.9075, 3420.5737, 2915.0933, 2424.0908,
+                  1929.7888, 1398.8309, 913.2089]),
+    "line_h02": dict(  # the same line with smoothing_length = 0.2
+        computed_density=[501.10648, 700.15857, 852.81036, 944.48535, 986.2611, 998.96576,
+                          997.5659, 980.23236, 929.7254, 825.95825],
+        density=[1001.98303, 1001.8848, 1001.7575, 1001.59985, 1001.41754, 1001.2164, 1001.0109,
+                 1000.81616, 1000.6457, 1000.5056],
+        pressure=[4668.169, 4437.7715, 4137.7075, 3768.1145, 3337.1655, 2863.6277, 2379.349,
+                  1921.7727, 1519.3884, 1190.5823]),
+    "plane": dict(  # interpolate_plane_2d (0, 0) -> (1, 1), resolution 0.4, cut_off_bnd=false
+        computed_density=[250.47523, 500.98248, 500.49924, 253.77109, 500.0491, 1000.0818,
+                          999.6527, 503.08704],
+        density=[1002.2373, 1002.22516, 1001.4339, 999.3567, 1000.8318, 1000.80237, 1000.3408,
+                 999.92017],
+        pressure=[5267.867, 5239.2466, 3376.045, -1514.4237, 1958.2637, 1888.739, 802.3146,
+                  -187.81871]),
+}
+INTERP_RTOL = float(np.sqrt(np.finfo(np.float32).eps))
+
+
+def interp_golden_errors(results: dict) -> dict:
+    """2-norm relative differences of the interpolated fields from INTERP_GOLDEN."""
+    out = {}
+    for case, fields in INTERP_GOLDEN.items():
+        for f, ref in fields.items():
+            ref = np.asarray(ref, dtype=np.float64)
+            got = np.asarray(results[case][f], dtype=np.float64)
+            out[f"{case}.{f}"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    return out

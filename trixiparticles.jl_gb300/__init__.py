@@ -19,6 +19,7 @@ from .semidiscretization import (
     ODEProblem,
     Semidiscretization,
     SortingCallback,
+    StepsizeCallback,
     SymplecticPositionVerlet,
     WallBoundarySystem,
     WeaklyCompressibleSPHSystem,
@@ -32,17 +33,19 @@ from .semidiscretization import (
 from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
 from . import adjoint, ensemble, interpolation, vtk
 from .vtk import SolutionSavingCallback, trixi2vtk, vtk2trixi
-from .interpolation import interpolate_line, interpolate_points
+from .interpolation import interpolate_line, interpolate_plane_2d, interpolate_plane_3d, \
+    interpolate_points
 
 __all__ = [
     "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
     "CarpenterKennedy2N54", "ContinuityDensity", "DensityDiffusionMolteniColagrossi",
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
     "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole",
-    "SortingCallback", "SymplecticPositionVerlet", "TpConfig",
+    "SortingCallback", "StepsizeCallback", "SymplecticPositionVerlet", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
     "SolutionSavingCallback", "adjoint", "build", "dam_break", "ensemble", "trixi2vtk",
-    "vtk", "vtk2trixi", "interpolate_line", "interpolate_points",
+    "vtk", "vtk2trixi", "interpolate_line", "interpolate_points", "interpolate_plane_2d",
+    "interpolate_plane_3d",
     "interpolation", "dam_break_semidiscretization", "default_config", "drift", "kick",
     "load_library", "semidiscretize", "solve",
 ]

@@ -1,4 +1,5 @@
-"""interpolate_points / interpolate_line (src/general/interpolation.jl:381-697) and the pressure
+"""interpolate_points / interpolate_line / interpolate_plane_2d / interpolate_plane_3d
+(src/general/interpolation.jl:56-322, 381-697, 787-824) and the pressure
 sensors of the 2D dam-break validation (validation/dam_break_2d/sensors.jl:5-18), through the
 library's tp_interpolate_points."""
 from __future__ import annotations
@@ -68,6 +69,76 @@ def interpolate_line(start, end_, n_points, semi, ref_system, v_ode, u_ode, *, e
                               cut_off_bnd=cut_off_bnd,
                               clip_negative_pressure=clip_negative_pressure,
                               include_wall_velocity=include_wall_velocity)
+
+
+def _keep_points_with_neighbors(res: dict) -> dict:
+    """Drop the points without fluid neighbours from every field (interpolation.jl:211-223)."""
+    keep = np.nonzero(res["neighbor_count"] > 0)[0]
+    return {k: (x[keep] if x.ndim == 1 else x[:, keep]) for k, x in res.items()}
+
+
+def plane_points_2d(min_corner, max_corner, resolution) -> np.ndarray:
+    """The (2, n) grid of interpolate_plane_2d (interpolation.jl:183-209): ceil((max - min) /
+    resolution) + 1 points per axis, the first on `min_corner`, spaced by `resolution`, x
+    fastest (rectangular_shape_coords with place_on_shell, rectangular_shape.jl:198-224)."""
+    lo = np.asarray(min_corner, dtype=np.float64)
+    hi = np.asarray(max_corner, dtype=np.float64)
+    if lo.shape != (2,) or hi.shape != (2,):
+        raise ValueError("ArgumentError: function is intended for 2D coordinates only")
+    if np.any(lo > hi):
+        raise ValueError("ArgumentError: `min_corner` should be smaller than `max_corner` in "
+                         "every dimension")
+    s = float(resolution)
+    n = np.ceil((hi - lo) / s).astype(int) + 1
+    iy, ix = np.meshgrid(np.arange(1, n[1] + 1), np.arange(1, n[0] + 1), indexing="ij")
+    idx = np.stack([ix.ravel(), iy.ravel()])
+    return (lo - 0.5 * s)[:, None] + s * (idx - 0.5)
+
+
+def interpolate_plane_2d(min_corner, max_corner, resolution, semi, ref_system, v_ode, u_ode, *,
+                         include_wall_velocity=False, smoothing_length=None, cut_off_bnd=True,
+                         clip_negative_pressure=False) -> dict:
+    """interpolate_points on the grid of plane_points_2d, points without fluid neighbours
+    removed (interpolation.jl:73-87, 183-225)."""
+    res = interpolate_points(plane_points_2d(min_corner, max_corner, resolution), semi,
+                             ref_system, v_ode, u_ode, smoothing_length=smoothing_length,
+                             cut_off_bnd=cut_off_bnd,
+                             clip_negative_pressure=clip_negative_pressure,
+                             include_wall_velocity=include_wall_velocity)
+    return _keep_points_with_neighbors(res)
+
+
+def face_points(point1, point2, point3, resolution) -> np.ndarray:
+    """The (3, n) points of the parallelogram spanned by point2 - point1 and point3 - point1,
+    ceil(|edge| / resolution) + 1 points per edge, the second edge fastest
+    (sample_face_with_fixed_size, interpolation.jl:787-824)."""
+    p1, p2, p3 = (np.asarray(p, dtype=np.float64) for p in (point1, point2, point3))
+    if p1.shape != (3,) or p2.shape != (3,) or p3.shape != (3,):
+        raise ValueError("ArgumentError: all points must be 3D coordinates")
+    e1, e2 = p2 - p1, p3 - p1
+    if abs(np.linalg.norm(np.cross(e1, e2))) <= np.finfo(np.float64).eps:
+        raise ValueError("ArgumentError: the vectors `AB` and `AC` must not be collinear")
+    n1 = int(np.ceil(np.linalg.norm(e1) / resolution))
+    n2 = int(np.ceil(np.linalg.norm(e2) / resolution))
+    i, j = np.meshgrid(np.arange(n1 + 1), np.arange(n2 + 1), indexing="ij")
+    a = (i.ravel() / n1)[None, :]
+    b = (j.ravel() / n2)[None, :]
+    return (p1[:, None] + a * e1[:, None]) + b * e2[:, None]
+
+
+def interpolate_plane_3d(point1, point2, point3, resolution, semi, ref_system, v_ode, u_ode, *,
+                         include_wall_velocity=False, smoothing_length=None, cut_off_bnd=True,
+                         clip_negative_pressure=False) -> dict:
+    """interpolate_points on the points of face_points, points without fluid neighbours removed
+    (interpolation.jl:295-322)."""
+    if semi.ndims != 3:
+        raise ValueError("ArgumentError: `interpolate_plane_3d` requires a 3D simulation")
+    res = interpolate_points(face_points(point1, point2, point3, resolution), semi, ref_system,
+                             v_ode, u_ode, smoothing_length=smoothing_length,
+                             cut_off_bnd=cut_off_bnd,
+                             clip_negative_pressure=clip_negative_pressure,
+                             include_wall_velocity=include_wall_velocity)
+    return _keep_points_with_neighbors(res)
 
 
 def interpolated_pressure(coord_top, coord_bottom, v_ode, u_ode, semi) -> float:

@@ -384,6 +384,32 @@ class SymplecticPositionVerlet:
     by rho_prev (2 - eps) / (2 + eps))."""
 
 
+class StepsizeCallback:
+    """StepsizeCallback(; cfl) (src/callbacks/stepsize.jl:35-75): at initialisation the
+    integrator's fixed step becomes calculate_dt of the semidiscretization, the minimum over its
+    systems (semidiscretization.jl:510-520).  The WCSPH fluid's (fluid.jl:199-229) is
+    min(0.125 h^2 / nu, 0.25 sqrt(h / |g|), cfl h / c) with nu = alpha h c / (2 ndims + 4) for
+    the Monaghan viscosity (viscosity.jl:82-87); the wall's is Inf (wall_boundary/system.jl:
+    291-293).  It depends on no state, so the step stays constant, as in the reference."""
+
+    def __init__(self, *, cfl: float):
+        self.cfl = float(cfl)
+
+    def calculate_dt(self, semi) -> float:
+        f = semi.fluid
+        h = float(f.smoothing_length)
+        c = float(f.state_equation.sound_speed)
+        dt_viscosity = math.inf
+        if isinstance(f.viscosity, ArtificialViscosityMonaghan):
+            nu = f.viscosity.alpha * h * c / (2 * f.ndims + 4)
+            if nu > 0.0:
+                dt_viscosity = 0.125 * h ** 2 / nu
+        g = math.sqrt(sum(float(a) ** 2 for a in (f.acceleration or ())))
+        dt_acceleration = 0.25 * math.sqrt(h / g) if g > 0.0 else math.inf
+        dt_sound_speed = self.cfl * h / c
+        return min(dt_viscosity, dt_acceleration, dt_sound_speed)
+
+
 class SortingCallback:
     """SortingCallback(; interval=-1, dt=0.0, initial_sort=true) (src/callbacks/sorting.jl:
     24-55): reorder the fluid particles by neighbour-search cell at the end of every `interval`
@@ -425,35 +451,62 @@ class ODESolution:
     perm: object = None  # with a SortingCallback: original index of every particle
 
 
+def fixed_step_schedule(t0: float, t1: float, dt: float) -> tuple[int, float | None]:
+    """The steps OrdinaryDiffEq takes with a fixed `dt` from t0 to the tstop t1: dt = min(dt,
+    t1 - t) (the last step shortened to land on t1), and a time within 100 ulp of t1 snapped to it
+    (`fixed_t_for_floatingpoint_error!`), so that a span of a whole number of steps takes no extra
+    step of rounding size.  Returns (full steps, length of the shortened last step or None)."""
+    if not dt > 0.0:
+        raise _argument_error("dt must be positive")
+    t, n = float(t0), 0
+    while t < t1:
+        d = min(dt, t1 - t)
+        tn = t + d
+        if abs(tn - t1) < 100.0 * float(np.spacing(max(abs(t), abs(t1)))):
+            tn = t1
+        if d < dt:
+            return n, d
+        n += 1
+        t = tn
+    return n, None
+
+
 def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int | None = None,
           save_everystep: bool = False, callback=None) -> ODESolution:
-    """Fixed-step CarpenterKennedy2N54 or SymplecticPositionVerlet from tspan[0] for `n_steps`
-    steps (default: to tspan[1]), advanced by the library's fused integrators; v/u of the result
-    are new tensors.  `callback`: SortingCallback and/or SolutionSavingCallback (one or a list),
-    applied between integrator calls at their step / time intervals."""
+    """Fixed-step CarpenterKennedy2N54 or SymplecticPositionVerlet from tspan[0], advanced by the
+    library's fused integrators; v/u of the result are new tensors.  Without `n_steps` the run
+    ends on tspan[1] as OrdinaryDiffEq's does (fixed_step_schedule: the last step shortened);
+    with it, exactly `n_steps` steps of `dt`.  `callback`: SortingCallback and/or
+    SolutionSavingCallback (one or a list), applied between integrator calls at their step /
+    time intervals, and StepsizeCallback, whose step replaces `dt`."""
     if not isinstance(alg, (CarpenterKennedy2N54, SymplecticPositionVerlet)):
         raise _argument_error("only CarpenterKennedy2N54 and SymplecticPositionVerlet are "
                               "provided by the GB300 backend")
     semi = ode.p["semi"]
-    t0, t1 = ode.tspan
-    if n_steps is None:
-        n_steps = int(math.ceil((t1 - t0) / dt - 1e-9))
-    v = ode.v0.clone()
-    u = ode.u0.clone()
-    semi._set_stream()
-    entry = "tp_integrate_spv" if isinstance(alg, SymplecticPositionVerlet) else \
-        "tp_integrate_ck2n54"
     from .vtk import SolutionSavingCallback
 
     cbs = callback if isinstance(callback, (list, tuple)) else \
         ([] if callback is None else [callback])
     for c in cbs:
-        if not isinstance(c, (SortingCallback, SolutionSavingCallback)):
-            raise _argument_error("only SortingCallback and SolutionSavingCallback are "
-                                  "supported as callbacks")
+        if not isinstance(c, (SortingCallback, SolutionSavingCallback, StepsizeCallback)):
+            raise _argument_error("only SortingCallback, SolutionSavingCallback and "
+                                  "StepsizeCallback are supported as callbacks")
+    for c in cbs:  # the step size callback overwrites `dt` before the first step
+        if isinstance(c, StepsizeCallback):
+            dt = c.calculate_dt(semi)
+    cbs = [c for c in cbs if not isinstance(c, StepsizeCallback)]
+    t0, t1 = ode.tspan
+    last = None
+    if n_steps is None:
+        n_steps, last = fixed_step_schedule(t0, t1, dt)
+    v = ode.v0.clone()
+    u = ode.u0.clone()
+    semi._set_stream()
+    entry = "tp_integrate_spv" if isinstance(alg, SymplecticPositionVerlet) else \
+        "tp_integrate_ck2n54"
 
-    def advance(t, k):
-        semi._call(entry, v.data_ptr(), u.data_ptr(), ctypes.c_double(t), ctypes.c_double(dt),
+    def advance(t, k, step=dt):
+        semi._call(entry, v.data_ptr(), u.data_ptr(), ctypes.c_double(t), ctypes.c_double(step),
                    ctypes.c_int64(k))
 
     def next_step(c, done):
@@ -482,12 +535,17 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
                 c.last_t = t
             else:
                 c.save(semi, v, u, t)
+    t_end = t0 + n_steps * dt
+    if last is not None:  # the shortened step that lands on tspan[1]
+        advance(t_end, 1, last)
+        n_steps += 1
+        t_end = t1
     for c in cbs:
         if isinstance(c, SolutionSavingCallback) and c.save_final_solution and \
-                c.last_t != t0 + n_steps * dt:
-            c.save(semi, v, u, t0 + n_steps * dt)
+                c.last_t != t_end:
+            c.save(semi, v, u, t_end)
     semi.sync()
-    return ODESolution(v=v, u=u, t=t0 + n_steps * dt, n_steps=n_steps, perm=perm)
+    return ODESolution(v=v, u=u, t=t_end, n_steps=n_steps, perm=perm)
 
 
 def dam_break_semidiscretization(tank, eos, smoothing_length: float, *, precision="float64",
