@@ -179,6 +179,15 @@ tp_status tp_wall_state(tp_handle* h, double* p_wall, double* rho_wall, double* 
 tp_status tp_nhs_debug(tp_handle* h, const double* u_ode, int32_t* cell, int32_t* order,
                        int32_t* nnb_ff, int32_t* nnb_fw, int32_t* nnb_wf);
 
+/* Diagnostic (parity checks): the divisions the pair kernels use where the reference writes
+ * `div_fast` (src/util.jl:3-5, its CUDA definitions ext/TrixiParticlesCUDAExt.jl:12-32), run on
+ * the device over n device elements:  out64[i] = x64 / y64[i] as the FP64 drop-in divides (the
+ * approximate reciprocal rcp.approx.ftz.f64 refined by one cubic step, then multiplied),
+ * out32[i] = x32 / y32[i] as the FP32 form divides (__fdividef).  Either pair of arrays may be
+ * NULL.  Asynchronous on the handle's stream. */
+tp_status tp_div_fast(tp_handle* h, double x64, const double* y64, double* out64, float x32,
+                      const float* y32, float* out32, int64_t n);
+
 /* Grid layout: dims[0..2] cells per dimension (padding included), *cell_size = 2h. */
 tp_status tp_grid_info(tp_handle* h, int32_t dims[3], double* cell_size, double lo[3]);
 

@@ -6,7 +6,7 @@ built in-tree (build.py); loading fails loudly when it is missing -- there is no
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
@@ -91,6 +91,8 @@ PROTOTYPES = [
     ("tp_fluid_pressure", c_int32, [c_void_p, c_void_p]),
     ("tp_wall_state", c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("tp_nhs_debug", c_int32, [c_void_p] + [c_void_p] * 6),
+    ("tp_div_fast", c_int32, [c_void_p, c_double, c_void_p, c_void_p, c_float, c_void_p,
+                             c_void_p, c_int64]),
     ("tp_grid_info", c_int32, [c_void_p, POINTER(c_int32), POINTER(c_double), POINTER(c_double)]),
     ("tp_conservation", c_int32, [c_void_p, c_void_p, POINTER(c_double)]),
     ("tp_sync", c_int32, [c_void_p]),

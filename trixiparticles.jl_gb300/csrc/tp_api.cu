@@ -1279,6 +1279,19 @@ tp_status tp_wall_state(tp_handle* h, double* p_wall, double* rho_wall, double* 
     return TP_OK;
 }
 
+tp_status tp_div_fast(tp_handle* h, double x64, const double* y64, double* out64, float x32,
+                      const float* y32, float* out32, int64_t n) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (n < 0 || n > (int64_t)1 << 36)
+        return fail(h, TP_ERR_ARGUMENT, "tp_div_fast: bad element count");
+    if ((y64 == nullptr) != (out64 == nullptr) || (y32 == nullptr) != (out32 == nullptr))
+        return fail(h, TP_ERR_ARGUMENT, "tp_div_fast: an input array without its output");
+    if (n == 0 || (!y64 && !y32)) return TP_OK;
+    div_fast_check(h, x64, y64, out64, x32, y32, out32, (long long)n);
+    TP_LAUNCHED(h, "div_fast");
+    return TP_OK;
+}
+
 tp_status tp_nhs_debug(tp_handle* h, const double* u_ode, int32_t* cell, int32_t* order,
                        int32_t* nnb_ff, int32_t* nnb_fw, int32_t* nnb_wf) {
     if (!h) return TP_ERR_ARGUMENT;

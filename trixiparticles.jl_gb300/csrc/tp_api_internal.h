@@ -16,6 +16,8 @@ void fp64_adami(tp_handle* h);
 void fp64_pair_kick(tp_handle* h, double* dv);
 void fp64_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt, int first);
 void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf);
+void div_fast_check(tp_handle* h, double x64, const double* y64, double* out64, float x32,
+                    const float* y32, float* out32, long long n);
 
 // FP32 precision form (tp_fp32.cu)
 void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,

@@ -849,4 +849,21 @@ void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf) {
         run(std::integral_constant<int, 3>{});
 }
 
+// The divisions of the pair kernels over caller arrays (tp_div_fast): FP64 div_fast as the
+// drop-in evaluates it (x * fast_inv(y)) and the FP32 form's __fdividef.
+__global__ void k_div_fast(double x64, const double* __restrict__ y64, double* __restrict__ out64,
+                           float x32, const float* __restrict__ y32, float* __restrict__ out32,
+                           long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (y64) out64[i] = div_fast(x64, y64[i]);
+    if (y32) out32[i] = __fdividef(x32, y32[i]);
+}
+
+void div_fast_check(tp_handle* h, double x64, const double* y64, double* out64, float x32,
+                    const float* y32, float* out32, long long n) {
+    k_div_fast<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(x64, y64, out64, x32, y32,
+                                                                     out32, n);
+}
+
 }  // namespace tp
