@@ -1,7 +1,8 @@
 """kick!/drift! on the GPU against the FP64 oracle.
 
 Tolerances: the FP64 drop-in differs from the CPU oracle only by FMA contraction in the pair
-sums, CUDA's pow in the Cole EOS, the reference's CUDA `div_fast` (relative error < 1e-15
+sums, the Cole EOS power by repeated multiplication and its inverse by Newton's method, the
+reference's CUDA `div_fast` (relative error < 1e-15
 per division, ext/TrixiParticlesCUDAExt.jl), ulp-level rearrangements of reciprocals and square
 roots, and -- in the symmetric pair mode -- the summation order: relative L2 error of
 dv <= 1e-11 in both pair modes; the gather mode is bitwise reproducible.  The FP32
