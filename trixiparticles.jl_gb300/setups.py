@@ -102,8 +102,10 @@ class InitialCondition:
 @dataclass
 class RectangularTank:
     """RectangularTank (rectangular_tank.jl:99-200): fluid block at the tank's min corner with
-    `n_layers` of wall particles on the faces (-x, +x, -y, +y[, -z, +z]), hydrostatic fluid density
-    from the inverse state equation, fluid mass rho*dx^d and wall mass rho0*dx^d."""
+    `n_layers` of wall particles of spacing particle_spacing / spacing_ratio on the faces
+    (-x, +x, -y, +y[, -z, +z]), hydrostatic fluid density from the inverse state equation, fluid
+    mass rho dx^d, wall density boundary_density (default fluid_density) and wall mass
+    boundary_density (dx / spacing_ratio)^d; the whole tank moved to min_coordinates."""
 
     particle_spacing: float
     fluid_size: tuple
@@ -113,6 +115,9 @@ class RectangularTank:
     acceleration: tuple | None = None
     state_equation: StateEquationCole | None = None
     faces: tuple | None = None
+    spacing_ratio: float = 1.0  # particle_spacing / wall particle spacing
+    min_coordinates: tuple | None = None  # the tank's corner in the negative directions
+    boundary_density: float | None = None  # default: fluid_density
     fluid: InitialCondition = field(init=False)
     boundary: InitialCondition = field(init=False)
     n_particles_per_dimension: tuple = field(init=False)
@@ -135,7 +140,9 @@ class RectangularTank:
         for d in range(nd):
             if _isapprox(float(self.fluid_size[d]), float(self.tank_size[d])):
                 tsz[d] = fsz[d]
-        bdx = dx / 1.0
+        if not float(self.spacing_ratio) > 0.0:
+            raise ValueError("`spacing_ratio` must be positive")
+        bdx = dx / float(self.spacing_ratio)
         nbd = []
         for d in range(nd):
             n, s = round_n_particles(tsz[d], bdx)
@@ -151,15 +158,21 @@ class RectangularTank:
         bvol = bdx * bdx if nd == 2 else (bdx * bdx) * bdx
         nw = wall.shape[0]
         rho0 = float(self.fluid_density)
+        rho_w = rho0 if self.boundary_density is None else float(self.boundary_density)
+        shift = np.zeros(nd) if self.min_coordinates is None else \
+            np.asarray(self.min_coordinates, dtype=np.float64)
+        if shift.shape != (nd,):
+            raise ValueError(f"`min_coordinates` must be of length {nd} for a {nd}D problem")
+        wall = wall + shift  # the tank's corner moved to min_coordinates
         self.boundary = InitialCondition(
             coordinates=wall,
             velocity=np.zeros_like(wall),
-            mass=np.full(nw, rho0 * bvol),
-            density=np.full(nw, rho0),
+            mass=np.full(nw, rho_w * bvol),
+            density=np.full(nw, rho_w),
             pressure=np.zeros(nw),
             particle_spacing=bdx,
         )
-        coords = rectangular_shape_coords(dx, nfd, [0.0] * nd)
+        coords = rectangular_shape_coords(dx, nfd, [0.0] * nd) + shift
         nf = coords.shape[0]
         pressure = np.zeros(nf)
         eos = self.state_equation
