@@ -12,7 +12,9 @@ Writes
   every face selection, read from the Julia matrix literals of that file;
 * tests/golden/rectangular_tank_coordinates.json: the expected fluid and wall coordinates of its
   "Coordinates" tests in 2D and 3D (one layer for two spacings, two spacing ratios and two
-  corners; three layers), test/setups/rectangular_tank.jl:1-58, 125-141, 274-340, 373-387.
+  corners; three layers), test/setups/rectangular_tank.jl:1-58, 125-141, 274-340, 373-387;
+* tests/golden/rectangular_shape_coordinates.json: the expected coordinates of the "Positions"
+  and "Loop Orders" tests of test/setups/rectangular_shape.jl (2D: 1-52, 3D: 193-240).
 """
 import json
 import re
@@ -59,6 +61,40 @@ def main(ref_root: str) -> None:
     (HERE / "validation_wcsph_40.json").write_text(json.dumps(out))
     tank_faces(ref_root)
     tank_coordinates(ref_root)
+    shape_coordinates(ref_root)
+
+
+def shape_coordinates(ref_root: str) -> None:
+    src = (Path(ref_root) / "test" / "setups" / "rectangular_shape.jl").read_text()
+    cases = []
+    for nd, text in ((2, src[src.index('"Rectangular Shape 2D"'):
+                             src.index('"Rectangular Shape 3D"')]),
+                     (3, src[src.index('"Rectangular Shape 3D"'):])):
+        pos = text[text.index('"Positions"'):text.index('"Loop Orders"')]
+        corners = [[float(x) for x in t.split(",")] for t in
+                   re.findall(r"\(([-0-9., ]+)\)", pos[pos.index("positions = ["):
+                                                   pos.index("expected_coords")])]
+        spacing = float(re.search(r"particle_spacing = ([0-9.]+)", pos).group(1))
+        n = [int(x) for x in re.search(r"n_particles_per_dimension = \(([0-9, ]+)\)",
+                                        pos).group(1).split(",")]
+        exp = _julia_array(pos[pos.index("expected_coords = ["):])
+        assert len(corners) == len(exp)
+        for corner, coords in zip(corners, exp):
+            cases.append({"ndims": nd, "particle_spacing": spacing, "n": n,
+                          "min_coordinates": corner, "loop_order": "x_first",
+                          "place_on_shell": False, "coordinates": coords})
+        lo = text[text.index('"Loop Orders"'):text.index('"Incompressible Hydrostatic Pressure"')]
+        orders = re.findall(r":(\w+_first)", lo[lo.index("loop_orders = ["):
+                                                lo.index("expected_coords")])
+        exp = _julia_array(lo[lo.index("expected_coords = ["):])
+        assert len(orders) == len(exp)
+        for order, coords in zip(orders, exp):
+            cases.append({"ndims": nd, "particle_spacing": 1.0, "n": [2] * nd,
+                          "min_coordinates": [0.0] * nd, "loop_order": order,
+                          "place_on_shell": True, "coordinates": coords})
+    out = {"source": "test/setups/rectangular_shape.jl (Positions, Loop Orders)",
+           "cases": cases}
+    (HERE / "rectangular_shape_coordinates.json").write_text(json.dumps(out))
 
 
 def _julia_array(text: str):

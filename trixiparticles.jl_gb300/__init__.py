@@ -30,7 +30,8 @@ from .semidiscretization import (
     semidiscretize,
     solve,
 )
-from .setups import InitialCondition, RectangularTank, StateEquationCole, dam_break
+from .setups import InitialCondition, RectangularShape, RectangularTank, StateEquationCole, \
+    dam_break
 from . import adjoint, ensemble, interpolation, vtk
 from .vtk import SolutionSavingCallback, trixi2vtk, vtk2trixi
 from .interpolation import interpolate_line, interpolate_plane_2d, interpolate_plane_3d, \
@@ -40,7 +41,7 @@ __all__ = [
     "AdamiPressureExtrapolation", "ArtificialViscosityMonaghan", "BoundaryModelDummyParticles",
     "CarpenterKennedy2N54", "ContinuityDensity", "DensityDiffusionMolteniColagrossi",
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
-    "ODEProblem", "RectangularTank", "Semidiscretization", "StateEquationCole",
+    "ODEProblem", "RectangularShape", "RectangularTank", "Semidiscretization", "StateEquationCole",
     "SortingCallback", "StepsizeCallback", "SymplecticPositionVerlet", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
     "SolutionSavingCallback", "adjoint", "build", "dam_break", "ensemble", "trixi2vtk",

@@ -30,12 +30,10 @@ def _isapprox(a: float, b: float) -> bool:
     return abs(a - b) <= math.sqrt(EPS) * max(abs(a), abs(b))
 
 
-def rectangular_shape_coords(spacing: float, n_per_dim, min_coords, loop_order=None) -> np.ndarray:
-    """rectangular_shape.jl:196-224 with loop_permutation (:168-194).
-
-    Returns an `(n, ndims)` array.  `loop_order` is None, 'x', 'y' or 'z' as in the reference:
-    linear iteration over `permutedims(CartesianIndices(n), perm)`, first permuted index fastest.
-    """
+def _shape_indices(n_per_dim, loop_order=None) -> list:
+    """The 0-based cartesian index of every particle along each axis, in the order of
+    `permutedims(CartesianIndices(n), loop_permutation(loop_order))` (rectangular_shape.jl:
+    168-224): first permuted index fastest."""
     nd = len(n_per_dim)
     if nd == 2:
         perm = (1, 0) if loop_order == "x" else (0, 1)
@@ -47,6 +45,17 @@ def rectangular_shape_coords(spacing: float, n_per_dim, min_coords, loop_order=N
     for k in range(nd):
         idx[perm[k]] = rem % sizes[k]
         rem = rem // sizes[k]
+    return idx
+
+
+def rectangular_shape_coords(spacing: float, n_per_dim, min_coords, loop_order=None) -> np.ndarray:
+    """rectangular_shape.jl:196-224 with loop_permutation (:168-194).
+
+    Returns an `(n, ndims)` array.  `loop_order` is None, 'x', 'y' or 'z' as in the reference:
+    linear iteration over `permutedims(CartesianIndices(n), perm)`, first permuted index fastest.
+    """
+    nd = len(n_per_dim)
+    idx = _shape_indices(n_per_dim, loop_order)
     out = np.empty((len(idx[0]), nd), dtype=np.float64)
     for d in range(nd):
         out[:, d] = float(min_coords[d]) + spacing * ((idx[d] + 1).astype(np.float64) - 0.5)
@@ -97,6 +106,96 @@ class InitialCondition:
     @property
     def n_particles(self) -> int:
         return self.coordinates.shape[0]
+
+
+_LOOP_ORDERS = {2: {None: None, "y_first": None, "x_first": "x"},
+                3: {None: None, "z_first": None, "y_first": "y", "x_first": "x"}}
+
+
+def hydrostatic_pressure(spacing: float, acceleration, density_fun, n_per_dim,
+                         loop_order=None) -> np.ndarray:
+    """initialize_pressure! (rectangular_shape.jl:226-267): explicit Euler from the surface,
+    half a step above the first particle, along the one axis the acceleration acts on; the
+    levels reversed when it points in the negative direction, then read per particle through
+    the shape's index order."""
+    acc = [float(a) for a in acceleration]
+    if sum(abs(a) > EPS for a in acc) > 1:
+        raise ValueError("ArgumentError: hydrostatic pressure calculation is not supported "
+                         "with diagonal acceleration")
+    ad = next(d for d in range(len(acc)) if abs(acc[d]) > EPS)
+    factor = spacing * abs(acc[ad])
+    p1d = [0.0] * int(n_per_dim[ad])
+    p1d[0] = (0.5 * factor) * density_fun(0.0)
+    for i in range(len(p1d) - 1):
+        p1d[i + 1] = p1d[i] + factor * density_fun(p1d[i])
+    if acc[ad] < 0:
+        p1d.reverse()
+    return np.asarray(p1d, dtype=np.float64)[_shape_indices(n_per_dim, loop_order)[ad]]
+
+
+def RectangularShape(particle_spacing, n_particles_per_dimension, min_coordinates, *,
+                     velocity=None, mass=None, density=None, pressure=0.0, acceleration=None,
+                     state_equation=None, place_on_shell=False,
+                     loop_order=None) -> InitialCondition:
+    """RectangularShape (rectangular_shape.jl:79-151): particles at min_coordinates +
+    (i - 1/2) dx (with place_on_shell the first ones on min_coordinates: the corner moved back by
+    dx / 2 first, :205-209), in `loop_order` (None, "x_first", "y_first", "z_first"); with `acceleration`
+    a hydrostatic pressure column (hydrostatic_pressure) and, with a state equation, the density
+    of every particle from its inverse; mass density dx^d unless given.  Errors as the
+    reference's (ArgumentError)."""
+    dx = float(particle_spacing)
+    if not dx >= EPS:
+        raise ValueError(f"ArgumentError: `particle_spacing` needs to be positive and larger "
+                         f"than {EPS}")
+    n = tuple(int(k) for k in n_particles_per_dimension)
+    nd = len(n)
+    if len(min_coordinates) != nd:
+        raise ValueError(f"ArgumentError: `min_coordinates` must be of length {nd} for a "
+                         f"{nd}D problem")
+    if loop_order not in _LOOP_ORDERS.get(nd, {None: None}):
+        raise ValueError(f"ArgumentError: {loop_order} is not a valid loop order")
+    order = _LOOP_ORDERS.get(nd, {None: None})[loop_order]
+    if density is not None and np.any(np.asarray(density) < EPS):
+        raise ValueError(f"ArgumentError: `density` needs to be positive and larger than {EPS}")
+    corner = [float(c) for c in min_coordinates]
+    if place_on_shell:
+        corner = [c - 0.5 * dx for c in corner]
+    coords = rectangular_shape_coords(dx, n, corner, order)
+    n_p = coords.shape[0]
+    if acceleration is not None:
+        if pressure != 0.0:
+            raise ValueError("ArgumentError: `pressure` cannot be used together with "
+                             "`acceleration` and `state_equation` (hydrostatic pressure "
+                             "gradient)")
+        if state_equation is None:
+            if density is None:
+                raise ValueError("ArgumentError: `density` must be specified when not using "
+                                 "`acceleration` and `state_equation`")
+            rho = float(density)
+            p = hydrostatic_pressure(dx, acceleration, lambda _p: rho, n, order)
+        else:
+            if density is not None:
+                raise ValueError("ArgumentError: `density` cannot be used together with "
+                                 "`acceleration` and `state_equation` (hydrostatic pressure "
+                                 "gradient)")
+            p = hydrostatic_pressure(dx, acceleration, state_equation.inverse, n, order)
+            density = np.array([state_equation.inverse(x) for x in p], dtype=np.float64)
+    else:
+        if state_equation is not None:
+            raise ValueError("ArgumentError: `state_equation` must be used together with "
+                             "`acceleration`")
+        p = np.full(n_p, float(pressure))
+    if density is None:
+        raise ValueError("ArgumentError: `density` must be specified when not using "
+                         "`acceleration` and `state_equation` (hydrostatic pressure gradient)")
+    rho = np.broadcast_to(np.asarray(density, dtype=np.float64), (n_p,)).copy()
+    vol = dx * dx if nd == 2 else ((dx * dx) * dx if nd == 3 else dx)
+    m = rho * vol if mass is None else \
+        np.broadcast_to(np.asarray(mass, dtype=np.float64), (n_p,)).copy()
+    vel = np.zeros_like(coords) if velocity is None else \
+        np.broadcast_to(np.asarray(velocity, dtype=np.float64), coords.shape).copy()
+    return InitialCondition(coordinates=coords, velocity=vel, mass=m, density=rho, pressure=p,
+                            particle_spacing=dx)
 
 
 @dataclass
@@ -172,44 +271,19 @@ class RectangularTank:
             pressure=np.zeros(nw),
             particle_spacing=bdx,
         )
-        coords = rectangular_shape_coords(dx, nfd, [0.0] * nd) + shift
-        nf = coords.shape[0]
-        pressure = np.zeros(nf)
+        # the fluid: a RectangularShape at the tank's corner (rectangular_tank.jl:171-190), with
+        # the hydrostatic column when an acceleration acts (a zero acceleration gives the
+        # density of zero pressure everywhere)
+        acc = self.acceleration
         eos = self.state_equation
-        density = None
-        if self.acceleration is not None:
-            acc = [float(a) for a in self.acceleration]
-            if sum(abs(a) > EPS for a in acc) > 1:
-                raise ValueError("hydrostatic pressure calculation is not supported with "
-                                 "diagonal acceleration")
-            ad = next((d for d in range(nd) if abs(acc[d]) > EPS), None)
-            if ad is not None:
-                dens = (lambda p: eos.inverse(p)) if eos is not None else (lambda p: rho0)
-                factor = dx * abs(acc[ad])
-                p1d = [0.0] * nfd[ad]
-                p1d[0] = (0.5 * factor) * dens(0.0)
-                for i in range(nfd[ad] - 1):
-                    p1d[i + 1] = p1d[i] + factor * dens(p1d[i])
-                if acc[ad] < 0:
-                    p1d.reverse()
-                k = np.arange(nf)
-                strides = [1, nfd[0], nfd[0] * nfd[1]]
-                idx_ad = (k // strides[ad]) % nfd[ad]
-                pressure = np.asarray(p1d, dtype=np.float64)[idx_ad]
-                if eos is not None:  # one inverse-EOS evaluation per hydrostatic level
-                    d1d = np.array([eos.inverse(p) for p in p1d], dtype=np.float64)
-                    density = d1d[idx_ad]
-        if density is None:
-            density = (np.full(nf, eos.inverse(0.0)) if eos is not None else np.full(nf, rho0))
-        fvol = dx * dx if nd == 2 else (dx * dx) * dx
-        self.fluid = InitialCondition(
-            coordinates=coords,
-            velocity=np.zeros_like(coords),
-            mass=fvol * density,
-            density=density,
-            pressure=pressure,
-            particle_spacing=dx,
-        )
+        if acc is not None and any(abs(float(a)) > EPS for a in acc):
+            fluid = RectangularShape(dx, nfd, [0.0] * nd, acceleration=acc, state_equation=eos,
+                                     density=None if eos is not None else rho0)
+        else:
+            fluid = RectangularShape(dx, nfd, [0.0] * nd,
+                                     density=eos.inverse(0.0) if eos is not None else rho0)
+        fluid.coordinates = fluid.coordinates + shift
+        self.fluid = fluid
 
 
 def _initialize_boundaries(bdx, tsz, nbd, n_layers, faces) -> np.ndarray:
