@@ -98,3 +98,26 @@ def test_cut_off_bnd(rest_case):
     keep = model.interpolate(v, u, pts, 0.035, cut_off_bnd=False)
     assert np.isnan(cut["pressure"][0]) and cut["neighbor_count"][0] == 0
     assert np.isfinite(keep["pressure"][0]) and keep["neighbor_count"][0] > 0
+
+
+def test_plane_point_grids(pkg):
+    """The point sets of interpolate_plane_2d (interpolation.jl:183-209) and interpolate_plane_3d
+    (sample_face_with_fixed_size, :787-824) and their argument errors."""
+    I = pkg.interpolation
+    p = I.plane_points_2d((0.0, 0.0), (1.0, 1.0), 0.4)
+    assert p.shape == (2, 16)
+    assert np.allclose(p[:, :4], [[0.0, 0.4, 0.8, 1.2], [0.0] * 4], rtol=0, atol=1e-15)
+    assert np.allclose(p[:, 4], [0.0, 0.4], rtol=0, atol=1e-15)  # x fastest
+    with pytest.raises(ValueError, match="2D coordinates only"):
+        I.plane_points_2d((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), 0.4)
+    with pytest.raises(ValueError, match="smaller than `max_corner`"):
+        I.plane_points_2d((1.0, 0.0), (0.0, 1.0), 0.4)
+    f = I.face_points((0.0, 0.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.5, 0.5), 0.25)
+    n2 = int(np.ceil(np.sqrt(0.5) / 0.25))
+    assert f.shape == (3, 5 * (n2 + 1))
+    assert np.array_equal(f[:, 0], [0.0, 0.0, 0.0]) and np.allclose(f[:, -1], [1.0, 0.5, 0.5])
+    assert np.allclose(f[:, n2], [0.0, 0.5, 0.5])  # the second edge runs fastest
+    with pytest.raises(ValueError, match="must not be collinear"):
+        I.face_points((0.0, 0.0, 0.0), (1.0, 0.0, 0.0), (2.0, 0.0, 0.0), 0.25)
+    with pytest.raises(ValueError, match="3D coordinates"):
+        I.face_points((0.0, 0.0), (1.0, 0.0), (0.0, 1.0), 0.25)
