@@ -51,6 +51,13 @@ def test_rejects_missing_cell_list_and_wall_eos(pkg):
                                parallelization_backend=pkg.GB300Backend())
     bm = dataclasses.replace(w.boundary_model, state_equation=None)
     w2 = dataclasses.replace(w, boundary_model=bm)
-    with pytest.raises(ValueError, match="state_equation"):
+    # test/general/semidiscretization.jl:209-227: the reference's message
+    msg = ("`WeaklyCompressibleSPHSystem` cannot be used without setting a `state_equation` "
+           "for all boundary models")
+    with pytest.raises(ValueError, match=msg.replace("`", ".")):
         pkg.Semidiscretization(f, w2, neighborhood_search=nhs,
+                               parallelization_backend=pkg.GB300Backend())
+    f2 = dataclasses.replace(f, state_equation=None)
+    with pytest.raises(ValueError, match="needs the fluid's `state_equation`"):
+        pkg.Semidiscretization(f2, w, neighborhood_search=nhs,
                                parallelization_backend=pkg.GB300Backend())

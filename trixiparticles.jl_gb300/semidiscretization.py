@@ -161,9 +161,11 @@ class Semidiscretization:
         if bm.viscosity is not None or bm.correction is not None or \
                 w.prescribed_motion is not None:
             raise _argument_error("wall viscosity, corrections and moving walls are not supported")
-        if bm.state_equation is None:
-            raise _argument_error("`state_equation` must be given for the wall model "
-                                  "with WeaklyCompressibleSPHSystem")
+        if bm.state_equation is None:  # the reference's check_configuration message
+            raise _argument_error("`WeaklyCompressibleSPHSystem` cannot be used without setting "
+                                  "a `state_equation` for all boundary models")
+        if f.state_equation is None:
+            raise _argument_error("ContinuityDensity needs the fluid's `state_equation`")
         if not isinstance(bm.smoothing_kernel, WendlandC2Kernel) or \
                 float(bm.smoothing_length) != float(f.smoothing_length):
             raise _argument_error("the wall model must share the fluid's WendlandC2 kernel and "
