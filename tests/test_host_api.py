@@ -36,10 +36,23 @@ def test_rejects_other_kernel_and_models(pkg):
     for change in [dict(smoothing_kernel=pkg.WendlandC2Kernel(3)), dict(correction="shepard"),
                    dict(viscosity="morris"), dict(density_diffusion="antuono"),
                    dict(density_calculator=None)]:
-        f2 = dataclasses.replace(f, **change)
         with pytest.raises(ValueError, match="ArgumentError"):
+            f2 = dataclasses.replace(f, **change)
             pkg.Semidiscretization(f2, w, neighborhood_search=nhs,
                                    parallelization_backend=pkg.GB300Backend())
+
+
+def test_wcsph_constructor_checks(pkg):
+    """test/systems/wcsph_system.jl:3-68: the reference's messages for a wrong acceleration
+    length and kernel dimension; the acceleration defaults to zeros."""
+    import dataclasses
+
+    f, _, _ = _systems(pkg)
+    with pytest.raises(ValueError, match="`acceleration` must be of length 2 for a 2D problem"):
+        dataclasses.replace(f, acceleration=0.0)
+    with pytest.raises(ValueError, match="smoothing kernel dimensionality must be 2 for a 2D"):
+        dataclasses.replace(f, smoothing_kernel=pkg.WendlandC2Kernel(3))
+    assert dataclasses.replace(f, acceleration=None).acceleration == (0.0, 0.0)
 
 
 def test_rejects_missing_cell_list_and_wall_eos(pkg):

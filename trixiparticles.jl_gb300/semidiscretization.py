@@ -81,6 +81,19 @@ class WeaklyCompressibleSPHSystem:
     surface_tension: object = None
     shifting_technique: object = None
 
+    def __post_init__(self):
+        # the constructor's checks and default (weakly_compressible_sph/system.jl:65-174)
+        nd = self.ndims
+        if self.acceleration is None:
+            self.acceleration = (0.0,) * nd
+        acc = tuple(float(a) for a in np.atleast_1d(self.acceleration))
+        if len(acc) != nd:
+            raise _argument_error(f"`acceleration` must be of length {nd} for a {nd}D problem")
+        self.acceleration = acc
+        if getattr(self.smoothing_kernel, "ndims", nd) != nd:
+            raise _argument_error(f"smoothing kernel dimensionality must be {nd} for a {nd}D "
+                                  "problem")
+
     @property
     def ndims(self) -> int:
         return self.initial_condition.ndims
