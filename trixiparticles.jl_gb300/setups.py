@@ -90,14 +90,74 @@ class StateEquationCole:
 
 @dataclass
 class InitialCondition:
-    """InitialCondition: coordinates/velocity `(n, ndims)`, mass/density/pressure `(n,)`."""
+    """InitialCondition (initial_condition.jl:114-215): coordinates/velocity `(n, ndims)`,
+    mass/density/pressure `(n,)`.  As in the reference, velocity, mass, density and pressure may
+    also be given as constants or as functions of a particle's coordinates; without a mass it is
+    density * particle_spacing^ndims (particle_spacing required then); the reference's argument
+    errors are raised as ValueError("ArgumentError: ...")."""
 
     coordinates: np.ndarray
-    velocity: np.ndarray
-    mass: np.ndarray
-    density: np.ndarray
-    pressure: np.ndarray
-    particle_spacing: float
+    velocity: object = None
+    mass: object = None
+    density: object = None
+    pressure: object = 0.0
+    particle_spacing: float = -1.0
+
+    def __post_init__(self):
+        x = np.asarray(self.coordinates, dtype=np.float64)
+        if x.ndim != 2:
+            raise ValueError("ArgumentError: `coordinates` must be an (n, ndims) array")
+        self.coordinates = x
+        n, nd = x.shape
+        if n == 0:
+            self.velocity = np.zeros((0, nd))
+            self.mass = np.zeros(0)
+            self.density = np.zeros(0)
+            self.pressure = np.zeros(0)
+            return
+
+        def per_particle(value, name):
+            if callable(value):
+                return np.array([value(r.copy()) for r in x], dtype=np.float64)
+            a = np.asarray(value, dtype=np.float64)
+            if a.ndim == 0:
+                return np.full(n, float(a))
+            if a.shape != (n,):
+                raise ValueError(f"ArgumentError: Expected: length({name}) == size(coordinates, "
+                                 f"2)\nGot: size(coordinates, 2) = {n}, length({name}) = "
+                                 f"{a.size}")
+            return a
+
+        v = self.velocity
+        if v is None:
+            v = np.zeros((n, nd))
+        elif callable(v) or np.ndim(v) == 1:
+            f = v if callable(v) else (lambda _r, c=np.asarray(v, dtype=np.float64): c)
+            if np.size(f(x[0].copy())) != nd:
+                raise ValueError(f"ArgumentError: `velocity` must be {nd}-dimensional for "
+                                 f"{nd}-dimensional `coordinates`")
+            v = np.array([np.asarray(f(r.copy()), dtype=np.float64) for r in x])
+        v = np.asarray(v, dtype=np.float64)
+        if v.shape != x.shape:
+            raise ValueError("ArgumentError: `coordinates` and `velocities` must be of the "
+                             "same size")
+        self.velocity = v
+        if self.density is None:
+            raise ValueError("ArgumentError: `density` must be given")
+        rho = per_particle(self.density, "density")
+        if np.any(rho < EPS):
+            raise ValueError("ArgumentError: density must be positive and larger than `eps()`")
+        self.density = rho
+        self.pressure = per_particle(self.pressure, "pressure")
+        if self.mass is None:
+            if self.particle_spacing < 0:
+                raise ValueError("ArgumentError: `mass` must be specified when not using "
+                                 "`particle_spacing`")
+            dx = float(self.particle_spacing)
+            vol = dx * dx if nd == 2 else ((dx * dx) * dx if nd == 3 else dx)
+            self.mass = vol * rho
+        else:
+            self.mass = per_particle(self.mass, "mass")
 
     @property
     def ndims(self) -> int:
