@@ -28,9 +28,13 @@ ATM = 101_325.0
     (1.0, [(1, 998.34), (100, 1002.8949541016121), (500, 1021.298809057621),
            (1000, 1044.3036277526319), (3000, 1136.3229025326757), (9000, 1412.380726872807)]),
 ])
-def test_cole_inverse_golden(orc, gamma, golden):
+def test_cole_inverse_golden(orc, pkg, gamma, golden):
+    # the oracle's and the host setup's state equation (used for the hydrostatic initial state)
+    eos = pkg.StateEquationCole(sound_speed=1484.0, reference_density=998.34, exponent=gamma,
+                                background_pressure=1 * ATM)
     for p_atm, rho in golden:
         assert orc.cole_inverse(1484.0, 998.34, gamma, 1 * ATM, p_atm * ATM) == rho
+        assert eos.inverse(p_atm * ATM) == rho
 
 
 @pytest.mark.parametrize("c,gamma,p_bg", [(1484.0, 7.15, 101_325.0), (10.0, 7.0, 10_000.0),
