@@ -18,8 +18,14 @@ pytestmark = pytest.mark.gpu
 def test_reference_interpolation_goldens(pkg, cuda, precision):
     semi, _ = gpu_example_dam_break(pkg, precision)
     ode = pkg.semidiscretize(semi, (0.0, 0.01))
-    sol = pkg.solve(ode, pkg.CarpenterKennedy2N54(), dt=1.0,
-                    callback=pkg.StepsizeCallback(cfl=0.9))
+    if precision == "float64":
+        sol = pkg.solve(ode, pkg.CarpenterKennedy2N54(), dt=1.0,
+                        callback=pkg.StepsizeCallback(cfl=0.9))
+    else:  # the examples' form: CallbackSet with an InfoCallback and `nothing` entries
+        info = pkg.InfoCallback(interval=2)
+        sol = pkg.solve(ode, pkg.CarpenterKennedy2N54(williamson_condition=False), dt=1.0,
+                        callback=pkg.CallbackSet(info, None, pkg.StepsizeCallback(cfl=0.9)))
+        assert len(info.lines) == 2  # after steps 2 and 4 of the five full ones
     assert sol.n_steps == 6 and sol.t == 0.01
     kw = dict(cut_off_bnd=False)
     res = {

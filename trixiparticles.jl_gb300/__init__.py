@@ -18,6 +18,8 @@ from .semidiscretization import (
     GridNeighborhoodSearch,
     ODEProblem,
     Semidiscretization,
+    CallbackSet,
+    InfoCallback,
     SortingCallback,
     StepsizeCallback,
     SymplecticPositionVerlet,
@@ -42,7 +44,7 @@ __all__ = [
     "CarpenterKennedy2N54", "ContinuityDensity", "DensityDiffusionMolteniColagrossi",
     "FullGridCellList", "GB300Backend", "GridNeighborhoodSearch", "InitialCondition",
     "ODEProblem", "RectangularShape", "RectangularTank", "Semidiscretization", "StateEquationCole",
-    "SortingCallback", "StepsizeCallback", "SymplecticPositionVerlet", "TpConfig",
+    "SortingCallback", "StepsizeCallback", "CallbackSet", "InfoCallback", "SymplecticPositionVerlet", "TpConfig",
     "TpError", "WallBoundarySystem", "WeaklyCompressibleSPHSystem", "WendlandC2Kernel",
     "SolutionSavingCallback", "adjoint", "build", "dam_break", "ensemble", "trixi2vtk",
     "vtk", "vtk2trixi", "interpolate_line", "interpolate_points", "interpolate_plane_2d",

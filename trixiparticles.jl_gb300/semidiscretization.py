@@ -399,6 +399,28 @@ class SymplecticPositionVerlet:
     by rho_prev (2 - eps) / (2 + eps))."""
 
 
+def CallbackSet(*callbacks) -> list:
+    """CallbackSet(callbacks...) as the reference's examples build it: the callbacks in order,
+    `nothing` entries (None here) dropped; `solve` takes the list."""
+    return [c for c in callbacks if c is not None]
+
+
+class InfoCallback:
+    """InfoCallback(; interval=0) (src/callbacks/info.jl): a progress line every `interval` steps
+    (interval 0: none) with the step count, the step size and the simulation time."""
+
+    def __init__(self, *, interval: int = 0):
+        if int(interval) < 0:
+            raise _argument_error("`interval` must be non-negative")
+        self.interval = int(interval) if int(interval) > 0 else None
+        self.lines = []
+
+    def report(self, steps: int, dt: float, t: float) -> None:
+        line = f"#timesteps: {steps:10d} | dt: {dt:.4e} | sim. time: {t:.4e}"
+        self.lines.append(line)
+        print(line, flush=True)
+
+
 class StepsizeCallback:
     """StepsizeCallback(; cfl) (src/callbacks/stepsize.jl:35-75): at initialisation the
     integrator's fixed step becomes calculate_dt of the semidiscretization, the minimum over its
@@ -492,8 +514,9 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
     library's fused integrators; v/u of the result are new tensors.  Without `n_steps` the run
     ends on tspan[1] as OrdinaryDiffEq's does (fixed_step_schedule: the last step shortened);
     with it, exactly `n_steps` steps of `dt`.  `callback`: SortingCallback and/or
-    SolutionSavingCallback (one or a list), applied between integrator calls at their step /
-    time intervals, and StepsizeCallback, whose step replaces `dt`."""
+    SolutionSavingCallback and InfoCallback (one, a list or a CallbackSet), applied between
+    integrator calls at their step / time intervals, and StepsizeCallback, whose step replaces
+    `dt`."""
     if not isinstance(alg, (CarpenterKennedy2N54, SymplecticPositionVerlet)):
         raise _argument_error("only CarpenterKennedy2N54 and SymplecticPositionVerlet are "
                               "provided by the GB300 backend")
@@ -503,13 +526,15 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
     cbs = callback if isinstance(callback, (list, tuple)) else \
         ([] if callback is None else [callback])
     for c in cbs:
-        if not isinstance(c, (SortingCallback, SolutionSavingCallback, StepsizeCallback)):
-            raise _argument_error("only SortingCallback, SolutionSavingCallback and "
-                                  "StepsizeCallback are supported as callbacks")
+        if not isinstance(c, (SortingCallback, SolutionSavingCallback, StepsizeCallback,
+                              InfoCallback)):
+            raise _argument_error("only SortingCallback, SolutionSavingCallback, "
+                                  "StepsizeCallback and InfoCallback are supported as callbacks")
     for c in cbs:  # the step size callback overwrites `dt` before the first step
         if isinstance(c, StepsizeCallback):
             dt = c.calculate_dt(semi)
-    cbs = [c for c in cbs if not isinstance(c, StepsizeCallback)]
+    cbs = [c for c in cbs if not isinstance(c, StepsizeCallback) and
+           not (isinstance(c, InfoCallback) and c.interval is None)]
     t0, t1 = ode.tspan
     last = None
     if n_steps is None:
@@ -548,6 +573,8 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
             if isinstance(c, SortingCallback):
                 perm = c.sort(semi, v, u, perm)
                 c.last_t = t
+            elif isinstance(c, InfoCallback):
+                c.report(done, dt, t)
             else:
                 c.save(semi, v, u, t)
     t_end = t0 + n_steps * dt
