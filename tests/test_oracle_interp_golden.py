@@ -10,6 +10,7 @@ size rule and the interpolation together.
 import math
 
 import numpy as np
+import pytest
 
 from helpers import INTERP_RTOL, gpu_example_dam_break, initial_state, interp_golden_errors, \
     oracle_model
@@ -26,6 +27,12 @@ def test_stepsize_callback_and_schedule(pkg):
     assert n == 5 and abs(last - (0.01 - 5 * dt)) < 1e-15
     assert sched(0.0, 1.0, 0.1) == (10, None)  # lands on the end within 100 ulp: no extra step
     assert sched(0.0, 0.25, 0.1)[0] == 2
+    assert sched(0.5, 0.5, 0.1) == (0, None)  # empty span
+    assert sched(0.0, 0.05, 0.1) == (0, 0.05)  # one shortened step
+    n, last = sched(0.0, 1.0, 0.1 * (1 - 1e-15))  # ends within 100 ulp of tspan[1]: snapped
+    assert n == 10 and last is None
+    with pytest.raises(ValueError, match="dt must be positive"):
+        sched(0.0, 1.0, 0.0)
 
 
 def test_oracle_matches_reference_interpolation(pkg, orc):
