@@ -74,3 +74,22 @@ def test_rejects_missing_cell_list_and_wall_eos(pkg):
     with pytest.raises(ValueError, match="needs the fluid's `state_equation`"):
         pkg.Semidiscretization(f2, w, neighborhood_search=nhs,
                                parallelization_backend=pkg.GB300Backend())
+
+
+def test_callback_mirrors(pkg):
+    """CallbackSet drops `nothing` entries; InfoCallback's interval; StepsizeCallback's rule
+    without viscosity and gravity is the sound-speed limit cfl h / c (fluid.jl:199-229)."""
+    import dataclasses
+
+    info = pkg.InfoCallback(interval=100)
+    st = pkg.StepsizeCallback(cfl=0.5)
+    assert pkg.CallbackSet(None, info, None, st) == [info, st]
+    assert pkg.InfoCallback().interval is None
+    with pytest.raises(ValueError, match="non-negative"):
+        pkg.InfoCallback(interval=-1)
+    f, w, nhs = _systems(pkg)
+    f0 = dataclasses.replace(f, viscosity=None, acceleration=(0.0, 0.0))
+    semi = pkg.Semidiscretization(f0, w, neighborhood_search=nhs,
+                                  parallelization_backend=pkg.GB300Backend())
+    h, c = f0.smoothing_length, f0.state_equation.sound_speed
+    assert st.calculate_dt(semi) == 0.5 * h / c
