@@ -209,4 +209,6 @@ def tank_faces(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path of the TrixiParticles.jl source tree>")
+    main(sys.argv[1])
