@@ -22,9 +22,14 @@ import numpy as np
 
 _VTK_TYPES = {np.dtype(np.float64): "Float64", np.dtype(np.float32): "Float32",
               np.dtype(np.int64): "Int64", np.dtype(np.int32): "Int32",
-              np.dtype(np.uint8): "UInt8"}
+              np.dtype(np.uint8): "UInt8", np.dtype(np.uint32): "UInt32",
+              np.dtype(np.uint64): "UInt64", np.dtype(np.int8): "Int8",
+              np.dtype(np.int16): "Int16", np.dtype(np.uint16): "UInt16"}
 _NP_TYPES = {v: k for k, v in _VTK_TYPES.items()}
 VTK_VERTEX = 1
+# the `solver_version` field data of the reference's files holds its git hash; ours names the
+# library
+SOLVER_VERSION = "trixiparticles.jl_gb300"
 
 
 def _block(a: np.ndarray, compress: bool) -> bytes:
@@ -62,6 +67,11 @@ def write_vtu(filename: str, points: np.ndarray, point_data: dict, field_data: d
     if field_data:
         fd = ET.SubElement(grid, "FieldData")
         for name, val in field_data.items():
+            if isinstance(val, str):  # a vtkStringArray: byte values, closed by a 0, in ASCII
+                ET.SubElement(fd, "DataArray", type="String", Name=name, NumberOfTuples="1",
+                              format="ascii").text = " ".join(
+                                  [str(b) for b in val.encode()] + ["0"])
+                continue
             a = np.atleast_1d(np.asarray(val))
             if a.dtype.kind == "i":
                 a = a.astype(np.int64)
@@ -107,39 +117,93 @@ def write_vtu(filename: str, points: np.ndarray, point_data: dict, field_data: d
     return fn
 
 
-def _decode(buf: bytes, pos: int, dtype: np.dtype, compressed: bool) -> np.ndarray:
+def _decode(buf: bytes, pos: int, dtype: np.dtype, compressed: bool,
+            header: str = "UInt64") -> np.ndarray:
+    """One data block at buf[pos:]: [UInt32|UInt64 header][payload]; compressed blocks carry the
+    vtkZLibDataCompressor header (number of blocks, block size, last block size, sizes)."""
+    f, w = ("<Q", 8) if header == "UInt64" else ("<I", 4)
     if compressed:
-        nb, bs, last = struct.unpack_from("<QQQ", buf, pos)
-        sizes = struct.unpack_from("<" + "Q" * nb, buf, pos + 24)
-        p = pos + 24 + 8 * nb
-        raw = b""
+        (nb,) = struct.unpack_from(f, buf, pos)
+        sizes = struct.unpack_from("<" + f[1] * nb, buf, pos + 3 * w)
+        p = pos + (3 + nb) * w
+        parts = []
         for s in sizes:
-            raw += zlib.decompress(buf[p:p + s])
+            parts.append(zlib.decompress(buf[p:p + s]))
             p += s
+        raw = b"".join(parts)
     else:
-        (nbytes,) = struct.unpack_from("<Q", buf, pos)
-        raw = buf[pos + 8:pos + 8 + nbytes]
+        (nbytes,) = struct.unpack_from(f, buf, pos)
+        raw = buf[pos + w:pos + w + nbytes]
     return np.frombuffer(raw, dtype=dtype.newbyteorder("<")).astype(dtype)
 
 
+def _inline_binary(text: str, dtype: np.dtype, compressed: bool, header: str) -> np.ndarray:
+    """format="binary": base64 text; a compressed array encodes its header and its payload as two
+    separate base64 runs, an uncompressed one encodes [header][payload] as one."""
+    import base64
+
+    t = "".join(text.split())
+    if not compressed:
+        return _decode(base64.b64decode(t), 0, dtype, False, header)
+    w = 8 if header == "UInt64" else 4
+    f = "<Q" if w == 8 else "<I"
+    # the header is 3 + nb words; its base64 run has ceil(bytes / 3) * 4 characters
+    (nb,) = struct.unpack_from(f, base64.b64decode(t[:((w + 2) // 3) * 4])[:w])
+    hbytes = (3 + nb) * w
+    hchars = ((hbytes + 2) // 3) * 4
+    head = base64.b64decode(t[:hchars])[:hbytes]
+    payload = base64.b64decode(t[hchars:])
+    return _decode(head + payload, 0, dtype, True, header)
+
+
+def _string_ascii(text: str) -> str:
+    """A vtkStringArray in ASCII: byte values, each string closed by a 0."""
+    codes = [int(x) for x in text.split()]
+    return bytes(c for c in codes if c != 0).decode()
+
+
 def read_vtu(filename: str) -> dict:
-    """Points, point data and field data of a .vtu with appended raw data (compressed or not),
-    as WriteVTK writes them."""
+    """Points, point data and field data of an UnstructuredGrid .vtu as WriteVTK.jl (and VTK)
+    write them: appended raw data, inline base64 ("binary") or ASCII arrays, zlib-compressed or
+    not, UInt32 or UInt64 headers; string arrays (ASCII) come back as str."""
     buf = open(filename, "rb").read()
-    start = buf.index(b"<AppendedData")
-    us = buf.index(b"_", start) + 1
-    end = buf.rindex(b"</AppendedData>")
-    xml = buf[:start].decode() + "<AppendedData/>" + buf[end + len(b"</AppendedData>"):].decode()
+    data = b""
+    if b"<AppendedData" in buf:
+        start = buf.index(b"<AppendedData")
+        us = buf.index(b"_", start) + 1
+        end = buf.rindex(b"</AppendedData>")
+        data = buf[us:end]
+        xml = (buf[:start].decode() + "<AppendedData/>"
+               + buf[end + len(b"</AppendedData>"):].decode())
+    else:
+        xml = buf.decode()
     root = ET.fromstring(xml)
+    if root.get("type") != "UnstructuredGrid":
+        raise ValueError(f"{filename}: not an UnstructuredGrid file")
+    if root.get("byte_order", "LittleEndian") != "LittleEndian":
+        raise ValueError(f"{filename}: only little-endian files are supported")
     compressed = root.get("compressor") is not None
-    if root.get("header_type", "UInt32") != "UInt64":
-        raise ValueError("only UInt64 headers are supported")
-    data = buf[us:end]
+    header = root.get("header_type", "UInt32")
+    if header not in ("UInt32", "UInt64"):
+        raise ValueError(f"{filename}: unsupported header_type {header}")
     piece = root.find("UnstructuredGrid/Piece")
     n = int(piece.get("NumberOfPoints"))
 
     def arr(e):
-        a = _decode(data, int(e.get("offset")), _NP_TYPES[e.get("type")], compressed)
+        typ, fmt = e.get("type"), e.get("format", "ascii")
+        if typ == "String":
+            if fmt != "ascii":
+                raise ValueError(f"{filename}: string arrays are read in ASCII only")
+            return _string_ascii(e.text or "")
+        dtype = _NP_TYPES[typ]
+        if fmt == "appended":
+            a = _decode(data, int(e.get("offset")), dtype, compressed, header)
+        elif fmt == "binary":
+            a = _inline_binary(e.text or "", dtype, compressed, header)
+        elif fmt == "ascii":
+            a = np.array((e.text or "").split(), dtype=np.float64).astype(dtype)
+        else:
+            raise ValueError(f"{filename}: unsupported DataArray format {fmt}")
         k = int(e.get("NumberOfComponents", "1"))
         return a.reshape(-1, k) if k > 1 else a
 
@@ -179,7 +243,7 @@ def vtk2trixi(filename: str) -> dict:
             res[k] = v
     for k, v in d["field_data"].items():
         if k not in ("ndims", "time"):
-            res[k] = v[0] if np.size(v) == 1 else v
+            res[k] = v if isinstance(v, str) else (v[0] if np.size(v) == 1 else v)
     return res
 
 
@@ -235,7 +299,8 @@ def trixi2vtk(semi, v_ode, u_ode, t: float, *, output_directory: str = "out", pr
         pdata = dict(pdata)
         pdata["index"] = np.arange(1, n + 1, dtype=np.int64)
         pdata["particle_spacing"] = np.full(n, float(spacing))
-        f = write_vtu(fn, pts, pdata, {"time": float(t), "ndims": int(semi.ndims)})
+        f = write_vtu(fn, pts, pdata, {"time": float(t), "ndims": int(semi.ndims),
+                                       "solver_version": SOLVER_VERSION})
         files.append(f)
         if iter is not None and collections is not None:
             collections.setdefault(base, []).append((t, f))
