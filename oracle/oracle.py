@@ -51,6 +51,9 @@ def lib():
         L.orc_last_state.argtypes = [c_void_p, dp, dp, dp, dp]
         L.orc_integrate_ck2n54.restype = c_int
         L.orc_integrate_ck2n54.argtypes = [c_void_p, dp, dp, c_double, c_int64]
+        L.orc_integrate_ck2n54_jvp.restype = c_int
+        L.orc_integrate_ck2n54_jvp.argtypes = [c_void_p, dp, dp, dp, dp, dp, dp, dp, c_double,
+                                               c_int64, dp, dp]
         L.orc_ck2n54_coefficients.argtypes = [dp, dp, dp]
         L.orc_sort_perm.restype = c_int
         L.orc_sort_perm.argtypes = [c_void_p, dp, c_int64, ip]
@@ -177,6 +180,28 @@ class Model:
         u = np.array(u, dtype=np.float64).reshape(-1)
         st = self.L.orc_integrate_ck2n54(self.h, _dp(v), _dp(u), dt, n_steps)
         return v, u, st
+
+
+def integrate_jvp(cfg, x_w, m_w, m_f, v, u, dt: float, n_steps: int, v_dir=None, u_dir=None):
+    """Forward-mode derivatives (dual numbers through the oracle's own CK2N54 and right-hand
+    side) of n_steps steps from (v, u): returns (v, u, dv, du, status) where dv[k], du[k] are the
+    derivatives of the final state along direction k = Monaghan alpha, Molteni-Colagrossi delta,
+    gravity magnitude, initial state along (v_dir, u_dir)."""
+    L = lib()
+    v = np.array(v, dtype=np.float64).reshape(-1)
+    u = np.array(u, dtype=np.float64).reshape(-1)
+    keep = [np.ascontiguousarray(x_w, dtype=np.float64).reshape(-1),
+            np.ascontiguousarray(m_w, dtype=np.float64), np.ascontiguousarray(m_f, np.float64)]
+    vd = None if v_dir is None else np.ascontiguousarray(v_dir, np.float64).reshape(-1)
+    ud = None if u_dir is None else np.ascontiguousarray(u_dir, np.float64).reshape(-1)
+    dv = np.zeros((4, v.size))
+    du = np.zeros((4, u.size))
+    null = ctypes.POINTER(c_double)()
+    st = L.orc_integrate_ck2n54_jvp(ctypes.byref(cfg), *[_dp(a) for a in keep], _dp(v), _dp(u),
+                                    _dp(vd) if vd is not None else null,
+                                    _dp(ud) if ud is not None else null, dt, n_steps, _dp(dv),
+                                    _dp(du))
+    return v, u, dv, du, st
 
 
 def nhs(cfg, x_f: np.ndarray, x_w: np.ndarray):

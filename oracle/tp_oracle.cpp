@@ -27,8 +27,11 @@
 #include <vector>
 
 #include "../include/tp_wcsph.h"
+#include "dual.h"
 
 namespace {
+
+using orc::val;
 
 constexpr double kPi = 3.141592653589793;  // Float64(pi)
 constexpr double kEps = 2.220446049250313e-16;  // eps(Float64)
@@ -44,26 +47,30 @@ inline double wc2_norm(int nd, double h_inv) {
 }
 
 // kernel_unsafe(::WendlandC2Kernel), smoothing_kernels.jl:436-441 (@fastpow: t^4 = (t*t)^2).
-inline double wc2_kernel_unsafe(int nd, double r, double h) {
+// T: double, or a dual number for forward-mode derivatives (dual.h); h is a constant.
+template <class T>
+inline T wc2_kernel_unsafe(int nd, T r, double h) {
     double h_inv = 1.0 / h;
-    double q = r * h_inv;
-    double t = 1.0 - q / 2.0;
-    double t2 = t * t;
-    double t4 = t2 * t2;
+    T q = r * h_inv;
+    T t = 1.0 - q / 2.0;
+    T t2 = t * t;
+    T t4 = t2 * t2;
     return (wc2_norm(nd, h_inv) * t4) * (2.0 * q + 1.0);
 }
 
 // kernel(kernel, r, h), smoothing_kernels.jl:30-34: zero outside the compact support 2h.
-inline double wc2_kernel(int nd, double r, double h) {
-    return (r < 2.0 * h) ? wc2_kernel_unsafe(nd, r, h) : 0.0;
+template <class T>
+inline T wc2_kernel(int nd, T r, double h) {
+    return (r < 2.0 * h) ? wc2_kernel_unsafe(nd, r, h) : T(0.0);
 }
 
 // kernel_deriv_div_r_unsafe(::WendlandC2Kernel), smoothing_kernels.jl:443-448.
-inline double wc2_deriv_div_r(int nd, double r, double h) {
+template <class T>
+inline T wc2_deriv_div_r(int nd, T r, double h) {
     double h_inv = 1.0 / h;
-    double q = r * h_inv;
-    double t = 1.0 - q / 2.0;
-    double t3 = (t * t) * t;
+    T q = r * h_inv;
+    T t = 1.0 - q / 2.0;
+    T t3 = (t * t) * t;
     return ((-5.0 * wc2_norm(nd, h_inv)) * t3) * (h_inv * h_inv);
 }
 
@@ -89,20 +96,27 @@ struct Eos {
     double rho0, c, gamma, p_bg;
     bool clip;
     double B() const { return (rho0 * (c * c)) / gamma; }
-    double pressure(double rho) const {
-        double p = B() * (std::pow(rho / rho0, gamma) - 1.0) + p_bg;
-        if (clip) p = (std::isnan(p) || p > 0.0) ? p : 0.0;  // max(0, p)
+    template <class T>
+    T pressure(T rho) const {
+        using std::pow;
+        using std::isnan;
+        T p = B() * (pow(rho / rho0, gamma) - 1.0) + p_bg;
+        if (clip) p = (isnan(p) || p > 0.0) ? p : T(0.0);  // max(0, p)
         return p;
     }
-    double inverse(double p) const {
-        double tmp = (p - p_bg) / B() + 1.0;
-        return rho0 * std::pow(tmp, 1.0 / gamma);
+    template <class T>
+    T inverse(T p) const {
+        using std::pow;
+        T tmp = (p - p_bg) / B() + 1.0;
+        return rho0 * pow(tmp, 1.0 / gamma);
     }
 };
 
-inline double clip_nonneg(double p) {  // max(p, 0) with Julia's NaN / signed-zero rules
-    if (std::isnan(p)) return p;
-    return (p > 0.0) ? p : 0.0;
+template <class T>
+inline T clip_nonneg(T p) {  // max(p, 0) with Julia's NaN / signed-zero rules
+    using std::isnan;
+    if (isnan(p)) return p;
+    return (p > 0.0) ? p : T(0.0);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -157,12 +171,15 @@ struct CellList {
     std::vector<int32_t> order;  // sorted position -> particle
     std::vector<int64_t> start;  // ncells + 1
     bool ok = true;
-    void build(const Grid& g, const double* x, int64_t n) {
+    template <class T>
+    void build(const Grid& g, const T* x, int64_t n) {
         key.assign(n, 0);
         ok = true;
         for (int64_t i = 0; i < n; ++i) {
             int64_t c[3];
-            if (!g.cell_of(x + i * g.nd, c)) ok = false;
+            double xv[3] = {0.0, 0.0, 0.0};
+            for (int d = 0; d < g.nd; ++d) xv[d] = val(x[i * g.nd + d]);
+            if (!g.cell_of(xv, c)) ok = false;
             key[i] = (int32_t)g.key(c);
         }
         order.resize(n);
@@ -176,12 +193,16 @@ struct CellList {
 };
 
 // Visits the neighbours b (of a list over coordinates xb) of the point xa in PointNeighbors
-// order; f(b, pos_diff, distance) for every b with |xa - xb|^2 <= sr^2.
-template <class F>
-inline void foreach_neighbor(const Grid& g, const CellList& cl, const double* xb, const double* xa,
+// order; f(b, pos_diff, distance) for every b with |xa - xb|^2 <= sr^2 (decided on the values).
+template <class TA, class TB, class F>
+inline void foreach_neighbor(const Grid& g, const CellList& cl, const TB* xb, const TA* xa,
                              double sr, F&& f) {
+    using std::sqrt;
+    using T = decltype(xa[0] - xb[0]);
     int64_t c[3];
-    g.cell_of(xa, c);
+    double xav[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < g.nd; ++d) xav[d] = val(xa[d]);
+    g.cell_of(xav, c);
     const int nd = g.nd;
     const double sr2 = sr * sr;
     int64_t zlo = (nd == 3) ? c[2] - 1 : 0, zhi = (nd == 3) ? c[2] + 1 : 0;
@@ -191,22 +212,27 @@ inline void foreach_neighbor(const Grid& g, const CellList& cl, const double* xb
                 int64_t k = cx + g.n[0] * (cy + g.n[1] * cz);
                 for (int64_t s = cl.start[k]; s < cl.start[k + 1]; ++s) {
                     int32_t b = cl.order[s];
-                    double pd[3] = {0, 0, 0};
+                    T pd[3] = {T(0.0), T(0.0), T(0.0)};
                     for (int d = 0; d < nd; ++d) pd[d] = xa[d] - xb[b * nd + d];
-                    double d2 = pd[0] * pd[0] + pd[1] * pd[1];
+                    T d2 = pd[0] * pd[0] + pd[1] * pd[1];
                     if (nd == 3) d2 = d2 + pd[2] * pd[2];
-                    if (d2 <= sr2) f(b, pd, std::sqrt(d2));
+                    if (val(d2) <= sr2) f(b, pd, sqrt(d2));
                 }
             }
 }
 
-inline double dot(int nd, const double* a, const double* b) {
-    double s = a[0] * b[0] + a[1] * b[1];
+template <class TA, class TB>
+inline auto dot(int nd, const TA* a, const TB* b) -> decltype(a[0] * b[0]) {
+    auto s = a[0] * b[0] + a[1] * b[1];
     if (nd == 3) s = s + a[2] * b[2];
     return s;
 }
 
-struct Model {
+// T = double: the oracle.  T = orc::Dual<N>: the same arithmetic carrying N directional
+// derivatives (forward mode); masses and wall positions are constants, the state and the
+// parameters alpha, delta and gravity are differentiable.
+template <class T>
+struct ModelT {
     tp_config cfg;
     Grid grid;
     Eos eos_f, eos_w;
@@ -215,9 +241,11 @@ struct Model {
     std::vector<double> xw, mw, mf;
     CellList wall_cl;
     // Per-kick outputs.
-    std::vector<double> pf, pw, rhow, volw;
+    std::vector<T> pf, pw, rhow, volw;
     CellList fluid_cl;
     bool grid_ok = true;
+    // Monaghan alpha, Molteni-Colagrossi delta, gravity (the configuration's values)
+    T alpha_p, delta_p, grav[3];
 
     bool init(const tp_config& c) {
         cfg = c;
@@ -229,15 +257,18 @@ struct Model {
                  c.fluid_clip_negative_pressure != 0};
         eos_w = eos_f;
         eos_w.clip = false;
-        pf.assign(nf, 0.0);
-        pw.assign(nw, 0.0);
-        rhow.assign(nw, c.reference_density);
-        volw.assign(nw, 0.0);
+        pf.assign(nf, T(0.0));
+        pw.assign(nw, T(0.0));
+        rhow.assign(nw, T(c.reference_density));
+        volw.assign(nw, T(0.0));
+        alpha_p = c.viscosity_alpha;
+        delta_p = c.density_diffusion_delta;
+        for (int d = 0; d < 3; ++d) grav[d] = c.acceleration[d];
         return true;
     }
 
     // compute_pressure! (weakly_compressible_sph/system.jl:426-438).
-    void fluid_pressure(const double* v) {
+    void fluid_pressure(const T* v) {
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < nf; ++i) pf[i] = eos_f.pressure(v[i * (nd + 1) + nd]);
     }
@@ -245,23 +276,23 @@ struct Model {
     // compute_pressure!(::AdamiPressureExtrapolation) (dummy_particles.jl:489-569) with the
     // gather boundary_pressure_extrapolation!(Val(true)) and boundary_pressure_inner!
     // (dummy_particles.jl:586-606, 637-672).
-    void adami(const double* v, const double* u) {
+    void adami(const T* v, const T* u) {
         const double h = cfg.smoothing_length;
         const double sr = 2.0 * h;  // compact_support(wall, fluid) = model's 2h
-        const double* g = cfg.acceleration;
+        const T* g = grav;
 #pragma omp parallel for schedule(dynamic, 64)
         for (int64_t w = 0; w < nw; ++w) {
-            double P = 0.0, V = 0.0;
+            T P = 0.0, V = 0.0;
             foreach_neighbor(grid, fluid_cl, u, &xw[w * nd], sr,
-                             [&](int32_t f, const double* pd, double r) {
-                                 double rho_f = v[f * (nd + 1) + nd];
-                                 double p_f = pf[f];
-                                 double ra[3] = {g[0] - 0.0, g[1] - 0.0, g[2] - 0.0};
-                                 double rpd[3] = {rho_f * pd[0], rho_f * pd[1],
-                                                  nd == 3 ? rho_f * pd[2] : 0.0};
-                                 double hp = dot(nd, ra, rpd);
-                                 double sum = ((cfg.pressure_offset + p_f) + 0.0) + hp;
-                                 double W = wc2_kernel(nd, r, h);
+                             [&](int32_t f, const T* pd, T r) {
+                                 T rho_f = v[f * (nd + 1) + nd];
+                                 T p_f = pf[f];
+                                 T ra[3] = {g[0] - 0.0, g[1] - 0.0, g[2] - 0.0};
+                                 T rpd[3] = {rho_f * pd[0], rho_f * pd[1],
+                                             nd == 3 ? rho_f * pd[2] : T(0.0)};
+                                 T hp = dot(nd, ra, rpd);
+                                 T sum = ((cfg.pressure_offset + p_f) + 0.0) + hp;
+                                 T W = wc2_kernel(nd, r, h);
                                  P += sum * W;
                                  V += W;
                              });
@@ -275,21 +306,21 @@ struct Model {
 
     // kick! (semidiscretization.jl:589-612) for the fluid system; the wall contributes no
     // ODE rows (wall_boundary/system.jl:78-90).
-    void kick(double* dv, const double* v, const double* u) {
+    void kick(T* dv, const T* v, const T* u) {
         const double h = cfg.smoothing_length;
         const double sr = 2.0 * h;
         const double sr2 = sr * sr;
         // almostzero = sqrt(eps(compact_support^2)), rhs.jl:27-28; eps(x) = ulp spacing at x.
         const double almostzero = std::sqrt(std::nextafter(sr2, INFINITY) - sr2);
         const double c = cfg.sound_speed;
-        const double alpha = cfg.viscosity_alpha, beta = cfg.viscosity_beta,
-                     epsv = cfg.viscosity_epsilon, delta = cfg.density_diffusion_delta;
+        const T alpha = alpha_p, delta = delta_p;
+        const double beta = cfg.viscosity_beta, epsv = cfg.viscosity_epsilon;
         const bool visc = cfg.viscosity_model == TP_VISCOSITY_MONAGHAN;
         const bool diff = cfg.density_diffusion_model == TP_DIFFUSION_MOLTENI_COLAGROSSI;
         const int nv = nd + 1;
 
         // set_zero!(dv_ode), :600
-        std::fill(dv, dv + nf * nv, 0.0);
+        std::fill(dv, dv + nf * nv, T(0.0));
         // update_nhs!, neighborhood_search.jl:479-519
         fluid_cl.build(grid, u, nf);
         grid_ok = fluid_cl.ok && wall_cl.ok;
@@ -300,33 +331,33 @@ struct Model {
         // system_interaction!: (fluid, fluid) then (fluid, wall), rhs.jl:5-127
 #pragma omp parallel for schedule(dynamic, 64)
         for (int64_t a = 0; a < nf; ++a) {
-            const double* xa = u + a * nd;
-            const double* va = v + a * nv;
-            const double rho_a = va[nd];
-            const double p_a = pf[a];
+            const T* xa = u + a * nd;
+            const T* va = v + a * nv;
+            const T rho_a = va[nd];
+            const T p_a = pf[a];
             // ---- fluid-fluid ----
-            double dva[3] = {0, 0, 0}, drho = 0.0;
-            foreach_neighbor(grid, fluid_cl, u, xa, sr, [&](int32_t b, const double* pd, double r) {
+            T dva[3] = {T(0.0), T(0.0), T(0.0)}, drho = 0.0;
+            foreach_neighbor(grid, fluid_cl, u, xa, sr, [&](int32_t b, const T* pd, T r) {
                 if (r < almostzero) return;
-                double s = wc2_deriv_div_r(nd, r, h);
-                double grad[3] = {s * pd[0], s * pd[1], nd == 3 ? s * pd[2] : 0.0};
+                T s = wc2_deriv_div_r(nd, r, h);
+                T grad[3] = {s * pd[0], s * pd[1], nd == 3 ? s * pd[2] : T(0.0)};
                 const double m_b = mf[b];
-                const double* vb = v + b * nv;
-                const double rho_b = vb[nd];
-                const double p_b = pf[b];
+                const T* vb = v + b * nv;
+                const T rho_b = vb[nd];
+                const T p_b = pf[b];
                 // pressure_acceleration_continuity_density, pressure_acceleration.jl:34-41
-                double coef = (-m_b) * ((p_a + p_b) / (rho_a * rho_b));
+                T coef = (-m_b) * ((p_a + p_b) / (rho_a * rho_b));
                 for (int d = 0; d < nd; ++d) dva[d] = dva[d] + coef * grad[d];
-                double vd[3] = {va[0] - vb[0], va[1] - vb[1], nd == 3 ? va[2] - vb[2] : 0.0};
+                T vd[3] = {va[0] - vb[0], va[1] - vb[1], nd == 3 ? va[2] - vb[2] : T(0.0)};
                 // ArtificialViscosityMonaghan, viscosity.jl:99-132
                 if (visc) {
-                    double vr = dot(nd, vd, pd);
+                    T vr = dot(nd, vd, pd);
                     if (vr < 0.0) {
                         double hh = (h + h) / 2.0;
-                        double rho_mean = (rho_a + rho_b) / 2.0;
-                        double mu = (hh * vr) / (r * r + epsv * (hh * hh));
-                        double num = ((m_b * alpha) * c) * mu + (m_b * beta) * (mu * mu);
-                        double f = num / rho_mean;
+                        T rho_mean = (rho_a + rho_b) / 2.0;
+                        T mu = (hh * vr) / (r * r + epsv * (hh * hh));
+                        T num = ((m_b * alpha) * c) * mu + (m_b * beta) * (mu * mu);
+                        T f = num / rho_mean;
                         for (int d = 0; d < nd; ++d) dva[d] = dva[d] + f * grad[d];
                     }
                 }
@@ -334,10 +365,10 @@ struct Model {
                 drho = drho + ((rho_a / rho_b) * m_b) * dot(nd, vd, grad);
                 // density_diffusion! Molteni-Colagrossi, density_diffusion.jl:49-55, 213-240
                 if (diff) {
-                    double volume_b = m_b / rho_b;
-                    double pc = (2.0 * (rho_a - rho_b)) / (r * r);
-                    double psi[3] = {pc * pd[0], pc * pd[1], nd == 3 ? pc * pd[2] : 0.0};
-                    double term = volume_b * dot(nd, psi, grad);
+                    T volume_b = m_b / rho_b;
+                    T pc = (2.0 * (rho_a - rho_b)) / (r * r);
+                    T psi[3] = {pc * pd[0], pc * pd[1], nd == 3 ? pc * pd[2] : T(0.0)};
+                    T term = volume_b * dot(nd, psi, grad);
                     double havg = (h + h) / 2.0;
                     drho = drho + ((delta * havg) * c) * term;
                 }
@@ -345,25 +376,25 @@ struct Model {
             for (int d = 0; d < nd; ++d) dv[a * nv + d] = dv[a * nv + d] + dva[d];
             dv[a * nv + nd] = dv[a * nv + nd] + drho;
             // ---- fluid-wall ----
-            double dvw[3] = {0, 0, 0}, drhow = 0.0;
+            T dvw[3] = {T(0.0), T(0.0), T(0.0)}, drhow = 0.0;
             foreach_neighbor(grid, wall_cl, xw.data(), xa, sr,
-                             [&](int32_t b, const double* pd, double r) {
+                             [&](int32_t b, const T* pd, T r) {
                                  if (r < almostzero) return;
-                                 double s = wc2_deriv_div_r(nd, r, h);
-                                 double grad[3] = {s * pd[0], s * pd[1], nd == 3 ? s * pd[2] : 0.0};
+                                 T s = wc2_deriv_div_r(nd, r, h);
+                                 T grad[3] = {s * pd[0], s * pd[1], nd == 3 ? s * pd[2] : T(0.0)};
                                  const double m_b = mw[b];
-                                 const double rho_b = rhow[b];
-                                 const double p_b = pw[b];
-                                 double coef = (-m_b) * ((p_a + p_b) / (rho_a * rho_b));
+                                 const T rho_b = rhow[b];
+                                 const T p_b = pw[b];
+                                 T coef = (-m_b) * ((p_a + p_b) / (rho_a * rho_b));
                                  for (int d = 0; d < nd; ++d) dvw[d] = dvw[d] + coef * grad[d];
-                                 double vd[3] = {va[0] - 0.0, va[1] - 0.0,
-                                                 nd == 3 ? va[2] - 0.0 : 0.0};
+                                 T vd[3] = {va[0] - 0.0, va[1] - 0.0,
+                                            nd == 3 ? va[2] - 0.0 : T(0.0)};
                                  drhow = drhow + ((rho_a / rho_b) * m_b) * dot(nd, vd, grad);
                              });
             for (int d = 0; d < nd; ++d) dv[a * nv + d] = dv[a * nv + d] + dvw[d];
             dv[a * nv + nd] = dv[a * nv + nd] + drhow;
             // add_source_terms! -> add_acceleration!, semidiscretization.jl:701-731
-            for (int d = 0; d < nd; ++d) dv[a * nv + d] = dv[a * nv + d] + cfg.acceleration[d];
+            for (int d = 0; d < nd; ++d) dv[a * nv + d] = dv[a * nv + d] + grav[d];
         }
     }
 
@@ -441,7 +472,7 @@ struct Model {
     }
 
     // drift! -> set_velocity!, semidiscretization.jl:561-571 (delta_v = 0).
-    void drift(double* du, const double* v) const {
+    void drift(T* du, const T* v) const {
         for (int64_t i = 0; i < nf; ++i)
             for (int d = 0; d < nd; ++d) du[i * nd + d] = v[i * (nd + 1) + d];
     }
@@ -463,6 +494,42 @@ const double kC[5] = {0.0,
                       2526269341429.0 / 6820363962896.0,
                       2006345519317.0 / 3224310063776.0,
                       2802321613138.0 / 2924317926251.0};
+
+using Model = ModelT<double>;
+
+// n_steps CarpenterKennedy2N54 steps at fixed dt, in place on (v, u); the stage update
+// tmp = A_i tmp + dt k; x += B_i tmp with fused multiply-adds (the @muladd of
+// OrdinaryDiffEqLowStorageRK).  Returns 0, or 3 if a particle left the grid.
+template <class T>
+int integrate_ck2n54(ModelT<T>* m, T* v, T* u, double dt, int64_t n_steps) {
+    using std::fma;
+    const int64_t nvv = m->nf * (m->nd + 1), nuu = m->nf * m->nd;
+    std::vector<T> kv(nvv), ku(nuu), tv(nvv), tu(nuu);
+    const T dtt = dt;
+    int status = 0;
+    for (int64_t step = 0; step < n_steps; ++step) {
+        for (int s = 0; s < 5; ++s) {
+            if (s > 0) {
+                for (int64_t i = 0; i < nvv; ++i) tv[i] = kA[s] * tv[i];
+                for (int64_t i = 0; i < nuu; ++i) tu[i] = kA[s] * tu[i];
+            }
+            m->kick(kv.data(), v, u);
+            if (!m->grid_ok) status = 3;
+            m->drift(ku.data(), v);
+            if (s == 0) {
+                for (int64_t i = 0; i < nvv; ++i) tv[i] = dt * kv[i];
+                for (int64_t i = 0; i < nuu; ++i) tu[i] = dt * ku[i];
+            } else {
+                for (int64_t i = 0; i < nvv; ++i) tv[i] = fma(dtt, kv[i], tv[i]);
+                for (int64_t i = 0; i < nuu; ++i) tu[i] = fma(dtt, ku[i], tu[i]);
+            }
+            const T bs = kB[s];
+            for (int64_t i = 0; i < nvv; ++i) v[i] = fma(bs, tv[i], v[i]);
+            for (int64_t i = 0; i < nuu; ++i) u[i] = fma(bs, tu[i], u[i]);
+        }
+    }
+    return status;
+}
 
 }  // namespace
 
@@ -511,31 +578,52 @@ void orc_last_state(orc_model* p, double* pf, double* pw, double* rhow, double* 
 
 // n_steps CarpenterKennedy2N54 steps at fixed dt, in place on (v, u).
 int orc_integrate_ck2n54(orc_model* p, double* v, double* u, double dt, int64_t n_steps) {
-    Model* m = reinterpret_cast<Model*>(p);
-    const int64_t nvv = m->nf * (m->nd + 1), nuu = m->nf * m->nd;
-    std::vector<double> kv(nvv), ku(nuu), tv(nvv), tu(nuu);
-    int status = 0;
-    for (int64_t step = 0; step < n_steps; ++step) {
-        for (int s = 0; s < 5; ++s) {
-            if (s > 0) {
-                for (int64_t i = 0; i < nvv; ++i) tv[i] = kA[s] * tv[i];
-                for (int64_t i = 0; i < nuu; ++i) tu[i] = kA[s] * tu[i];
-            }
-            m->kick(kv.data(), v, u);
-            if (!m->grid_ok) status = 3;
-            m->drift(ku.data(), v);
-            if (s == 0) {
-                for (int64_t i = 0; i < nvv; ++i) tv[i] = dt * kv[i];
-                for (int64_t i = 0; i < nuu; ++i) tu[i] = dt * ku[i];
-            } else {
-                for (int64_t i = 0; i < nvv; ++i) tv[i] = std::fma(dt, kv[i], tv[i]);
-                for (int64_t i = 0; i < nuu; ++i) tu[i] = std::fma(dt, ku[i], tu[i]);
-            }
-            for (int64_t i = 0; i < nvv; ++i) v[i] = std::fma(kB[s], tv[i], v[i]);
-            for (int64_t i = 0; i < nuu; ++i) u[i] = std::fma(kB[s], tu[i], u[i]);
-        }
+    return integrate_ck2n54(reinterpret_cast<Model*>(p), v, u, dt, n_steps);
+}
+
+// Forward-mode derivatives (dual numbers, dual.h) of n_steps CarpenterKennedy2N54 steps from
+// (v, u): four directions -- Monaghan alpha, Molteni-Colagrossi delta, the gravity magnitude
+// (along the configured acceleration) and the initial state along (v_dir, u_dir) (either may be
+// null = zero).  (v, u) are advanced in place (their values equal orc_integrate_ck2n54's);
+// dv_out (4 x n_fluid*(ndims+1)) and du_out (4 x n_fluid*ndims) receive the derivatives of
+// the final state, direction by direction.  Returns 0, 1 (bad configuration) or 3.
+int orc_integrate_ck2n54_jvp(const tp_config* cfg, const double* x_wall, const double* m_wall,
+                             const double* m_fluid, double* v, double* u, const double* v_dir,
+                             const double* u_dir, double dt, int64_t n_steps, double* dv_out,
+                             double* du_out) {
+    using D = orc::Dual<4>;
+    ModelT<D> m;
+    if (!m.init(*cfg)) return 1;
+    m.xw.assign(x_wall, x_wall + cfg->n_wall * cfg->ndims);
+    m.mw.assign(m_wall, m_wall + cfg->n_wall);
+    m.mf.assign(m_fluid, m_fluid + cfg->n_fluid);
+    m.wall_cl.build(m.grid, m.xw.data(), cfg->n_wall);
+    m.alpha_p.d[0] = 1.0;
+    m.delta_p.d[1] = 1.0;
+    double gn = 0.0;
+    for (int d = 0; d < 3; ++d) gn += cfg->acceleration[d] * cfg->acceleration[d];
+    gn = std::sqrt(gn);
+    for (int d = 0; d < 3; ++d) m.grav[d].d[2] = gn > 0.0 ? cfg->acceleration[d] / gn : 0.0;
+    const int64_t nvv = cfg->n_fluid * (cfg->ndims + 1), nuu = cfg->n_fluid * cfg->ndims;
+    std::vector<D> vd(nvv), ud(nuu);
+    for (int64_t i = 0; i < nvv; ++i) {
+        vd[i] = v[i];
+        vd[i].d[3] = v_dir ? v_dir[i] : 0.0;
     }
-    return status;
+    for (int64_t i = 0; i < nuu; ++i) {
+        ud[i] = u[i];
+        ud[i].d[3] = u_dir ? u_dir[i] : 0.0;
+    }
+    const int st = integrate_ck2n54(&m, vd.data(), ud.data(), dt, n_steps);
+    for (int64_t i = 0; i < nvv; ++i) {
+        v[i] = vd[i].v;
+        for (int k = 0; k < 4; ++k) dv_out[k * nvv + i] = vd[i].d[k];
+    }
+    for (int64_t i = 0; i < nuu; ++i) {
+        u[i] = ud[i].v;
+        for (int k = 0; k < 4; ++k) du_out[k * nuu + i] = ud[i].d[k];
+    }
+    return st;
 }
 
 // SymplecticPositionVerlet (ext/TrixiParticlesOrdinaryDiffEqSymplecticRKExt.jl:89-171), the
