@@ -81,3 +81,61 @@ def test_noalloc_rejects_oversize_and_reports_out_of_grid(pkg, lib, cuda):
     st, cell, order = _noalloc(lib, semi.config, ode.u0, n, torch, semi.device)
     assert st == 0  # the error word is cleared per call
     semi.close()
+
+
+def _grid_cells(cfg, nd):
+    """Cell count of the grid that tp_create / tp_cell_sort_noalloc lay over cfg's corners."""
+    import math
+
+    cs = 2.0 * cfg.smoothing_length
+    total = 1
+    for d in range(nd):
+        lo = math.floor(cfg.min_corner[d] / cs) - 1
+        hi = math.floor(cfg.max_corner[d] / cs) + 1
+        total *= hi - lo + 1
+    return total
+
+
+def test_noalloc_rejects_too_many_cells(pkg, lib, cuda):
+    """A grid one cell row beyond TP_NOALLOC_MAX_CELLS is refused before any GPU work."""
+    torch = cuda
+    semi, tank = dam_break_case(pkg, 2, 0.05, (1.0, 0.5), (2.0, 1.0))
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    cfg = type(semi.config).from_buffer_copy(semi.config)
+    cs = 2.0 * cfg.smoothing_length
+    cfg.min_corner[0] = cfg.min_corner[1] = 0.0
+    cfg.max_corner[0] = 509.5 * cs   # 512 cells along x (one padding cell each side)
+    cfg.max_corner[1] = 1022.5 * cs  # 1025 cells along y
+    assert _grid_cells(cfg, 2) == pkg._abi.TP_NOALLOC_MAX_CELLS + 512
+    st, cell, order = _noalloc(lib, cfg, ode.u0, semi.n_fluid, torch, semi.device)
+    assert st == pkg._abi.TP_ERR_CAPACITY
+    assert bool((cell == -1).all()) and bool((order == -1).all())  # nothing was written
+    semi.close()
+
+
+def test_noalloc_grid_at_cell_limit_matches_handle(pkg, lib, cuda):
+    """A grid of exactly TP_NOALLOC_MAX_CELLS cells (the cell starts then end at the last slot
+    before the scan partials of the fixed array) sorts as the handle path does."""
+    import math
+
+    torch = cuda
+    semi, tank = dam_break_case(pkg, 2, 0.05, (1.0, 0.5), (2.0, 1.0), jitter=0.3, seed=4)
+    cfg = semi.config
+    cs = 2.0 * cfg.smoothing_length
+    # keep the tank's min corner (walls must lie inside the box) and widen the box to 512 x 1024
+    # cells: n = floor(max / cs) - floor(min / cs) + 3 along each axis
+    for d, n in ((0, 512), (1, 1024)):
+        cfg.max_corner[d] = (math.floor(cfg.min_corner[d] / cs) + n - 3 + 0.5) * cs
+    assert _grid_cells(cfg, 2) == pkg._abi.TP_NOALLOC_MAX_CELLS
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    u = ode.u0
+    r = semi.nhs_debug(u)
+    semi.sync()
+    ref_cell, ref_order = r["cell"].clone(), r["order"].clone()
+    for _ in range(2):
+        st, cell, order = _noalloc(lib, semi.config, u, semi.n_fluid, torch, semi.device)
+        assert st == 0
+        torch.cuda.synchronize()
+        assert torch.equal(cell, ref_cell)
+        assert torch.equal(order, ref_order)
+    semi.close()

@@ -11,15 +11,17 @@
 // coordinates and the two output arrays.
 //
 // The array below is a device symbol: its name in host code is only a host-side stand-in, so
-// host code never passes it to a kernel.  The first call on a device (with that device
-// current) resolves its device address once with cudaGetSymbolAddress and caches it; that
-// first call should therefore come before any stream capture.  Every later call on the device
-// reuses the same scratch: the histogram and the error word are cleared at the start of each
-// call, everything else is overwritten, and calls that overlap on the GPU (two streams, or
-// two host threads) race on the shared scratch and must be serialised by the caller.
+// host code never passes it to a kernel.  Every call looks up its device address with
+// cudaGetSymbolAddress in the context that is current at the call (a lookup allocates nothing),
+// so a caller that switches contexts (CUDA.jl and other driver-API hosts can make a non-primary
+// context current) or resets the device between calls never receives an address of another
+// context.  Every call shares the same scratch: the histogram and the error word are cleared at
+// the start of each call, everything else is overwritten, and calls that overlap on the GPU (two
+// streams, or two host threads) race on the shared scratch and must be serialised by the caller.
+// The call is synchronous (it waits for `stream` to read the error word back), so it must not be
+// issued while its stream is being captured into a CUDA graph.
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "tp_api_internal.h"
 #include "tp_nhs.cuh"
@@ -37,26 +39,14 @@ constexpr size_t kScratchInts =
 
 static __device__ __align__(256) int g_sort_scratch[kScratchInts];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-int* g_scratch_ptr[kMaxDevices] = {};
-
 inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 
-// Device address of the scratch array on the current device (resolved once per device).
-cudaError_t scratch_on_current_device(int** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+// Device address of the scratch array in the current context.
+cudaError_t scratch_in_current_context(int** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = (int*)p;
-    }
-    *out = g_scratch_ptr[dev];
+    *out = (int*)p;
     return cudaSuccess;
 }
 
@@ -96,7 +86,7 @@ extern "C" tp_status tp_cell_sort_noalloc(const tp_config* cfg, const double* u,
     if (n == 0) return TP_OK;
 
     int* base = nullptr;
-    if (scratch_on_current_device(&base) != cudaSuccess) return TP_ERR_CUDA;
+    if (scratch_in_current_context(&base) != cudaSuccess) return TP_ERR_CUDA;
     int* key = base;
     int* tmp = key + kMaxParticles;
     int* skey = tmp + kMaxParticles;
@@ -127,6 +117,8 @@ extern "C" tp_status tp_cell_sort_noalloc(const tp_config* cfg, const double* u,
     if (cudaMemcpyAsync(cell, key, (size_t)ni * sizeof(int), cudaMemcpyDeviceToDevice, s) !=
         cudaSuccess)
         return TP_ERR_CUDA;
+    // the error word comes back through a pageable host int: the copy is staged by the driver,
+    // and the synchronisation below is what makes `bits` valid to read
     int bits = 0;
     if (cudaMemcpyAsync(&bits, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return TP_ERR_CUDA;
