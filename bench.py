@@ -7,15 +7,25 @@ WendlandC2, Cole EOS (gamma 7, c = 20 sqrt(9.81)), Monaghan alpha 0.02, Molteni-
 0.1, Adami walls, gravity -9.81, CarpenterKennedy2N54 at dt = 5e-5.  One step = one CK2N54 step
 (5 RHS evaluations + the fused 2N update).  particle-steps/s = (n_fluid + n_wall) * steps / s.
 
+Timed window: the dam break in motion.  Before the window (untimed) the precision form advances
+the hydrostatic start by --flow-time seconds of physical time (default 0.2 s = 4000 steps; the
+collapsing column then moves at up to ~2 m/s, so the neighbour search is rebuilt every few
+steps); the FP64 drop-in takes that state, runs --warmup steps and then the --steps timed steps.
+The line carries the number of neighbour-search rebuilds inside the window, the same window
+from the hydrostatic start (`at_rest`, where no rebuild happens) and with a rebuild at every stage
+(`rebuild_every_stage`, skin 0: the reference's update_nhs! schedule).
+
 The `forms` object adds the precision form (FP32 pair arithmetic) and the FP64 drop-in on the
-finer dx = 0.0064 geometry, with the FP32-vs-FP64 field errors after the timed steps.
+finer dx = 0.0064 geometry over the same kind of window (flowing start, same --steps), with the
+FP32-vs-FP64 field errors after the timed steps.
 
 Synthetic data: the inputs are the reference's own dam-break setup (RectangularTank with
 hydrostatic density), generated here; no dataset is involved.  The state (> 300 MB) is larger
 than the 129 MB L2, so no L2 flush is needed between steps.
 
 --impl reference: the FP64 CPU restatement of the reference (oracle/, OpenMP on all host cores)
-on the same workload; each timed step is one full CK2N54 step of the full state.
+on the same workload; each timed step is one full CK2N54 step of the full state (the oracle
+rebuilds its cell list at every stage, so its cost per step does not depend on the start state).
 """
 from __future__ import annotations
 
@@ -62,19 +72,19 @@ def load_peaks():
 
 
 def load_profile_value(key: str, kernel: str):
-    """`key[kernel]: value` line of the committed ncu summaries (profiles/*.md)."""
+    """`key[kernel]: value` line of the committed ncu summaries (profiles/*.md): (value, file)."""
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
             if line.startswith(f"{key}[{kernel}]:"):
                 try:
-                    return float(line.split(":", 1)[1].split()[0])
+                    return float(line.split(":", 1)[1].split()[0]), f"profiles/{f.name}"
                 except ValueError:
-                    return None
-    return None
+                    return None, f"profiles/{f.name}"
+    return None, None
 
 
 def load_traffic(kernel: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary: (value, file)."""
     return load_profile_value("traffic_bytes_per_launch", kernel)
 
 
@@ -180,23 +190,102 @@ def roofline_for(precision, nf, nw, stages, pair_ms, hbm, peak_kind, kernel):
     bytes_launch = nf * bf + nw * bw
     avg_s = pair_ms / 1e3 / stages
     achieved = bytes_launch / avg_s / 1e9
-    traffic = load_traffic(kernel)
+    traffic, tsrc = load_traffic(kernel)
+    fp64, fsrc = load_profile_value("fp64_pipe_active_pct", kernel)
+    issue, isrc = load_profile_value("issue_active_pct", kernel)
+    l1, lsrc = load_profile_value("l1tex_throughput_pct", kernel)
     return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 2),
             "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
             "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
             "bytes_per_launch": bytes_launch, "avg_launch_ms": round(pair_ms / stages, 4),
             "traffic": traffic,
-            # what bounds the kernel instead (ncu, committed summary of the same workload)
-            "fp64_pipe_active_pct": load_profile_value("fp64_pipe_active_pct", kernel),
-            "issue_active_pct": load_profile_value("issue_active_pct", kernel)}
+            # what bounds the kernel instead; these four are NOT measured in this run: they are
+            # copied from the committed ncu summary of the same kernel and workload
+            "from_profiles": {"traffic": tsrc, "fp64_pipe_active_pct": fp64,
+                              "issue_active_pct": issue, "l1tex_throughput_pct": l1,
+                              "source": fsrc or isrc or lsrc or tsrc}}
 
 
-def e2e_run(pkg, torch, semi, ode, steps, dt):
+def flow_state(pkg, torch, cfg, device, flow_steps):
+    """Untimed prefix: the precision form advances the hydrostatic dam break `flow_steps`
+    CarpenterKennedy2N54 steps; returns the state (device tensors, caller order) and seconds."""
+    semi, _ = make_case(pkg, cfg, "float32", device)
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    v, u = ode.v0.clone(), ode.u0.clone()
+    semi._set_stream()
+    t0 = time.perf_counter()
+    if flow_steps:
+        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(cfg["dt"]), ctypes.c_int64(flow_steps))
+    semi.sync()
+    el = time.perf_counter() - t0
+    semi.close()
+    del ode
+    return v, u, el
+
+
+def rebuilds(semi):
+    c = ctypes.c_int64()
+    semi._call("tp_rebuild_count", ctypes.byref(c))
+    return int(c.value)
+
+
+def timed_window(torch, semi, v, u, steps, warmup, dt, clk=None, dist=None):
+    """`warmup` untimed steps, then `steps` timed CK2N54 steps of (v, u) in one fused call
+    (CUDA events on the launching stream, synchronised on both sides); phase times from the
+    library's event pool; rebuilds of the neighbour search inside the timed steps."""
+    lib = semi._lib
+    semi._set_stream()
+    if warmup:
+        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(dt), ctypes.c_int64(warmup))
+    semi.sync()
+    r0 = rebuilds(semi)
+    lib.tp_enable_timing(semi._handle, 1)
+    l0 = lib.tp_kernel_launches(semi._handle)
+    stream = torch.cuda.current_stream(semi.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    import contextlib
+
+    with (clk if clk is not None else contextlib.nullcontext()):
+        e0.record(stream)
+        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
+                   ctypes.c_double(dt), ctypes.c_int64(steps))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    semi.sync()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = lib.tp_kernel_launches(semi._handle) - l0
+    ph = (ctypes.c_double * 3)()
+    lib.tp_phase_times(semi._handle, ph, 3)
+    lib.tp_enable_timing(semi._handle, 0)
+    return {"ms": ms, "launches": int(launches), "phases": list(ph),
+            "rebuilds": rebuilds(semi) - r0}
+
+
+def phases_per_step(ph, steps):
+    return {"update nhs": ph[0] / steps, "compute boundary pressure": ph[1] / steps,
+            "system interaction": ph[2] / steps}
+
+
+def workload_config(cfg, nf, nw):
+    """The `config` object of both arms (the same keys and values)."""
+    return {"workload": cfg["name"], "n_fluid": nf, "n_wall": nw, "particles": nf + nw,
+            "dx": cfg["dx"], "dt": cfg["dt"],
+            "l2": "inputs larger than L2 (state + records > 300 MB), no flush"}
+
+
+def e2e_run(pkg, torch, semi, v0, u0, steps, dt):
     """Through the public C ABI with HOST buffers: every step copies the state host->device from
     pinned memory, advances one CK2N54 step and reads the result back to pinned memory."""
-    v_h = ode.v0.cpu().pin_memory()
-    u_h = ode.u0.cpu().pin_memory()
-    v_d, u_d = torch.empty_like(ode.v0), torch.empty_like(ode.u0)
+    v_h = v0.cpu().pin_memory()
+    u_h = u0.cpu().pin_memory()
+    v_d, u_d = torch.empty_like(v0), torch.empty_like(u0)
     stream = torch.cuda.current_stream(semi.device)
     semi._set_stream()
     torch.cuda.synchronize()
@@ -215,18 +304,16 @@ def e2e_run(pkg, torch, semi, ode, steps, dt):
     return el, nbytes
 
 
-def cpu_baseline(semi, tank, cfg, threads=None):
-    """Bounded CPU sample: one full CK2N54 step of the same state with the FP64 oracle."""
+def cpu_baseline(semi, tank, cfg, v, u, state):
+    """Bounded CPU sample: full CK2N54 steps of the same state (host arrays v (N, 4), u (N, 3))
+    with the FP64 oracle on all host cores."""
     import __graft_entry__ as g
 
     orc = g.load_oracle()
     orc.build()
     model = orc.Model(semi.config, tank.boundary.coordinates, tank.boundary.mass,
                       tank.fluid.mass)
-    nd = 3
-    v = np.zeros((tank.fluid.n_particles, nd + 1))
-    v[:, nd] = tank.fluid.density
-    u = tank.fluid.coordinates.copy()
+    v, u = v.copy(), u.copy()
     t0 = time.perf_counter()
     steps = 0
     while steps < 8 and (steps == 0 or time.perf_counter() - t0 < 10.0):
@@ -237,7 +324,7 @@ def cpu_baseline(semi, tank, cfg, threads=None):
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{steps} CarpenterKennedy2N54 steps (5 RHS each) of the full workload "
-                      f"({n} particles) with the FP64 C++ oracle, OpenMP, {el:.1f} s"}
+                      f"({n} particles, {state}) with the FP64 C++ oracle, OpenMP, {el:.1f} s"}
 
 
 def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
@@ -467,6 +554,7 @@ def run_reference(args):
     v[:, 3] = tank.fluid.density
     u = tank.fluid.coordinates.copy()
     n = tank.fluid.n_particles + tank.boundary.n_particles
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     warm = min(args.warmup, 1)
     steps = max(1, min(args.steps, 2))
     for _ in range(warm):
@@ -476,13 +564,14 @@ def run_reference(args):
         v, u, st = model.integrate(v, u, CFG1["dt"], 1)
     el = time.perf_counter() - t0
     val = n * steps / el
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     line = {"metric": METRIC, "value": val, "unit": UNIT, "impl": "reference",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": CFG1["name"], "n_fluid": tank.fluid.n_particles,
-                       "n_wall": tank.boundary.n_particles, "parallelism": "host threads"},
+            "config": workload_config(CFG1, tank.fluid.n_particles, tank.boundary.n_particles),
+            "parallelism": f"host threads ({cores})",
+            "start_state": "hydrostatic start (the oracle rebuilds its cell list at every "
+                           "stage, so the cost of a step does not depend on the state)",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{steps} full CarpenterKennedy2N54 steps of the "
                                        f"workload (Julia is absent: the C++ FP64 oracle stands "
@@ -502,17 +591,26 @@ def run_profile_form(args):
     cfg = {"cfg1": CFG1, "cfg2": CFG2}[wl]
     pkg = g.load_package()
     pkg.load_library()
+    flow_steps = int(round(args.profile_flow_time / cfg["dt"]))
+    if flow_steps:
+        v_f, u_f, _ = flow_state(pkg, torch, cfg, 0, flow_steps)
     semi, tank = make_case(pkg, cfg, prec, 0)
     ode = pkg.semidiscretize(semi, (0.0, 1.0))
     if args.pair_mode is not None:
         semi._call("tp_set_pair_mode", args.pair_mode)
-    v, u, ms, launches, ph = run_form(pkg, torch, semi, ode, args.steps, args.warmup, cfg["dt"],
-                                      prec)
+    if flow_steps:
+        win = timed_window(torch, semi, v_f, u_f, args.steps, args.warmup, cfg["dt"])
+        ms, launches, ph, reb = win["ms"], win["launches"], win["phases"], win["rebuilds"]
+    else:
+        v, u, ms, launches, ph = run_form(pkg, torch, semi, ode, args.steps, args.warmup,
+                                          cfg["dt"], prec)
+        reb = None
     n = semi.n_fluid + semi.n_wall
-    print(json.dumps({"profile_form": args.profile_form, "n_fluid": semi.n_fluid,
+    print(json.dumps({"profile_form": args.profile_form, "pair_mode": args.pair_mode,
+                      "flow_time": args.profile_flow_time, "n_fluid": semi.n_fluid,
                       "n_wall": semi.n_wall, "steps": args.steps, "ms_per_step": ms / args.steps,
                       "value": n * args.steps / (ms / 1e3), "launches": launches,
-                      "phase_ms": ph}), flush=True)
+                      "rebuilds": reb, "phase_ms": ph}), flush=True)
     semi.close()
     return 0
 
@@ -557,6 +655,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--flow-time", type=float, default=0.2,
+                    help="physical time (s) the precision form advances the dam break before "
+                         "the timed window (untimed); 0 = hydrostatic start")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-forms", action="store_true", help="skip the dx=0.0064 form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -567,11 +668,15 @@ def main():
     ap.add_argument("--profile-form", default=None, metavar="PRECISION:WORKLOAD",
                     help="profiling mode (e.g. float32:cfg2): only warm-up + timed steps of that "
                          "form, one summary line; used under ncu")
+    ap.add_argument("--profile-flow-time", type=float, default=0.0,
+                    help="--profile-form: start from the dam break advanced this many seconds "
+                         "by the precision form (untimed; default 0 = hydrostatic start)")
     ap.add_argument("--profile-ensemble", action="store_true",
                     help="profiling mode of the batching form: default launch shape, one warm-up "
                          "replay and --steps replays of the ensemble graph; used under ncu")
-    ap.add_argument("--pair-mode", type=int, default=None, choices=[0, 1],
-                    help="FP64 pair pass of --profile-form: 0 gather, 1 symmetric")
+    ap.add_argument("--pair-mode", type=int, default=None, choices=[0, 1, 2],
+                    help="pair pass of --profile-form: 0 gather (lists), 1 symmetric (FP64), "
+                         "2 tiled (FP32)")
     ap.add_argument("--precision-study", action="store_true",
                     help="FP32 form vs FP64 drop-in errors after 100/500/1000 steps (dx=0.0064, "
                          "lattice and jittered starts); prints one JSON line")
@@ -613,50 +718,41 @@ def main():
     pkg.load_library()
     hbm, peak_kind = load_peaks()
 
+    dt = CFG1["dt"]
+    flow_steps = int(round(args.flow_time / dt))
+    # untimed prefix: the dam break in motion (precision form, then handed to the FP64 drop-in)
+    v_flow, u_flow, flow_s = flow_state(pkg, torch, CFG1, local, flow_steps)
+
     semi, tank = make_case(pkg, CFG1, "float64", local)
     ode = pkg.semidiscretize(semi, (0.0, 1.0))
     nf, nw = semi.n_fluid, semi.n_wall
     ntot = nf + nw
-    dt = CFG1["dt"]
 
-    # warm-up + timed region (barrier + synchronize on both sides, max over ranks)
-    v, u = ode.v0.clone(), ode.u0.clone()
-    semi._set_stream()
-    if args.warmup:
-        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
-                   ctypes.c_double(dt), ctypes.c_int64(args.warmup))
-    semi.sync()
-    lib = semi._lib
-    lib.tp_enable_timing(semi._handle, 1)
-    l0 = lib.tp_kernel_launches(semi._handle)
-    stream = torch.cuda.current_stream(semi.device)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
-                   ctypes.c_double(dt), ctypes.c_int64(args.steps))
-        e1.record(stream)
-        torch.cuda.synchronize()
-    semi.sync()
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    launches = lib.tp_kernel_launches(semi._handle) - l0
-    ph = (ctypes.c_double * 3)()
-    lib.tp_phase_times(semi._handle, ph, 3)
-    lib.tp_enable_timing(semi._handle, 0)
+    # timed window on the flowing state (barrier + synchronize on both sides, max over ranks)
+    v, u = v_flow.clone(), u_flow.clone()
+    clk = ClockSampler(local)
+    win = timed_window(torch, semi, v, u, args.steps, args.warmup, dt, clk=clk, dist=dist)
+    ms = win["ms"]
+    ph = win["phases"]
     value, ms_max = replica_value(dist, ms, ntot, args.steps, semi.device)
     stages = 5 * args.steps
     bf, bw = BYTES_STAGE["float64"]
     step_bytes = 5 * (nf * bf + nw * bw)
 
-    # end to end through the C ABI with host buffers
+    # the same window from the hydrostatic start (no particle moves far enough for a rebuild)
+    v0, u0 = ode.v0.clone(), ode.u0.clone()
+    rest = timed_window(torch, semi, v0, u0, args.steps, args.warmup, dt)
+    del v0, u0
+
+    # end to end through the C ABI with host buffers, from the flowing state
     e2e_steps = max(1, min(args.steps, 10))
-    el, nbytes = e2e_run(pkg, torch, semi, ode, e2e_steps, dt)
+    el, nbytes = e2e_run(pkg, torch, semi, v_flow, u_flow, e2e_steps, dt)
     e2e_val = ntot * e2e_steps * world / el
+
+    # the reference's schedule: cell list and neighbour lists rebuilt at every stage (skin 0)
+    semi._call("tp_set_skin", ctypes.c_double(0.0))
+    v, u = v_flow.clone(), u_flow.clone()
+    every = timed_window(torch, semi, v, u, args.steps, args.warmup, dt)
 
     out = None
     if rank == 0:
@@ -665,10 +761,14 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": CFG1["name"], "n_fluid": nf, "n_wall": nw,
-                       "particles": ntot, "dx": CFG1["dx"], "dt": dt,
-                       "l2": "inputs larger than L2 (state + records > 300 MB), no flush",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": workload_config(CFG1, nf, nw),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "window": {"start_state": f"dam break in motion: hydrostatic start advanced "
+                                      f"{flow_steps} steps (t = {args.flow_time:g} s) by the "
+                                      f"precision form, untimed ({flow_s:.1f} s), then "
+                                      f"{args.warmup} FP64 warm-up steps",
+                       "rebuilds_in_window": win["rebuilds"],
+                       "rebuilds_per_step": win["rebuilds"] / args.steps},
             "roofline": roofline_for("float64", nf, nw, stages, ph[2], hbm, peak_kind,
                                      "k_pair64"),
             "step_roofline": {"bytes_per_step": step_bytes,
@@ -676,39 +776,52 @@ def main():
                                                     / 1e9, 2),
                               "frac": round(step_bytes / (ms_max / args.steps / 1e3) / 1e9
                                             / hbm, 4)},
-            "phase_ms_per_step": {"update nhs": ph[0] / args.steps,
-                                  "compute boundary pressure": ph[1] / args.steps,
-                                  "system interaction": ph[2] / args.steps},
+            "phase_ms_per_step": phases_per_step(ph, args.steps),
+            "at_rest": {"value": ntot * args.steps / (rest["ms"] / 1e3),
+                        "ms_per_step": rest["ms"] / args.steps,
+                        "rebuilds_in_window": rest["rebuilds"],
+                        "phase_ms_per_step": phases_per_step(rest["phases"], args.steps)},
+            "rebuild_every_stage": {"value": ntot * args.steps / (every["ms"] / 1e3),
+                                    "ms_per_step": every["ms"] / args.steps,
+                                    "rebuilds_in_window": every["rebuilds"],
+                                    "phase_ms_per_step": phases_per_step(every["phases"],
+                                                                         args.steps)},
             "e2e": {"value": e2e_val, "unit": UNIT, "steps": e2e_steps,
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
-            "gpu_launches": int(launches),
+            "gpu_launches": win["launches"],
             "clocks": clk.summary(),
         }
     semi.close()
     del ode
 
-    # precision forms on the finer geometry (rank 0 only, not part of the timed value)
+    # precision forms on the finer geometry over the same kind of window (rank 0 only)
     if rank == 0 and not args.no_forms:
-        k = max(1, min(args.steps, 5))
+        k = args.steps
         forms = {}
         res = {}
+        vf2, uf2, flow2_s = flow_state(pkg, torch, CFG2, local, flow_steps)
         for prec in ("float64", "float32"):
             s2, t2 = make_case(pkg, CFG2, prec, local)
             o2 = pkg.semidiscretize(s2, (0.0, 1.0))
-            v2, u2, ms2, l2, ph2 = run_form(pkg, torch, s2, o2, k, 1, CFG2["dt"], prec)
+            v2, u2 = vf2.clone(), uf2.clone()
+            w2 = timed_window(torch, s2, v2, u2, k, args.warmup, CFG2["dt"])
             n2 = s2.n_fluid + s2.n_wall
             forms[prec] = {
-                "value": n2 * k / (ms2 / 1e3), "ms_per_step": ms2 / k, "steps": k,
-                "n_fluid": s2.n_fluid, "n_wall": s2.n_wall,
-                "roofline": roofline_for(prec, s2.n_fluid, s2.n_wall, 5 * k, ph2[2], hbm,
-                                         peak_kind, "k_pair64" if prec == "float64"
-                                         else "k_pair32"),
+                "value": n2 * k / (w2["ms"] / 1e3), "ms_per_step": w2["ms"] / k, "steps": k,
+                "warmup": args.warmup, "n_fluid": s2.n_fluid, "n_wall": s2.n_wall,
+                "rebuilds_in_window": w2["rebuilds"],
+                "phase_ms_per_step": phases_per_step(w2["phases"], k),
+                "roofline": roofline_for(prec, s2.n_fluid, s2.n_wall, 5 * k, w2["phases"][2],
+                                         hbm, peak_kind,
+                                         "k_pair64" if prec == "float64" else "k_pair32"),
                 "step_hbm_frac": round(5 * (s2.n_fluid * BYTES_STAGE[prec][0] + s2.n_wall
-                                            * BYTES_STAGE[prec][1]) / (ms2 / k / 1e3) / 1e9
-                                       / hbm, 4),
+                                            * BYTES_STAGE[prec][1]) / (w2["ms"] / k / 1e3)
+                                       / 1e9 / hbm, 4),
             }
             res[prec] = (v2.view(-1, 4).cpu().numpy(), u2.view(-1, 3).cpu().numpy())
             s2.close()
+            del o2
+        del vf2, uf2
         (v64, u64), (v32, u32) = res["float64"], res["float32"]
 
         def rl2(a, b):
@@ -716,7 +829,8 @@ def main():
 
         forms["fp32_vs_fp64"] = {
             "speedup": forms["float32"]["value"] / forms["float64"]["value"],
-            "after_steps": k,
+            "after_steps": k + args.warmup,
+            "start_state": f"the same flowing state (t = {args.flow_time:g} s) for both forms",
             "rel_l2_rho": rl2(v32[:, 3], v64[:, 3]),
             "rel_l2_v": rl2(v32[:, :3], v64[:, :3]),
             "rel_l2_x": rl2(u32, u64)}
@@ -730,7 +844,9 @@ def main():
 
     if rank == 0 and not args.no_cpu:
         semi_c, tank_c = make_case(pkg, CFG1, "float64", local)
-        out["cpu_baseline"] = cpu_baseline(semi_c, tank_c, CFG1)
+        out["cpu_baseline"] = cpu_baseline(
+            semi_c, tank_c, CFG1, v_flow.view(-1, 4).cpu().numpy(),
+            u_flow.view(-1, 3).cpu().numpy(), f"the flowing state at t = {args.flow_time:g} s")
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:

@@ -235,16 +235,20 @@ tp_status tp_set_skin(tp_handle* h, double skin);
 tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth);
 
 /*
- * FP64 pair-pass mode.  TP_PAIR_GATHER (default): every fluid particle sums its own pair terms
- * in the reference's neighbour order (bitwise reproducible run to run).  TP_PAIR_SYMMETRIC:
- * every fluid-fluid pair is evaluated once and its two halves go to both particles (the second
- * by an FP64 atomic add), which cuts the FP64 arithmetic per pair by about 40 %; the terms are
- * the same, their summation order is not, so results differ from the gather mode in the last
- * bits and are not bitwise reproducible.  On GB300 the symmetric pass is not faster (lane
- * imbalance of the half lists and atomic traffic eat the saving); it is kept for GPUs with a
- * different FP64 / atomic balance.  The FP32 form always gathers.
+ * Pair-pass mode.  FP64 drop-in: TP_PAIR_GATHER (default): every fluid particle sums its own pair
+ * terms in the reference's neighbour order (bitwise reproducible run to run).
+ * TP_PAIR_SYMMETRIC: every fluid-fluid pair is evaluated once and its two halves go to both
+ * particles (the second by an FP64 atomic add), which cuts the FP64 arithmetic per pair by about
+ * 40 %; the terms are the same, their summation order is not, so results differ from the gather
+ * mode in the last bits and are not bitwise reproducible.  On GB300 the symmetric pass is not
+ * faster (lane imbalance of the half lists and atomic traffic eat the saving); it is kept for
+ * GPUs with a different FP64 / atomic balance.
+ * FP32 form: TP_PAIR_GATHER (default) walks per-particle neighbour lists built at a rebuild;
+ * TP_PAIR_TILED builds no fluid lists: each warp stages the candidate cell rows of its particles
+ * in shared memory and evaluates the pairs from there (the same neighbour set and pair terms; the
+ * summation order differs).  Other combinations return TP_ERR_ARGUMENT.
  */
-enum { TP_PAIR_GATHER = 0, TP_PAIR_SYMMETRIC = 1 };
+enum { TP_PAIR_GATHER = 0, TP_PAIR_SYMMETRIC = 1, TP_PAIR_TILED = 2 };
 tp_status tp_set_pair_mode(tp_handle* h, int32_t mode);
 
 /*
@@ -299,6 +303,12 @@ tp_status tp_sort_particles(tp_handle* h, double* v_ode, double* u_ode, int32_t 
 /* Number of CUDA kernels this handle has launched so far (diagnostics; memcpys not counted). */
 int64_t tp_kernel_launches(const tp_handle* h);
 
+/* Number of neighbour-search rebuilds (cell list + neighbour lists) the displacement gate of
+ * tp_kick / tp_integrate_ck2n54 has let through since tp_create (diagnostics, the counterpart of
+ * how often the reference's update_nhs! would have had to move a particle between cells).  HOST
+ * `count`; synchronises the handle's stream. */
+tp_status tp_rebuild_count(tp_handle* h, int64_t* count);
+
 /*
  * Cell sort without any device allocation.  This entry point has no counterpart in the
  * reference: it serves callers that must not allocate device memory -- a host that owns all
@@ -311,12 +321,13 @@ int64_t tp_kernel_launches(const tp_handle* h);
  * All scratch lives in one fixed device array owned by the library (about 10 MB, held by every
  * GPU that loads the library until the process exits): at most TP_NOALLOC_MAX_PARTICLES
  * particles and TP_NOALLOC_MAX_CELLS grid cells (padding included), larger requests return
- * TP_ERR_CAPACITY before any GPU work.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call before any
- * stream capture.  Calls share the scratch: the call clears what must start at zero, and
- * calls that overlap on the GPU race, so serialise them.  The call returns after the sort has
- * finished (it synchronises `stream`) and reports TP_ERR_OUT_OF_GRID / TP_ERR_NONFINITE
- * directly.  It calls no cudaMalloc, cudaFree or allocating library routine.
+ * TP_ERR_CAPACITY before any GPU work.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) in the context current at the call, so switching contexts or devices
+ * between calls is safe.  Calls share the scratch: the call clears what must start at zero, and
+ * calls that overlap on the GPU race, so serialise them.  The call is synchronous: it returns
+ * after the sort has finished (it synchronises `stream`) and reports TP_ERR_OUT_OF_GRID /
+ * TP_ERR_NONFINITE directly, so it must not be called while `stream` is being captured into a
+ * CUDA graph.  It calls no cudaMalloc, cudaFree or allocating library routine.
  */
 #define TP_NOALLOC_MAX_PARTICLES 262144
 #define TP_NOALLOC_MAX_CELLS 524288

@@ -39,11 +39,18 @@ static int run(int nd, int precision) {
     bad |= tp_set_launch(h, 256) != TP_OK;
     bad |= tp_set_launch(h, 100) != TP_ERR_ARGUMENT;
     bad |= tp_set_pair_mode(h, 5) != TP_ERR_ARGUMENT;
-    bad |= tp_set_pair_mode(h, precision == 0 ? TP_PAIR_GATHER : TP_PAIR_SYMMETRIC) != TP_OK;
+    bad |= tp_set_pair_mode(h, precision == 0 ? TP_PAIR_TILED : TP_PAIR_SYMMETRIC) !=
+           TP_ERR_ARGUMENT;
+    bad |= tp_set_pair_mode(h, precision == 0 ? TP_PAIR_SYMMETRIC : TP_PAIR_TILED) != TP_OK;
     bad |= tp_prepare_lists(h, u.data(), 1.5) != TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 2) != TP_OK;
     bad |= tp_integrate_ck2n54(h, v.data(), u.data(), 0.0, 1e-4, 1) != TP_OK;
     bad |= tp_kick(h, dv.data(), v.data(), u.data(), 0.0) != TP_OK;
+    {
+        int64_t rebuilds = -1;
+        bad |= tp_rebuild_count(h, &rebuilds) != TP_OK || rebuilds < 0;
+        bad |= tp_rebuild_count(h, nullptr) != TP_ERR_ARGUMENT;
+    }
     bad |= tp_fluid_pressure(h, pf.data()) != TP_OK;
     bad |= tp_wall_state(h, pw.data(), nullptr, nullptr) != TP_OK;
     bad |= tp_nhs_debug(h, u.data(), cell.data(), order.data(), nff.data(), nfw.data(),

@@ -14,8 +14,8 @@ from helpers import conservation_residuals, random_fluid_case
 
 pytestmark = pytest.mark.gpu
 
-FORMS = [("float64", 0), ("float64", 1), ("float32", 0)]
-FORM_IDS = ["fp64-gather", "fp64-symmetric", "fp32"]
+FORMS = [("float64", 0), ("float64", 1), ("float32", 0), ("float32", 2)]
+FORM_IDS = ["fp64-gather", "fp64-symmetric", "fp32", "fp32-tiled"]
 
 
 def _device_rates(pkg, cuda, nd, seed, viscosity, precision, pair_mode):

@@ -72,9 +72,10 @@ def test_integrate_fp64_3d_jittered(pkg, orc, cuda):
     semi.close()
 
 
-def test_integrate_fp32_form_2d(pkg, orc, cuda):
+@pytest.mark.parametrize("mode", [0, 2], ids=["lists", "tiled"])
+def test_integrate_fp32_form_2d(pkg, orc, cuda, mode):
     v, u, v_ref, u_ref, semi = _integrate(pkg, orc, cuda, 2, 0.02, (2.0, 1.0), (5.366, 4.0),
-                                          40, 1e-4, "float32")
+                                          40, 1e-4, "float32", pair_mode=mode)
     nd = 2
     vr, vg = v_ref.reshape(-1, nd + 1), v.reshape(-1, nd + 1)
     assert rel_l2(u, u_ref) <= 1e-8

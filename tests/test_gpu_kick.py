@@ -76,9 +76,10 @@ def test_kick_fp64_matches_oracle(pkg, orc, cuda, case, mode):
     assert np.all(out["p_w"][lone] == 0.0)
 
 
+@pytest.mark.parametrize("mode", [0, 2], ids=["lists", "tiled"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c['ndims']}d-j{c['jitter']}-v{c['vel']}")
-def test_kick_fp32_form_matches_oracle(pkg, orc, cuda, case):
-    out, dv_ref, ref, nd = _run(pkg, orc, cuda, case, "float32")
+def test_kick_fp32_form_matches_oracle(pkg, orc, cuda, case, mode):
+    out, dv_ref, ref, nd = _run(pkg, orc, cuda, case, "float32", pair_mode=mode)
     g = out["dv"].reshape(-1, nd + 1)
     r = dv_ref.reshape(-1, nd + 1)
     assert rel_l2(g[:, :nd], r[:, :nd]) <= 2e-5
@@ -90,11 +91,12 @@ def test_kick_fp32_form_matches_oracle(pkg, orc, cuda, case):
 FULL = dict(ndims=3, dx=0.008, fluid=(1.0, 0.5, 1.0), tank=(3.2, 1.0, 1.4), jitter=0.2, vel=0.5)
 
 
-@pytest.mark.parametrize("precision", ["float64", "float32"])
-def test_kick_full_3d_workload(pkg, orc, cuda, precision):
+@pytest.mark.parametrize("precision,mode", [("float64", 0), ("float32", 0), ("float32", 2)],
+                         ids=["fp64", "fp32-lists", "fp32-tiled"])
+def test_kick_full_3d_workload(pkg, orc, cuda, precision, mode):
     """One right-hand side of the full 3D benchmark workload (968 750 fluid + 876 666 wall
     particles, jittered, random velocities) against the oracle."""
-    out, dv_ref, ref, nd = _run(pkg, orc, cuda, FULL, precision)
+    out, dv_ref, ref, nd = _run(pkg, orc, cuda, FULL, precision, pair_mode=mode)
     g = out["dv"].reshape(-1, nd + 1)
     r = dv_ref.reshape(-1, nd + 1)
     if precision == "float64":
@@ -169,8 +171,37 @@ def test_kick_fp64_gather_mode_is_reproducible(pkg, orc, cuda):
 
 def test_pair_mode_argument_check(pkg, cuda):
     case = CASES[0]
-    semi, _ = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"])
-    pkg.semidiscretize(semi, (0.0, 1.0))
-    with pytest.raises(pkg.TpError):
-        semi._call("tp_set_pair_mode", 7)
+    for precision, bad in (("float64", (7, 2)), ("float32", (7, 1))):
+        semi, _ = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"],
+                                 precision=precision)
+        pkg.semidiscretize(semi, (0.0, 1.0))
+        for mode in bad:  # the tiled pass is an FP32 mode, the symmetric one an FP64 mode
+            with pytest.raises(pkg.TpError):
+                semi._call("tp_set_pair_mode", mode)
+        semi.close()
+
+
+def test_fp32_modes_switch_back_and_forth(pkg, orc, cuda):
+    """Switching an FP32 handle between the list and the tiled pass between kicks hands the
+    lists back: every kick matches the oracle."""
+    torch = cuda
+    case = CASES[1]
+    semi, tank = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"],
+                                jitter=case["jitter"], seed=5, precision="float32")
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    v, u = _state(tank, case)
+    model = oracle_model(orc, semi, tank)
+    dv_ref, st = model.kick(v, u)
+    assert st == 0
+    v_t = torch.as_tensor(v.ravel(), device=semi.device)
+    u_t = torch.as_tensor(u.ravel(), device=semi.device)
+    nd = case["ndims"]
+    r = dv_ref.reshape(-1, nd + 1)
+    for mode in (0, 2, 0, 2):
+        semi._call("tp_set_pair_mode", mode)
+        dv = torch.full_like(v_t, float("nan"))
+        pkg.kick(dv, v_t, u_t, ode.p, 0.0)
+        semi.sync()
+        g = dv.cpu().numpy().reshape(-1, nd + 1)
+        assert rel_l2(g[:, :nd], r[:, :nd]) <= 2e-5
     semi.close()

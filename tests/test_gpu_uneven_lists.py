@@ -60,8 +60,9 @@ def _uneven_case(pkg, nd, precision, seed):
 
 
 @pytest.mark.parametrize("nd", [2, 3])
-@pytest.mark.parametrize("precision,pair_mode", [("float64", 0), ("float64", 1), ("float32", 0)],
-                         ids=["fp64-gather", "fp64-symmetric", "fp32"])
+@pytest.mark.parametrize("precision,pair_mode", [("float64", 0), ("float64", 1), ("float32", 0),
+                                                 ("float32", 2)],
+                         ids=["fp64-gather", "fp64-symmetric", "fp32", "fp32-tiled"])
 def test_uneven_kick_matches_oracle(pkg, orc, cuda, nd, precision, pair_mode):
     torch = cuda
     semi, tank, v, u = _uneven_case(pkg, nd, precision, seed=21 + nd)

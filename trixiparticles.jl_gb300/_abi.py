@@ -102,6 +102,7 @@ PROTOTYPES = [
     ("tp_set_launch", c_int32, [c_void_p, c_int32]),
     ("tp_set_skin", c_int32, [c_void_p, c_double]),
     ("tp_kernel_launches", c_int64, [c_void_p]),
+    ("tp_rebuild_count", c_int32, [c_void_p, POINTER(c_int64)]),
     ("tp_cell_sort_noalloc", c_int32,
      [POINTER(TpConfig), c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     ("tp_adjoint_forward", c_int32,
@@ -130,6 +131,7 @@ PROTOTYPES = [
 
 TP_PAIR_GATHER = 0
 TP_PAIR_SYMMETRIC = 1
+TP_PAIR_TILED = 2
 TP_NOALLOC_MAX_PARTICLES = 262144
 TP_NOALLOC_MAX_CELLS = 524288
 

@@ -583,7 +583,9 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
     const float m = (float)(r - h->grid.cs + 1e-5 * h->grid.cs);
     auto run = [&](auto ndc) {
         constexpr int ND = decltype(ndc)::value;
-        if (nf > 0)
+        // the tiled FP32 pair pass enumerates its candidates itself: no fluid lists
+        const bool fluid_lists = h->pair_mode != TP_PAIR_TILED;
+        if (nf > 0 && fluid_lists)
             k_build_fluid_lists<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
                 h->grid, cs, m, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_skey,
                 h->w_start,
@@ -599,7 +601,7 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
     else
         run(std::integral_constant<int, 3>{});
     TP_LAUNCHED(h, "list build");
-    h->launches += (nf > 0) + (nw > 0);
+    h->launches += (nf > 0 && h->pair_mode != TP_PAIR_TILED) + (nw > 0);
     TP_DBG(h, "list build");
     return TP_OK;
 }
@@ -850,7 +852,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->c_ff, nf));
     A(dalloc(&h->c_fw, nf));
     A(dalloc(&h->c_wf, nw));
-    A(dalloc(&h->gate, 4));
+    A(dalloc(&h->gate, 5));
     A(dalloc(&h->d_max, 1));
     h->red_blocks = 256;
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
@@ -858,6 +860,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(cudaMallocHost((void**)&h->h_err, 4 * sizeof(int)));
     if (e == cudaSuccess) e = cudaMemset(h->f_count, 0, nc * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->gate, 0, 5 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(h->w_start, 0, (nc + 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->c_ff, 0, std::max<size_t>(nf, 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->c_fw, 0, std::max<size_t>(nf, 1) * sizeof(int));
@@ -1373,6 +1376,15 @@ int32_t tp_phase_times(tp_handle* h, double* ms, int32_t n) {
 
 int64_t tp_kernel_launches(const tp_handle* h) { return h ? (int64_t)h->launches : 0; }
 
+tp_status tp_rebuild_count(tp_handle* h, int64_t* count) {
+    if (!h || !count) return TP_ERR_ARGUMENT;
+    TP_CUDA(h, cudaMemcpyAsync(h->h_err + 2, h->gate + 4, sizeof(unsigned),
+                               cudaMemcpyDeviceToHost, h->stream));
+    TP_CUDA(h, cudaStreamSynchronize(h->stream));
+    *count = (int64_t)(unsigned)h->h_err[2];
+    return TP_OK;
+}
+
 tp_status tp_prepare_lists(tp_handle* h, const double* u_ode, double growth) {
     tp_status st = ready(h);
     if (st != TP_OK) return st;
@@ -1419,8 +1431,16 @@ tp_status tp_interpolate_points(tp_handle* h, const double* v_ode, const double*
 
 tp_status tp_set_pair_mode(tp_handle* h, int32_t mode) {
     if (!h) return TP_ERR_ARGUMENT;
-    if (mode != TP_PAIR_GATHER && mode != TP_PAIR_SYMMETRIC)
-        return fail(h, TP_ERR_ARGUMENT, "pair mode must be TP_PAIR_GATHER or TP_PAIR_SYMMETRIC");
+    if (h->cfg.precision == TP_PRECISION_FP32) {
+        if (mode != TP_PAIR_GATHER && mode != TP_PAIR_TILED)
+            return fail(h, TP_ERR_ARGUMENT,
+                        "the FP32 form's pair mode must be TP_PAIR_GATHER or TP_PAIR_TILED");
+    } else if (mode != TP_PAIR_GATHER && mode != TP_PAIR_SYMMETRIC) {
+        return fail(h, TP_ERR_ARGUMENT,
+                    "the FP64 form's pair mode must be TP_PAIR_GATHER or TP_PAIR_SYMMETRIC");
+    }
+    // the tiled pass builds no fluid lists: a change of mode hands the lists back
+    if (mode != h->pair_mode) h->lists_owner = 0;
     h->pair_mode = mode;
     return TP_OK;
 }

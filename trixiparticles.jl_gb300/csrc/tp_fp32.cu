@@ -199,110 +199,18 @@ struct Update32 {
     int first;
 };
 
-// Pair terms with the same identities as the FP64 kernels (grad W_ab = sg x_ab: one scalar for
-// pressure + viscosity, continuity through sg (v_ab . x_ab), diffusion as 2 (rho_a - rho_b) sg,
-// one reciprocal for the Monaghan mu / rho_mean), in FP32 on the cell-relative differences, with
-// Kahan-compensated per-particle sums.
-// Five 256-thread blocks per SM cap the kernel at 48 registers: the pass is bound by the L1 data
-// pipe serving its neighbour gathers and by their latency, and the extra resident warps (66 %
-// occupancy instead of 53 % at 56 registers) hide more of it (8 % faster at dx = 0.0064 in 3D).
-// The list is read four entries per 16-byte load (the chunked layout of tp_lists.cuh).
-// STD: the configuration of the dam-break setups (Monaghan viscosity with beta = 0, Molteni-
-// Colagrossi diffusion) with the model switches resolved at compile time; the pass is issue
-// bound, and the per-pair tests of the runtime switches are instructions of their own.
-template <int ND, bool INTEGRATE, bool STD>
-__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
-                                                const float4* __restrict__ ftest,
-                                                const float4* __restrict__ fvel,
-                                                const float* __restrict__ fpres,
-                                                const unsigned* __restrict__ ff,
-                                                const int* __restrict__ ffc,
-                                                const unsigned* __restrict__ fw,
-                                                const int* __restrict__ fwc,
-                                                const float4* __restrict__ wtest,
-                                                const float* __restrict__ wpres,
-                                                unsigned* __restrict__ gate, Update32 U) {
-    __shared__ float4 off[kOffsetCodes];
-    fill_offset_table(off, P.cs);
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nf) return;
-    const float4 ta = ftest[s];  // {offsets, rho - rho0}
-    const float4 va = fvel[s];   // {v, m / rho}
-    const float p_a = fpres[s];
-    const float drho_a = ta.w;
-    const float rho_a = P.rho0 + drho_a;
-    const float ia = __frcp_rn(rho_a);  // the pack's 1 / rho
-
-    Kahan a0, a1, a2, ar;
-    const int nff = ffc[s];
-    uint4 lq;  // the list quad holding entry k
-    for (int k = 0; k < nff; ++k) {
-        const unsigned e = list_next(ff, k, nf, s, lq);
-        const int b = (int)(e & kSlotMask);
-        const float4 cb = ftest[b];  // {offsets, rho_b - rho0}
-        float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, off, e, cb, pd0, pd1, pd2);
-        if (d2 > P.sr2 || d2 < P.az2) continue;
-        const float r = d2 * rsqrtf(d2);
-        const float4 vb = fvel[b];  // {v_b, m_b / rho_b}
-        const float p_b = fpres[b];
-        const float vol_b = vb.w;
-        const float t = fmaf(-r, P.half_hinv, 1.0f);
-        const float sg = P.sg_c * ((t * t) * t);
-        const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
-        const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
-        float vr = vd0 * pd0 + vd1 * pd1;
-        if (ND == 3) vr += vd2 * pd2;
-        float c = -(vol_b * ia) * (p_a + p_b);
-        if ((STD || P.visc) && vr < 0.0f) {
-            const float rho_b = P.rho0 + cb.w;
-            const float m_b = vol_b * rho_b;
-            const float den = d2 + P.visc_eps_h2;
-            const float rm = 0.5f * (rho_a + rho_b);
-            const float R = __fdividef(1.0f, den * rm);
-            if (STD || P.beta == 0.0f) {
-                c += (m_b * P.visc_k) * vr * R;
-            } else {
-                const float mu = (P.visc_h * vr) * (rm * R);
-                c += (m_b * mu) * (P.visc_ac + P.beta * mu) * (den * R);
-            }
-        }
-        c *= sg;
-        a0.add(c * pd0);
-        a1.add(c * pd1);
-        if (ND == 3) a2.add(c * pd2);
-        float er = (rho_a * vol_b) * (sg * vr);
-        if (STD || P.diff) er += (vol_b * (drho_a - cb.w)) * (sg * P.diff2);
-        ar.add(er);
-    }
-
-    Kahan w0, w1, w2, wr;
-    const int nfw = fwc[s];
-    for (int k = 0; k < nfw; ++k) {
-        const unsigned e = list_next(fw, k, nf, s, lq);
-        const int b = (int)(e & kSlotMask);
-        const float4 tb = wtest[b];  // {offsets, m_w / rho_w of the last Adami pass}
-        float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(ta, off, e, tb, pd0, pd1, pd2);
-        if (d2 > P.sr2 || d2 < P.az2) continue;
-        const float r = d2 * rsqrtf(d2);
-        const float vol_b = tb.w;
-        const float t = fmaf(-r, P.half_hinv, 1.0f);
-        const float sg = P.sg_c * ((t * t) * t);
-        const float c = (-(vol_b * ia) * (p_a + wpres[b])) * sg;
-        w0.add(c * pd0);
-        w1.add(c * pd1);
-        if (ND == 3) w2.add(c * pd2);
-        float vx = va.x * pd0 + va.y * pd1;
-        if (ND == 3) vx += va.z * pd2;
-        wr.add((rho_a * vol_b) * (sg * vx));
-    }
-
+// Stage update of one fluid slot from its compensated sums: the kick! path writes dv (gravity
+// added) in caller order; the integrator applies the fused CK2N54 register update (FP32
+// velocity/density, FP64 positions) and takes the next stage's displacement into the gate.
+template <int ND, bool INTEGRATE>
+__device__ __forceinline__ void pair32_finish(const Update32& U, int s, float4 va, float drho_a,
+                                              const Kahan& a0, const Kahan& a1, const Kahan& a2,
+                                              const Kahan& ar, const unsigned* gate) {
     double k[4];
-    k[0] = (a0.value() + w0.value()) + U.g[0];
-    k[1] = (a1.value() + w1.value()) + U.g[1];
-    k[2] = (ND == 3) ? (a2.value() + w2.value()) + U.g[2] : 0.0;
-    k[ND] = ar.value() + wr.value();
+    k[0] = a0.value() + U.g[0];
+    k[1] = a1.value() + U.g[1];
+    k[2] = (ND == 3) ? a2.value() + U.g[2] : 0.0;
+    k[ND] = ar.value();
 
     if (!INTEGRATE) {
         const int i = U.perm[s];
@@ -342,6 +250,387 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
     }
 }
 
+// Pair terms with the same identities as the FP64 kernels (grad W_ab = sg x_ab: one scalar for
+// pressure + viscosity, continuity through sg (v_ab . x_ab), diffusion as 2 (rho_a - rho_b) sg,
+// one reciprocal for the Monaghan mu / rho_mean), in FP32 on the cell-relative differences.
+// The list is walked one quad (four entries, one 16-byte load) at a time: the four candidates'
+// test records are requested together, the accepted pairs add into plain FP32 partial sums, and
+// each quad's partials enter the per-particle Kahan-compensated sums (blocked compensation: a
+// partial holds at most four terms, so its rounding is that of a four-term sum, and the running
+// sum over the ~50 quads of a 3D particle stays compensated).
+// Five 256-thread blocks per SM cap the kernel at 48 registers: the pass is bound by the L1 data
+// pipe serving its neighbour gathers and by their latency, and the extra resident warps hide
+// more of it.
+// STD: the configuration of the dam-break setups (Monaghan viscosity with beta = 0, Molteni-
+// Colagrossi diffusion) with the model switches resolved at compile time, and the viscosity
+// switch v_ab . x_ab < 0 taken as min(v_ab . x_ab, 0) instead of a branch.
+struct FluidSums {
+    float x = 0.0f, y = 0.0f, z = 0.0f, r = 0.0f;
+};
+
+// The terms of one accepted fluid-fluid pair (pd = x_a - x_b, d2 = |pd|^2) into the partials.
+template <int ND, bool STD>
+__device__ __forceinline__ void ff_terms32(const Phys32& P, float4 va, float p_a, float rho_a,
+                                           float ia, float drho_a, float pd0, float pd1,
+                                           float pd2, float d2, float4 cb, float4 vb, float p_b,
+                                           FluidSums& q) {
+    const float r = d2 * rsqrtf(d2);
+    const float vol_b = vb.w;  // m_b / rho_b
+    const float t = fmaf(-r, P.half_hinv, 1.0f);
+    const float sg = P.sg_c * ((t * t) * t);
+    const float vd0 = va.x - vb.x, vd1 = va.y - vb.y;
+    const float vd2 = (ND == 3) ? va.z - vb.z : 0.0f;
+    float vr = vd0 * pd0 + vd1 * pd1;
+    if (ND == 3) vr += vd2 * pd2;
+    const float rho_b = P.rho0 + cb.w;
+    float c = -(vol_b * ia) * (p_a + p_b);
+    if (STD) {
+        const float m_b = vol_b * rho_b;
+        const float R = __fdividef(1.0f, (d2 + P.visc_eps_h2) * (0.5f * (rho_a + rho_b)));
+        c = fmaf((m_b * P.visc_k) * fminf(vr, 0.0f), R, c);
+    } else if (P.visc && vr < 0.0f) {
+        const float m_b = vol_b * rho_b;
+        const float den = d2 + P.visc_eps_h2;
+        const float rm = 0.5f * (rho_a + rho_b);
+        const float R = __fdividef(1.0f, den * rm);
+        if (P.beta == 0.0f) {
+            c += (m_b * P.visc_k) * vr * R;
+        } else {
+            const float mu = (P.visc_h * vr) * (rm * R);
+            c += (m_b * mu) * (P.visc_ac + P.beta * mu) * (den * R);
+        }
+    }
+    c *= sg;
+    q.x = fmaf(c, pd0, q.x);
+    q.y = fmaf(c, pd1, q.y);
+    if (ND == 3) q.z = fmaf(c, pd2, q.z);
+    // continuity rho_a m_b / rho_b v_ab . grad W plus the diffusion term, one factor sg m_b/rho_b
+    const float dterm = (STD || P.diff) ? P.diff2 * (drho_a - cb.w) : 0.0f;
+    q.r = fmaf((sg * vol_b), fmaf(rho_a, vr, dterm), q.r);
+}
+
+// The terms of one accepted fluid-wall pair (vol_b = m_w / rho_w of the last Adami pass).
+template <int ND>
+__device__ __forceinline__ void fw_terms32(const Phys32& P, float4 va, float p_a, float rho_a,
+                                           float ia, float pd0, float pd1, float pd2, float d2,
+                                           float vol_b, float p_w, FluidSums& q) {
+    const float r = d2 * rsqrtf(d2);
+    const float t = fmaf(-r, P.half_hinv, 1.0f);
+    const float sg = P.sg_c * ((t * t) * t);
+    const float c = (-(vol_b * ia) * (p_a + p_w)) * sg;
+    q.x = fmaf(c, pd0, q.x);
+    q.y = fmaf(c, pd1, q.y);
+    if (ND == 3) q.z = fmaf(c, pd2, q.z);
+    float vx = va.x * pd0 + va.y * pd1;
+    if (ND == 3) vx += va.z * pd2;
+    q.r = fmaf((rho_a * vol_b) * sg, vx, q.r);
+}
+
+// List entry e with the candidate's test record cb: the exact test, then the pair terms.
+template <int ND, bool STD>
+__device__ __forceinline__ void ff_pair32(const Phys32& P, const float4* off, float4 ta,
+                                          float4 va, float p_a, float rho_a, float ia,
+                                          float drho_a, unsigned e, float4 cb,
+                                          const float4* __restrict__ fvel,
+                                          const float* __restrict__ fpres, FluidSums& q) {
+    float pd0, pd1, pd2;
+    const float d2 = pair_diff<ND>(ta, off, e, cb, pd0, pd1, pd2);
+    if (d2 > P.sr2 || d2 < P.az2) return;
+    const int b = (int)(e & kSlotMask);
+    ff_terms32<ND, STD>(P, va, p_a, rho_a, ia, drho_a, pd0, pd1, pd2, d2, cb, fvel[b], fpres[b],
+                        q);
+}
+
+template <int ND>
+__device__ __forceinline__ void fw_pair32(const Phys32& P, const float4* off, float4 ta,
+                                          float4 va, float p_a, float rho_a, float ia,
+                                          unsigned e, float4 tb,
+                                          const float* __restrict__ wpres, FluidSums& q) {
+    float pd0, pd1, pd2;
+    const float d2 = pair_diff<ND>(ta, off, e, tb, pd0, pd1, pd2);
+    if (d2 > P.sr2 || d2 < P.az2) return;
+    fw_terms32<ND>(P, va, p_a, rho_a, ia, pd0, pd1, pd2, d2, tb.w, wpres[e & kSlotMask], q);
+}
+
+template <int ND, bool INTEGRATE, bool STD>
+__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
+                                                const float4* __restrict__ ftest,
+                                                const float4* __restrict__ fvel,
+                                                const float* __restrict__ fpres,
+                                                const unsigned* __restrict__ ff,
+                                                const int* __restrict__ ffc,
+                                                const unsigned* __restrict__ fw,
+                                                const int* __restrict__ fwc,
+                                                const float4* __restrict__ wtest,
+                                                const float* __restrict__ wpres,
+                                                unsigned* __restrict__ gate, Update32 U) {
+    __shared__ float4 off[kOffsetCodes];
+    fill_offset_table(off, P.cs);
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const float4 ta = ftest[s];  // {offsets, rho - rho0}
+    const float4 va = fvel[s];   // {v, m / rho}
+    const float p_a = fpres[s];
+    const float drho_a = ta.w;
+    const float rho_a = P.rho0 + drho_a;
+    const float ia = __frcp_rn(rho_a);  // the pack's 1 / rho
+
+    Kahan a0, a1, a2, ar;
+    auto settle = [&](const FluidSums& q) {
+        a0.add(q.x);
+        a1.add(q.y);
+        if (ND == 3) a2.add(q.z);
+        ar.add(q.r);
+    };
+    const int nff = ffc[s];
+    for (int k = 0; k < (nff & ~3); k += 4) {
+        const uint4 l = list_quad(ff, k, nf, s);
+        FluidSums q;
+        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.x, ftest[l.x & kSlotMask],
+                           fvel, fpres, q);
+        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.y, ftest[l.y & kSlotMask],
+                           fvel, fpres, q);
+        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.z, ftest[l.z & kSlotMask],
+                           fvel, fpres, q);
+        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.w, ftest[l.w & kSlotMask],
+                           fvel, fpres, q);
+        settle(q);
+    }
+    if (nff & 3) {  // the open quad: entries beyond the count are not part of the list
+        const int k = nff & ~3, m = nff & 3;
+        const uint4 l = list_quad(ff, k, nf, s);
+        FluidSums q;
+        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.x, ftest[l.x & kSlotMask],
+                           fvel, fpres, q);
+        if (m > 1)
+            ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.y,
+                               ftest[l.y & kSlotMask], fvel, fpres, q);
+        if (m > 2)
+            ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.z,
+                               ftest[l.z & kSlotMask], fvel, fpres, q);
+        settle(q);
+    }
+    // the wall neighbours continue the same compensated sums
+    const int nfw = fwc[s];
+    for (int k = 0; k < (nfw & ~3); k += 4) {
+        const uint4 l = list_quad(fw, k, nf, s);
+        FluidSums q;
+        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.x, wtest[l.x & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.y, wtest[l.y & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.z, wtest[l.z & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.w, wtest[l.w & kSlotMask], wpres, q);
+        settle(q);
+    }
+    if (nfw & 3) {
+        const int k = nfw & ~3, m = nfw & 3;
+        const uint4 l = list_quad(fw, k, nf, s);
+        FluidSums q;
+        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.x, wtest[l.x & kSlotMask], wpres, q);
+        if (m > 1)
+            fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.y, wtest[l.y & kSlotMask], wpres, q);
+        if (m > 2)
+            fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.z, wtest[l.z & kSlotMask], wpres, q);
+        settle(q);
+    }
+
+    pair32_finish<ND, INTEGRATE>(U, s, va, drho_a, a0, a1, a2, ar, gate);
+}
+
+// ------------------------------------------------------------------------------------------
+// Tiled pair pass (TP_PAIR_TILED): no neighbour lists.  Every warp enumerates the candidate
+// cells of its 32 fluid slots directly from the cell list -- lanes grouped by their (cy, cz)
+// row, the group's lanes bounded by a box, each neighbouring row's contiguous slot range
+// streamed 32 records at a time (the enumeration of the list builder, tp_lists.cuh) -- and
+// stages the records that pass the box test in shared memory with coalesced 16-byte loads:
+// test record (x taken relative to the group's first cell), velocity record and pressure.  Each
+// lane then tests every staged record against its own position (a broadcast shared load per
+// record) into a 32-bit accept mask, and evaluates its accepted pairs from shared memory, one
+// mask bit at a time, with the same pair terms as the list pass.  A quad of staged records
+// feeds one blocked-Kahan partial as in the list pass (here: one partial per staged chunk).
+// The reach (one or two cells towards a face, radius 2h (1 + skin) from the reference cell)
+// covers every particle within 2h until the displacement gate reopens, exactly as for the
+// lists; pairs are decided with |x_a - x_b|^2 <= (2h)^2 at use time.
+// ------------------------------------------------------------------------------------------
+struct TileStage {
+    float4 t[32];  // {X relative to the group's first cell, oy, oz, rho - rho0 | m/rho (wall)}
+    float4 v[32];  // fluid: {v, m / rho}
+    float p[32];   // pressure
+};
+
+template <int ND, bool WALL, bool STD>
+__device__ __forceinline__ void tile_sources(const Phys32& P, const GridDesc& g, float cs,
+                                             float m, float r2list, bool active, const int c[3],
+                                             float4 oa, float4 va, float p_a, float rho_a,
+                                             float ia, float drho_a,
+                                             const int* __restrict__ start,
+                                             const int* __restrict__ skey,
+                                             const float4* __restrict__ test,
+                                             const float4* __restrict__ vel,
+                                             const float* __restrict__ pres, TileStage& st,
+                                             Kahan& a0, Kahan& a1, Kahan& a2, Kahan& ar) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int xl = reach_lo(oa.x, m), xh = reach_hi(oa.x, cs, m);
+    const int yl = reach_lo(oa.y, m), yh = reach_hi(oa.y, cs, m);
+    const int zl = (ND == 3) ? reach_lo(oa.z, m) : 0, zh = (ND == 3) ? reach_hi(oa.z, cs, m) : 0;
+    const int yz = active ? (c[1] + g.n[1] * c[2]) : -1;
+    const float margin = 1e-3f * cs;
+    const float rbox = sqrtf(r2list) * 1.0001f + margin;
+    const float r2box = rbox * rbox;
+    unsigned todo = __ballot_sync(FULL, active);
+    while (todo) {
+        const int leader = __ffs(todo) - 1;
+        const int yz0 = __shfl_sync(FULL, yz, leader);
+        const int cx0 = __shfl_sync(FULL, c[0], leader);
+        const bool ing = active && (yz == yz0);
+        const unsigned grp = __ballot_sync(FULL, ing);
+        todo &= ~grp;
+        const int cy = yz0 % g.n[1], cz = yz0 / g.n[1];
+        const float xlane = fmaf((float)(c[0] - cx0), cs, oa.x);
+        const float ax = fmaxf(xlane, 0.0f);
+        const float ay = fmaxf(oa.y, 0.0f), az = fmaxf(oa.z, 0.0f);
+        auto gmin = [&](float x) {
+            return __int_as_float(__reduce_min_sync(FULL, ing ? __float_as_int(x) : INT_MAX));
+        };
+        auto gmax = [&](float x) {
+            return __int_as_float(__reduce_max_sync(FULL, ing ? __float_as_int(x) : 0));
+        };
+        const float bx0 = gmin(ax) - margin, bx1 = gmax(ax) + margin;
+        const float by0 = gmin(ay) - margin, by1 = gmax(ay) + margin;
+        float bz0 = 0.0f, bz1 = 0.0f;
+        if (ND == 3) {
+            bz0 = gmin(az) - margin;
+            bz1 = gmax(az) + margin;
+        }
+        auto slab = [&](int d, float b0, float b1) {
+            return fmaxf(fmaxf((float)d * cs - b1, b0 - (float)(d + 1) * cs), 0.0f);
+        };
+        const int zr = (ND == 3) ? 2 : 0;
+        for (int dz = -zr; dz <= zr; ++dz) {
+            if (cz + dz < 0 || cz + dz >= g.n[2]) continue;
+            const float ez = (ND == 3) ? slab(dz, bz0, bz1) : 0.0f;
+            for (int dy = -2; dy <= 2; ++dy) {
+                if (cy + dy < 0 || cy + dy >= g.n[1]) continue;
+                const float ey = slab(dy, by0, by1);
+                if (fmaf(ey, ey, ez * ez) > r2box) continue;
+                const bool need = ing && dy >= -yl && dy <= yh && dz >= -zl && dz <= zh;
+                if (!__ballot_sync(FULL, need)) continue;
+                const int xa = need ? max(c[0] - xl, 0) : INT_MAX;
+                const int xb = need ? min(c[0] + xh, g.n[0] - 1) : INT_MIN;
+                const int gxa = __reduce_min_sync(FULL, xa);
+                const int gxb = __reduce_max_sync(FULL, xb);
+                const int rb = g.n[0] * ((cy + dy) + g.n[1] * (cz + dz));
+                const int lo = start[rb + gxa];
+                const int hi = start[rb + gxb + 1];
+                if (lo >= hi) continue;
+                const float sy = fmaf(-(float)dy, cs, oa.y);
+                const float sz = fmaf(-(float)dz, cs, oa.z);
+                const float ryz = fmaf(ey, ey, ez * ez);
+                for (int base = lo; base < hi; base += 32) {
+                    const int j = base + lane;
+                    bool rel = false;
+                    float4 cb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (j < hi) {
+                        cb = test[j];
+                        const int cxb = skey[j] - rb;
+                        const float X = fmaf((float)(cxb - cx0), cs, cb.x);
+                        cb.x = X;
+                        const float Y = fmaf((float)dy, cs, cb.y);
+                        const float ex = fmaxf(fmaxf(bx0 - X, X - bx1), 0.0f);
+                        const float eyc = fmaxf(fmaxf(by0 - Y, Y - by1), 0.0f);
+                        float d2b = fmaf(ex, ex, eyc * eyc);
+                        if (ND == 3) {
+                            const float Z = fmaf((float)dz, cs, cb.z);
+                            const float ezc = fmaxf(fmaxf(bz0 - Z, Z - bz1), 0.0f);
+                            d2b = fmaf(ezc, ezc, d2b);
+                        }
+                        rel = fmaxf(d2b, ryz) <= r2box;
+                    }
+                    const unsigned hits = __ballot_sync(FULL, rel);
+                    if (rel) {
+                        const int pos = __popc(hits & ((1u << lane) - 1u));
+                        st.t[pos] = cb;
+                        if (!WALL) st.v[pos] = vel[j];
+                        st.p[pos] = pres[j];
+                    }
+                    __syncwarp();
+                    const int nrel = __popc(hits);
+                    // test phase: every lane against every staged record (broadcast loads)
+                    unsigned acc = 0u;
+                    if (ing) {
+                        for (int i = 0; i < nrel; ++i) {
+                            const float4 cbi = st.t[i];
+                            const float pdx = xlane - cbi.x;
+                            const float pdy = sy - cbi.y;
+                            float d2 = fmaf(pdy, pdy, pdx * pdx);
+                            if (ND == 3) {
+                                const float pdz = sz - cbi.z;
+                                d2 = fmaf(pdz, pdz, d2);
+                            }
+                            acc |= (d2 <= P.sr2 && d2 >= P.az2) ? (1u << i) : 0u;
+                        }
+                    }
+                    // pair phase: the lane's accepted records, one mask bit at a time
+                    if (acc) {
+                        FluidSums q;
+                        do {
+                            const int i = __ffs(acc) - 1;
+                            acc &= acc - 1u;
+                            const float4 cbi = st.t[i];
+                            const float pd0 = xlane - cbi.x, pd1 = sy - cbi.y;
+                            const float pd2 = (ND == 3) ? sz - cbi.z : 0.0f;
+                            float d2 = fmaf(pd1, pd1, pd0 * pd0);
+                            if (ND == 3) d2 = fmaf(pd2, pd2, d2);
+                            if (WALL)
+                                fw_terms32<ND>(P, va, p_a, rho_a, ia, pd0, pd1, pd2, d2, cbi.w,
+                                               st.p[i], q);
+                            else
+                                ff_terms32<ND, STD>(P, va, p_a, rho_a, ia, drho_a, pd0, pd1, pd2,
+                                                    d2, cbi, st.v[i], st.p[i], q);
+                        } while (acc);
+                        a0.add(q.x);
+                        a1.add(q.y);
+                        if (ND == 3) a2.add(q.z);
+                        ar.add(q.r);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+    }
+}
+
+template <int ND, bool INTEGRATE, bool STD>
+__global__ void __launch_bounds__(256, 3) k_pair32_tiled(
+    Phys32 P, GridDesc g, float m, float r2list, int nf, const int* __restrict__ fstart,
+    const int* __restrict__ fskey, const float4* __restrict__ ftest,
+    const float4* __restrict__ fvel, const float* __restrict__ fpres,
+    const int* __restrict__ wstart, const int* __restrict__ wskey,
+    const float4* __restrict__ wtest, const float* __restrict__ wpres, int nw,
+    unsigned* __restrict__ gate, Update32 U) {
+    __shared__ TileStage stage_all[8];
+    TileStage& st = stage_all[threadIdx.x >> 5];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = s < nf;
+    const int si = active ? s : 0;
+    const float4 ta = ftest[si];
+    const float4 va = fvel[si];
+    const float p_a = fpres[si];
+    const float drho_a = ta.w;
+    const float rho_a = P.rho0 + drho_a;
+    const float ia = __frcp_rn(rho_a);
+    int c[3];
+    key_to_coords(fskey[si], g, c);
+    Kahan a0, a1, a2, ar;
+    tile_sources<ND, false, STD>(P, g, P.cs, m, r2list, active, c, ta, va, p_a, rho_a, ia,
+                                 drho_a, fstart, fskey, ftest, fvel, fpres, st, a0, a1, a2, ar);
+    if (nw > 0)
+        tile_sources<ND, true, STD>(P, g, P.cs, m, r2list, active, c, ta, va, p_a, rho_a, ia,
+                                    drho_a, wstart, wskey, wtest, nullptr, wpres, st, a0, a1, a2,
+                                    ar);
+    if (!active) return;
+    pair32_finish<ND, INTEGRATE>(U, s, va, drho_a, a0, a1, a2, ar, gate);
+}
 // ------------------------------------------------------------------------------------------
 // Host launchers
 // ------------------------------------------------------------------------------------------
@@ -421,6 +710,18 @@ static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
     const Phys32& P = h->phys32;
     const bool std_cfg = P.visc && P.beta == 0.0f && P.diff;
     auto run = [&](auto stdc) {
+        if (h->pair_mode == TP_PAIR_TILED) {
+            // candidate enumeration of the list builder at radius 2h (1 + skin)
+            const double r = 2.0 * h->cfg.smoothing_length * (1.0 + h->skin);
+            const float r2list = (float)(r * r * (1.0 + 1e-5));
+            const float m = (float)(r - h->grid.cs + 1e-5 * h->grid.cs);
+            k_pair32_tiled<ND, INTEG, decltype(stdc)::value><<<nblk(nf, 256), 256, 0,
+                                                              h->stream>>>(
+                P, h->grid, m, r2list, nf, h->f_start, h->f_skey, h->f_test,
+                (const float4*)h->f_vel, (const float*)h->f_aux, h->w_start, h->w_skey,
+                h->w_test, h->w_p32, (int)h->cfg.n_wall, gate, U);
+            return;
+        }
         k_pair32<ND, INTEG, decltype(stdc)::value><<<nblk(nf, h->pair_block), h->pair_block, 0,
                                                      h->stream>>>(
             P, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux, h->l_ff, h->c_ff,

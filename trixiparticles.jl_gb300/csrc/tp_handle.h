@@ -97,12 +97,13 @@ struct tp_handle {
     int ecap_ff = 0, ecap_fw = 0, ecap_wf = 0;
     // FP64 form, symmetric pair mode: per-slot accumulator {dv (3), drho} of the pair pass
     double* acc = nullptr;
-    int pair_mode = 0;  // TP_PAIR_GATHER (default) or TP_PAIR_SYMMETRIC
+    int pair_mode = 0;  // TP_PAIR_GATHER (default), TP_PAIR_SYMMETRIC (FP64), TP_PAIR_TILED (FP32)
     // list radius 2h (1 + skin); rebuild after skin * h displacement.  0.05 measured best on
     // GB300 in both forms, at rest and in a 3 m/s flow (shorter lists outweigh the rebuilds).
     double skin = 0.05;
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
-    unsigned* gate = nullptr;   // {force, max squared displacement bits, squared threshold bits}
+    unsigned* gate = nullptr;   // {force, max squared displacement bits, squared threshold bits,
+                                //  next stage's displacement bits, rebuilds let through}
     int* d_max = nullptr;       // scratch for the largest cell occupancy
     int maxcell_w = 0;          // largest wall cell occupancy (walls are static)
     bool lists_fixed = false;   // capacity fixed by tp_prepare_lists (no sizing sync per call)

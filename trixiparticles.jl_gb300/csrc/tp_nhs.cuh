@@ -21,7 +21,8 @@
 // the squared half skin (skin * h)^2, lowered by 1e-5 relative so that FP32 rounding of the
 // displacement never lets a particle past the margin unseen (float bits).  A null gate means
 // "always rebuild".  When the gate is closed the kernels return at once and the rank pass packs
-// every slot in place.
+// every slot in place.  gate[4] counts the rebuilds the gate has let through since the handle was
+// created (the key pass bumps it once per open gate).
 #pragma once
 
 #include "tp_internal.cuh"
@@ -44,6 +45,8 @@ __global__ void __launch_bounds__(256) k_cell_keys(const double* __restrict__ u,
                                                    int* __restrict__ count, int* __restrict__ err,
                                                    const unsigned* __restrict__ gate = nullptr) {
     if (!gate_open(gate)) return;
+    // gate[4] counts the rebuilds the gate let through (diagnostics, tp_rebuild_count)
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(const_cast<unsigned*>(gate) + 4, 1u);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
