@@ -10,7 +10,8 @@ library's own fused integrator (tp_integrate_ck2n54) in FP64:
   * FP32 adjoint, dx = 0.01 (20 000 fluid particles), 500 steps, checkpoints every 25, FD step
     h = 1e-4: relative error <= 1e-3;
   * FP64 adjoint on the 2000-particle variant (dx = 0.0316) against central differences through
-    the FP64 CPU oracle: relative error <= 1e-5;
+    the FP64 CPU oracle: relative error <= 1e-5, and against forward-mode derivatives through
+    the oracle (dual numbers, the counterpart of ForwardDiff): relative error <= 1e-8;
   * gradients do not depend on the checkpoint interval (FP64, relative 1e-10).
 The adjoint's forward agrees with the fused integrator (FP64: v within 1e-9, u within 1e-12
 relative L2; FP32: the precision-form tolerances).
@@ -201,3 +202,35 @@ def test_adjoint_against_oracle_finite_differences(pkg, orc, cuda):
     fd["v0"] = (oracle_loss(vp, **base) - oracle_loss(vm, **base)) / (2 * h)
     assert abs(loss - oracle_loss(v0, **base)) <= 1e-12
     _compare(grad, fd, 1e-5)
+
+
+def test_adjoint_against_oracle_forward_mode(pkg, orc, cuda):
+    """2000-particle variant (dx = 0.0316): FP64 adjoint vs forward-mode derivatives through the
+    FP64 CPU oracle (dual numbers carried through the oracle's right-hand side and CK2N54 steps,
+    the counterpart of a ForwardDiff gradient through the reference's CPU path).  Both are exact
+    derivatives of the same discrete map up to rounding: relative error <= 1e-8 for alpha, delta,
+    |g| and the v0 direction."""
+    torch = cuda
+    dx, n, k = 0.0316, 60, 20
+    dt = 5e-3 * dx
+    tank, eos = _tank(pkg, dx)
+    v0, u0 = _initial(tank)
+    idx = pkg.adjoint.top_layer_indices(tank)
+    w = np.random.default_rng(11).normal(size=(tank.fluid.n_particles, 2))
+    loss, vb, ub, pbar, _, _ = _adjoint(pkg, torch, tank, eos, dx, "float64", v0, u0, dt, n, k,
+                                        idx)
+    grad = dict(pbar, v0=float((vb[:, :2] * w).sum()))
+    semi = _semi(pkg, tank, eos, dx, "float64")
+    vdir = np.zeros_like(v0)
+    vdir[:, :2] = w
+    _, uu, dv, du, st = orc.integrate_jvp(semi.config, tank.boundary.coordinates,
+                                          tank.boundary.mass, tank.fluid.mass, v0, u0, dt, n,
+                                          v_dir=vdir)
+    assert st == 0
+    assert abs(loss - float(uu.reshape(-1, 2)[idx, 1].mean())) <= 1e-12
+    fwd = {name: float(du[kk].reshape(-1, 2)[idx, 1].mean())
+           for kk, name in enumerate(("alpha", "delta", "gravity", "v0"))}
+    print(f"\nADJOINT vs forward mode: " + ", ".join(
+        f"{k_}: {grad[k_]:.9e} / {fwd[k_]:.9e} (rel {abs(grad[k_] - fwd[k_]) / abs(fwd[k_]):.2e})"
+        for k_ in fwd))
+    _compare(grad, fwd, 1e-8)

@@ -871,6 +871,11 @@ struct AdjointState {
     void* lam = nullptr;  // all adjoint arrays in one allocation
     double* theta = nullptr;
     double* h_theta = nullptr;  // pinned
+    // per-segment storage of the backward pass (null when it would not fit): the neighbour lists
+    // of every step and the pressure / wall state of every stage of the segment being reversed,
+    // kept from its recomputation so that the reverse sweep does not rebuild them
+    void* seg = nullptr;
+    size_t seg_bytes = 0;
     // recorded forward
     bool recorded = false;
     double dt = 0.0;
@@ -946,6 +951,75 @@ AdjPhys<T> make_phys(const tp_handle* h) {
     return P;
 }
 
+// The neighbour lists of one step and the pressure / wall state of one stage.
+struct ListSet {
+    int *ff, *fw, *wf, *ffc, *fwc, *wfc;
+};
+template <typename T>
+struct WallSet {
+    T *pf, *wp, *wr, *wnum, *wvol;
+};
+
+ListSet lists_of(const AdjointState& A) {
+    return ListSet{A.ff, A.fw, A.wf, A.ffc, A.fwc, A.wfc};
+}
+template <typename T>
+WallSet<T> walls_of(const AdjointState& A) {
+    return WallSet<T>{(T*)A.pf, (T*)A.wp, (T*)A.wr, (T*)A.wnum, (T*)A.wvol};
+}
+
+// Segment storage layout: `steps` list sets, then 5 * steps wall sets.
+size_t list_set_ints(const AdjointState& A) {
+    const size_t n = (size_t)A.nf, nw = (size_t)std::max(A.nw, 1);
+    return (size_t)A.cap_ff * n + (size_t)A.cap_fw * n + (size_t)A.cap_wf * nw + 2 * n + nw;
+}
+template <typename T>
+size_t wall_set_elems(const AdjointState& A) {
+    return (size_t)A.nf + 4 * (size_t)std::max(A.nw, 1);
+}
+template <typename T>
+size_t seg_bytes_for(const AdjointState& A, long long steps) {
+    const size_t lists = ((list_set_ints(A) * 4 + 255) / 256) * 256;
+    const size_t walls = ((wall_set_elems<T>(A) * sizeof(T) + 255) / 256) * 256;
+    return (size_t)steps * (lists + 5 * walls);
+}
+ListSet seg_lists(const AdjointState& A, long long j) {
+    const size_t n = (size_t)A.nf, nw = (size_t)std::max(A.nw, 1);
+    const size_t lists = ((list_set_ints(A) * 4 + 255) / 256) * 256;
+    int* p = (int*)((char*)A.seg + (size_t)j * lists);
+    ListSet L;
+    L.ff = p;
+    p += (size_t)A.cap_ff * n;
+    L.fw = p;
+    p += (size_t)A.cap_fw * n;
+    L.wf = p;
+    p += (size_t)A.cap_wf * nw;
+    L.ffc = p;
+    p += n;
+    L.fwc = p;
+    p += n;
+    L.wfc = p;
+    return L;
+}
+template <typename T>
+WallSet<T> seg_walls(const AdjointState& A, long long steps, long long k) {
+    const size_t nw = (size_t)std::max(A.nw, 1);
+    const size_t lists = ((list_set_ints(A) * 4 + 255) / 256) * 256;
+    const size_t walls = ((wall_set_elems<T>(A) * sizeof(T) + 255) / 256) * 256;
+    T* p = (T*)((char*)A.seg + (size_t)steps * lists + (size_t)k * walls);
+    WallSet<T> W;
+    W.pf = p;
+    p += A.nf;
+    W.wp = p;
+    p += nw;
+    W.wr = p;
+    p += nw;
+    W.wnum = p;
+    p += nw;
+    W.wvol = p;
+    return W;
+}
+
 template <typename T>
 AdjLam<T> lam_of(const AdjointState& A) {
     const size_t n = (size_t)A.nf, nd = (size_t)A.nd, nw = (size_t)std::max(A.nw, 1);
@@ -984,7 +1058,7 @@ size_t lam_elems(const AdjointState& A) {
 void free_all(AdjointState* A) {
     void* ptrs[] = {A->ff, A->fw, A->wf, A->ffc, A->fwc, A->wfc, A->xb, A->mf, A->pf, A->wp,
                     A->wr, A->wnum, A->wvol, A->tx, A->tv, A->tr, A->pingpong, A->ckpt, A->tape,
-                    A->lam, A->theta};
+                    A->lam, A->theta, A->seg};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (A->h_theta) cudaFreeHost(A->h_theta);
@@ -1065,7 +1139,7 @@ tp_status ensure_adjoint(tp_handle* h, const double* u) {
 }
 
 template <int ND>
-tp_status build_lists_at(tp_handle* h, const double* x) {
+tp_status build_lists_at(tp_handle* h, const double* x, const ListSet& L) {
     AdjointState& A = *h->adj;
     tp_status st = sort_fluid_cells(h, x, nullptr);
     if (st != TP_OK) return st;
@@ -1075,26 +1149,27 @@ tp_status build_lists_at(tp_handle* h, const double* x) {
     if (A.nf > 0)
         k_adj_fluid_lists<ND><<<nb(A.nf, 128), 128, 0, h->stream>>>(
             h->grid, rl2, m, A.nf, x, h->f_key, h->f_start, h->f_perm,
-            (const double4_32a*)h->w_pos, h->w_start, A.ff, A.ffc, A.cap_ff, A.fw, A.fwc, A.cap_fw,
+            (const double4_32a*)h->w_pos, h->w_start, L.ff, L.ffc, A.cap_ff, L.fw, L.fwc, A.cap_fw,
             A.xb, h->d_err);
     if (A.nw > 0)
         k_adj_wall_lists<ND><<<nb(A.nw, 128), 128, 0, h->stream>>>(
             h->grid, rl2, m, A.nw, (const double4_32a*)h->w_pos, h->w_skey, x, h->f_start,
-            h->f_perm, A.wf, A.wfc, A.cap_wf, h->d_err);
+            h->f_perm, L.wf, L.wfc, A.cap_wf, h->d_err);
     ADJ_LAUNCHED(h, "adjoint lists");
     A.kernels += 2;
     return TP_OK;
 }
 
-// Pressure + Adami of state s (wall state into A.wp / A.wr / A.wnum / A.wvol).
+// Pressure + Adami of state s over the wall lists of L, into W.
 template <typename T, int ND>
-tp_status wall_state(tp_handle* h, const AdjPhys<T>& P, AState<T> s) {
+tp_status wall_state(tp_handle* h, const AdjPhys<T>& P, AState<T> s, const ListSet& L,
+                     const WallSet<T>& W) {
     AdjointState& A = *h->adj;
-    k_adj_pressure<T><<<nb(A.nf, 256), 256, 0, h->stream>>>(P, s.r, (T*)A.pf, A.nf);
+    k_adj_pressure<T><<<nb(A.nf, 256), 256, 0, h->stream>>>(P, s.r, W.pf, A.nf);
     if (A.nw > 0)
         k_adj_adami<T, ND><<<nb(A.nw, 128), 128, 0, h->stream>>>(
-            P, A.nw, (const double4_32a*)h->w_pos, A.wf, A.wfc, s, (const T*)A.pf, (T*)A.wp,
-            (T*)A.wr, (T*)A.wnum, (T*)A.wvol);
+            P, A.nw, (const double4_32a*)h->w_pos, L.wf, L.wfc, s, (const T*)W.pf, W.wp, W.wr,
+            W.wnum, W.wvol);
     ADJ_LAUNCHED(h, "adjoint wall state");
     A.kernels += 1 + (A.nw > 0);
     return TP_OK;
@@ -1102,17 +1177,22 @@ tp_status wall_state(tp_handle* h, const AdjPhys<T>& P, AState<T> s) {
 
 // One CK2N54 step from state `from` using `scratch` as the ping-pong partner; the result lands
 // in `out`.  With `tape` non-null the five stage inputs are tape[0..4] (tape[0] = from) and the
-// result is tape[5].
+// result is tape[5].  `lists` (optional) receives the step's neighbour lists and `walls`
+// (optional, five entries) the pressure / wall state of each stage; by default both go to the
+// handle's working arrays.
 template <typename T, int ND>
 tp_status forward_step(tp_handle* h, const AdjPhys<T>& P, double dt, AState<T> from,
-                       AState<T> other, AState<T>* tape, AState<T>* out) {
+                       AState<T> other, AState<T>* tape, AState<T>* out,
+                       const ListSet* lists = nullptr, const WallSet<T>* walls = nullptr) {
     AdjointState& A = *h->adj;
-    tp_status st = build_lists_at<ND>(h, from.x);
+    const ListSet L = lists ? *lists : lists_of(A);
+    tp_status st = build_lists_at<ND>(h, from.x, L);
     if (st != TP_OK) return st;
     AState<T> src = from;
     for (int i = 0; i < 5; ++i) {
         AState<T> dst = tape ? tape[i + 1] : ((i % 2 == 0) ? other : from);
-        st = wall_state<T, ND>(h, P, src);
+        const WallSet<T> W = walls ? walls[i] : walls_of<T>(A);
+        st = wall_state<T, ND>(h, P, src, L, W);
         if (st != TP_OK) return st;
         AdjStage<T> S;
         S.A = (T)kCK2N54_A[i];
@@ -1123,8 +1203,8 @@ tp_status forward_step(tp_handle* h, const AdjPhys<T>& P, double dt, AState<T> f
         S.dtd = dt;
         S.first = i == 0;
         k_adj_stage<T, ND><<<nb(A.nf, 128), 128, 0, h->stream>>>(
-            P, A.nf, src, dst, (const T*)A.pf, (const T*)A.mf, A.ff, A.ffc, A.fw, A.fwc,
-            (const double4_32a*)h->w_pos, (const T*)A.wp, (const T*)A.wr, A.tx, (T*)A.tv,
+            P, A.nf, src, dst, (const T*)W.pf, (const T*)A.mf, L.ff, L.ffc, L.fw, L.fwc,
+            (const double4_32a*)h->w_pos, (const T*)W.wp, (const T*)W.wr, A.tx, (T*)A.tv,
             (T*)A.tr, S);
         ADJ_LAUNCHED(h, "adjoint forward stage");
         A.kernels += 1;
@@ -1225,37 +1305,67 @@ tp_status backward_impl(tp_handle* h, double* v_bar, double* u_bar, double* para
     ADJ_LAUNCHED(h, "adjoint seed load");
     std::vector<AState<T>> tape(A.n_tape);
     for (size_t k = 0; k < A.n_tape; ++k) tape[k] = state_at<T>(A, A.tape, k);
+    // segment storage for the lists and wall states of the recomputation (used when it takes at
+    // most a quarter of the free device memory; otherwise the reverse sweep rebuilds them)
+    const long long seg_steps = std::min(A.every, A.n_steps);
+    const size_t want = seg_bytes_for<T>(A, seg_steps);
+    if (A.seg_bytes < want) {
+        if (A.seg) cudaFree(A.seg);
+        A.seg = nullptr;
+        A.seg_bytes = 0;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && want <= free_b / 4 &&
+            dmalloc(&A.seg, want) == cudaSuccess)
+            A.seg_bytes = want;
+        else
+            cudaGetLastError();  // a refused allocation only selects the rebuilding path
+    }
+    const bool keep = A.seg != nullptr;
+    std::vector<ListSet> seg_l;
+    std::vector<WallSet<T>> seg_w;
+    if (keep) {
+        for (long long j = 0; j < seg_steps; ++j) seg_l.push_back(seg_lists(A, j));
+        for (long long k = 0; k < 5 * seg_steps; ++k) seg_w.push_back(seg_walls<T>(A, seg_steps, k));
+    }
     const long long n_seg = (A.n_steps + A.every - 1) / A.every;
     for (long long seg = n_seg - 1; seg >= 0; --seg) {
         const long long s0 = seg * A.every;
         const long long ns = std::min(A.every, A.n_steps - s0);
-        // recompute the segment, recording every stage input
+        // recompute the segment, recording every stage input (and, with segment storage, the
+        // lists of every step and the wall state of every stage)
         k_adj_copy<T, ND><<<nb(A.nf, 256), 256, 0, h->stream>>>(
             state_at<T>(A, A.ckpt, (size_t)seg), tape[0], A.nf);
         ADJ_LAUNCHED(h, "adjoint restore");
         for (long long j = 0; j < ns; ++j) {
             AState<T> out;
-            tp_status st =
-                forward_step<T, ND>(h, P, A.dt, tape[5 * j], tape[5 * j], &tape[5 * j], &out);
+            tp_status st = forward_step<T, ND>(h, P, A.dt, tape[5 * j], tape[5 * j], &tape[5 * j],
+                                               &out, keep ? &seg_l[j] : nullptr,
+                                               keep ? &seg_w[5 * j] : nullptr);
             if (st != TP_OK) return st;
         }
         // reverse the segment's steps and stages
         for (long long j = ns - 1; j >= 0; --j) {
-            tp_status st = build_lists_at<ND>(h, tape[5 * j].x);
-            if (st != TP_OK) return st;
+            const ListSet LS = keep ? seg_l[j] : lists_of(A);
+            if (!keep) {
+                tp_status st = build_lists_at<ND>(h, tape[5 * j].x, LS);
+                if (st != TP_OK) return st;
+            }
             for (int i = 4; i >= 0; --i) {
                 const AState<T> U = tape[5 * j + i];
-                st = wall_state<T, ND>(h, P, U);
-                if (st != TP_OK) return st;
+                const WallSet<T> W = keep ? seg_w[5 * j + i] : walls_of<T>(A);
+                if (!keep) {
+                    tp_status st = wall_state<T, ND>(h, P, U, LS, W);
+                    if (st != TP_OK) return st;
+                }
                 k_adj_seed<T, ND><<<nb(std::max(A.nf, A.nw), 256), 256, 0, h->stream>>>(
                     L, (T)kCK2N54_A[i], (T)kCK2N54_B[i], (T)A.dt, A.nf, A.nw);
                 k_adj_pair_vjp<T, ND><<<nb(A.nf, 128), 128, 0, h->stream>>>(
-                    P, A.nf, U, (const T*)A.pf, (const T*)A.mf, A.ff, A.ffc, A.fw, A.fwc,
-                    (const double4_32a*)h->w_pos, (const T*)A.wp, (const T*)A.wr, L, A.theta);
+                    P, A.nf, U, (const T*)W.pf, (const T*)A.mf, LS.ff, LS.ffc, LS.fw, LS.fwc,
+                    (const double4_32a*)h->w_pos, (const T*)W.wp, (const T*)W.wr, L, A.theta);
                 if (A.nw > 0)
                     k_adj_adami_vjp<T, ND><<<nb(A.nw, 128), 128, 0, h->stream>>>(
-                        P, A.nw, (const double4_32a*)h->w_pos, A.wf, A.wfc, U, (const T*)A.pf,
-                        (const T*)A.wp, (const T*)A.wnum, (const T*)A.wvol, L, A.theta);
+                        P, A.nw, (const double4_32a*)h->w_pos, LS.wf, LS.wfc, U, (const T*)W.pf,
+                        (const T*)W.wp, (const T*)W.wnum, (const T*)W.wvol, L, A.theta);
                 k_adj_eos_vjp<T><<<nb(A.nf, 256), 256, 0, h->stream>>>(P, U.r, L, A.nf);
                 ADJ_LAUNCHED(h, "adjoint stage");
                 A.kernels += 3 + (A.nw > 0);
