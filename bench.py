@@ -230,10 +230,11 @@ def rebuilds(semi):
     return int(c.value)
 
 
-def timed_window(torch, semi, v, u, steps, warmup, dt, clk=None, dist=None):
+def timed_window(torch, semi, v, u, steps, warmup, dt, clk=None, dist=None, label="window"):
     """`warmup` untimed steps, then `steps` timed CK2N54 steps of (v, u) in one fused call
     (CUDA events on the launching stream, synchronised on both sides); phase times from the
-    library's event pool; rebuilds of the neighbour search inside the timed steps."""
+    library's event pool; rebuilds of the neighbour search inside the timed steps.  The timed
+    call runs inside the NVTX range `label` (ncu --nvtx --nvtx-include selects its launches)."""
     lib = semi._lib
     semi._set_stream()
     if warmup:
@@ -251,11 +252,13 @@ def timed_window(torch, semi, v, u, steps, warmup, dt, clk=None, dist=None):
     import contextlib
 
     with (clk if clk is not None else contextlib.nullcontext()):
+        torch.cuda.nvtx.range_push(label)
         e0.record(stream)
         semi._call("tp_integrate_ck2n54", v.data_ptr(), u.data_ptr(), ctypes.c_double(0.0),
                    ctypes.c_double(dt), ctypes.c_int64(steps))
         e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     semi.sync()
     if dist:
         dist.barrier()
@@ -337,7 +340,7 @@ def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
     specs = e.ensemble_specs(n_instances, seed)
     groups = e.build_ensemble(specs)
     setup_s = time.perf_counter() - t0
-    tuned = e.autotune(groups, trial_steps=2)
+    tuned = e.autotune(groups, trial_steps=6)
     eg = e.EnsembleGraph(groups, steps_per_replay)
     eg.reset()
     eg.replay()  # warm-up replay
@@ -741,7 +744,7 @@ def main():
 
     # the same window from the hydrostatic start (no particle moves far enough for a rebuild)
     v0, u0 = ode.v0.clone(), ode.u0.clone()
-    rest = timed_window(torch, semi, v0, u0, args.steps, args.warmup, dt)
+    rest = timed_window(torch, semi, v0, u0, args.steps, args.warmup, dt, label="at_rest")
     del v0, u0
 
     # end to end through the C ABI with host buffers, from the flowing state
@@ -752,7 +755,8 @@ def main():
     # the reference's schedule: cell list and neighbour lists rebuilt at every stage (skin 0)
     semi._call("tp_set_skin", ctypes.c_double(0.0))
     v, u = v_flow.clone(), u_flow.clone()
-    every = timed_window(torch, semi, v, u, args.steps, args.warmup, dt)
+    every = timed_window(torch, semi, v, u, args.steps, args.warmup, dt,
+                         label="rebuild_every_stage")
 
     out = None
     if rank == 0:
@@ -804,7 +808,7 @@ def main():
             s2, t2 = make_case(pkg, CFG2, prec, local)
             o2 = pkg.semidiscretize(s2, (0.0, 1.0))
             v2, u2 = vf2.clone(), uf2.clone()
-            w2 = timed_window(torch, s2, v2, u2, k, args.warmup, CFG2["dt"])
+            w2 = timed_window(torch, s2, v2, u2, k, args.warmup, CFG2["dt"], label=f"form_{prec}")
             n2 = s2.n_fluid + s2.n_wall
             forms[prec] = {
                 "value": n2 * k / (w2["ms"] / 1e3), "ms_per_step": w2["ms"] / k, "steps": k,

@@ -369,8 +369,10 @@ int64_t tp_adjoint_kernel_launches(const tp_handle* h);
  * than the kernel support, so that they never interact) -- with their device state (v_ode,
  * u_ode in the reference layout, integrated in place) and time step.
  *   tp_batch_autotune: per member, times `trial_steps` steps on scratch copies of the state
- *     for pair-kernel block sizes {64, 128, 256} x list skins {0.05, 0.1, 0.2} and keeps the
- *     fastest; outputs (per member, optional): block size, skin, ms per step.
+ *     for every pair pass (neighbour lists; in the FP32 form also cell tiles staged in shared
+ *     memory, TP_PAIR_TILED) x list skins {0.03, 0.05, 0.1, 0.2} x pair-kernel block sizes
+ *     {64, 128, 256} (the tiled pass: 256) and keeps the fastest; outputs (per member, optional):
+ *     block size, skin, pair mode, ms per step.
  *   tp_batch_capture: sizes every member's lists for `growth` x the densest cell now
  *     (tp_prepare_lists), warms up on scratch state, then records `steps` steps of every member
  *     into one CUDA graph, the members as parallel branches.
@@ -384,7 +386,7 @@ tp_status tp_batch_create(tp_handle* const* handles, int32_t n, tp_batch** out);
 tp_status tp_batch_destroy(tp_batch* b);
 tp_status tp_batch_set_state(tp_batch* b, int32_t member, double* v_ode, double* u_ode, double dt);
 tp_status tp_batch_autotune(tp_batch* b, int32_t trial_steps, int32_t* pair_block_out,
-                            double* skin_out, double* ms_out);
+                            double* skin_out, int32_t* pair_mode_out, double* ms_out);
 tp_status tp_batch_capture(tp_batch* b, int64_t steps, double growth);
 tp_status tp_batch_launch(tp_batch* b, void* stream);
 tp_status tp_batch_sync(tp_batch* b);

@@ -110,7 +110,8 @@ static int run(int nd, int precision) {
     bad |= tp_batch_set_state(b, 0, v.data(), u.data(), 1e-4) != TP_OK;
     int32_t blk = 0;
     double skin = 0.0, tms = 0.0;
-    bad |= tp_batch_autotune(b, 2, &blk, &skin, &tms) != TP_OK;
+    int32_t mode = -1;
+    bad |= tp_batch_autotune(b, 2, &blk, &skin, &mode, &tms) != TP_OK || mode < 0;
     bad |= (blk != 64 && blk != 128 && blk != 256);
     bad |= tp_batch_capture(b, 3, 1.5) != TP_OK;
     bad |= tp_batch_steps(b) != 3;

@@ -115,7 +115,9 @@ def test_autotune_choice_keeps_results(pkg, cuda):
     for g in groups:
         c = choice[g.dx]
         assert c["pair_block"] in (64, 128, 256)
-        assert c["skin"] in (0.05, 0.1, 0.2)
+        assert c["skin"] in (0.03, 0.05, 0.1, 0.2)
+        assert c["pair_mode"] in ("lists", "tiled")
+        assert c["pair_mode"] == "lists" or c["pair_block"] == 256
         assert c["ms_per_step"] > 0.0
         _eager(pkg, g, K)
     for g, r in zip(groups, ref):

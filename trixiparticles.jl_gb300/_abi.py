@@ -120,7 +120,8 @@ PROTOTYPES = [
     ("tp_batch_destroy", c_int32, [c_void_p]),
     ("tp_batch_set_state", c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_double]),
     ("tp_batch_autotune", c_int32,
-     [c_void_p, c_int32, POINTER(c_int32), POINTER(c_double), POINTER(c_double)]),
+     [c_void_p, c_int32, POINTER(c_int32), POINTER(c_double), POINTER(c_int32),
+      POINTER(c_double)]),
     ("tp_batch_capture", c_int32, [c_void_p, c_int64, c_double]),
     ("tp_batch_launch", c_int32, [c_void_p, c_void_p]),
     ("tp_batch_sync", c_int32, [c_void_p]),

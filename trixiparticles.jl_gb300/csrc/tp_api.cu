@@ -422,6 +422,8 @@ void setup_phys(tp_handle* h) {
     Q.visc_k = Q.visc_ac * Q.visc_h;
     Q.diff2 = 2.0f * Q.diff_coef;
     Q.az2 = std::nextafter(Q.sr2, INFINITY) - Q.sr2;
+    Q.gamma7 = P.gamma == 7.0;
+    Q.inv_rho0 = 1.0f / Q.rho0;
 }
 
 bool setup_grid(tp_handle* h, std::string& msg) {
@@ -838,6 +840,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc((double4_32a**)&h->f_pos, nf));
     A(dalloc((double4_32a**)&h->f_vel, nf));
     A(dalloc((double4_32a**)&h->f_aux, nf));
+    if (cfg->precision == TP_PRECISION_FP32) A(dalloc((double4_32a**)&h->f_rec, nf));
     A(dalloc(&h->m_f, nf));
     A(dalloc(&h->w_key, nw));
     A(dalloc(&h->w_tmp, nw));
@@ -881,7 +884,7 @@ tp_status tp_destroy(tp_handle* h) {
     adjoint_release(h);
     void* ptrs[] = {h->f_key,   h->f_tmp,   h->f_perm,  h->f_skey,        h->f_count,
                     h->f_start, h->f_cursor, h->scan_partial, h->f_test, h->f_pos,
-                    h->f_vel,   h->f_aux,   h->m_f,     h->w_key,         h->w_tmp,
+                    h->f_vel,   h->f_aux,   h->f_rec,   h->m_f,     h->w_key,   h->w_tmp,
                     h->w_perm,  h->w_skey,  h->w_start, h->w_pos,         h->w_test,
                     h->w_state, h->w_p32,   h->w_vol,   h->red_partial, h->d_err};
     for (void* p : ptrs)

@@ -7,7 +7,8 @@
 // one stream per member), each branch the member's fused integrator with list capacities fixed
 // beforehand, so the graph contains no host synchronisation.  tp_batch_launch replays it on a
 // caller stream.  tp_batch_autotune times trial steps of every member on scratch copies of its
-// state over pair-kernel block sizes x neighbour-list skins and keeps the fastest pair.
+// state over the pair pass (neighbour lists or, in the FP32 form, cell tiles staged in shared
+// memory) x neighbour-list skins x pair-kernel block sizes and keeps the fastest combination.
 #include <cmath>
 #include <new>
 #include <string>
@@ -26,6 +27,7 @@ struct tp_batch {
         cudaEvent_t join = nullptr;
         int pair_block = 128;
         double skin = 0.05;
+        int pair_mode = TP_PAIR_GATHER;
         double trial_ms = 0.0;
     };
     std::vector<Member> m;
@@ -160,11 +162,11 @@ tp_status tp_batch_set_state(tp_batch* b, int32_t k, double* v_ode, double* u_od
 }
 
 tp_status tp_batch_autotune(tp_batch* b, int32_t trial_steps, int32_t* pair_block_out,
-                            double* skin_out, double* ms_out) {
+                            double* skin_out, int32_t* pair_mode_out, double* ms_out) {
     if (!b) return TP_ERR_ARGUMENT;
     if (trial_steps <= 0) return bfail(b, TP_ERR_ARGUMENT, "tp_batch_autotune: trial_steps <= 0");
     static const int kBlocks[3] = {64, 128, 256};
-    static const double kSkins[3] = {0.05, 0.1, 0.2};
+    static const double kSkins[4] = {0.03, 0.05, 0.1, 0.2};
     drop_graph(b);
     cudaEvent_t e0, e1;
     B_CUDA(b, cudaEventCreate(&e0));
@@ -181,11 +183,19 @@ tp_status tp_batch_autotune(tp_batch* b, int32_t trial_steps, int32_t* pair_bloc
         if (result != TP_OK) break;
         tp_status st = tp_set_stream(mb.h, mb.stream);
         double best = INFINITY;
-        for (double skin : kSkins) {
+        tp_config cfg{};
+        if (st == TP_OK) st = tp_get_config(mb.h, &cfg);
+        // the tiled pass exists in the FP32 form only and launches fixed 256-thread blocks
+        const int last_mode = cfg.precision == TP_PRECISION_FP32 ? TP_PAIR_TILED : TP_PAIR_GATHER;
+        for (int mode = TP_PAIR_GATHER; mode <= last_mode; ++mode) {
+          if (mode == TP_PAIR_SYMMETRIC) continue;
+          if (st == TP_OK) st = tp_set_pair_mode(mb.h, mode);
+          for (double skin : kSkins) {
             if (st == TP_OK) st = tp_set_skin(mb.h, skin);
             if (st == TP_OK) st = tp_prepare_lists(mb.h, s.u, 1.5);
             for (int blk : kBlocks) {
                 if (st != TP_OK) break;
+                if (mode == TP_PAIR_TILED && blk != 256) continue;
                 st = tp_set_launch(mb.h, blk);
                 if (st == TP_OK) result = restore_scratch(b, mb, s);
                 if (st == TP_OK && result == TP_OK)
@@ -207,17 +217,22 @@ tp_status tp_batch_autotune(tp_batch* b, int32_t trial_steps, int32_t* pair_bloc
                     best = per;
                     mb.pair_block = blk;
                     mb.skin = skin;
+                    mb.pair_mode = mode;
                 }
             }
             if (st != TP_OK || result != TP_OK) break;
+          }
+          if (st != TP_OK || result != TP_OK) break;
         }
         if (st == TP_OK) st = tp_sync(mb.h);
+        if (st == TP_OK) st = tp_set_pair_mode(mb.h, mb.pair_mode);
         if (st == TP_OK) st = tp_set_skin(mb.h, mb.skin);
         if (st == TP_OK) st = tp_set_launch(mb.h, mb.pair_block);
         if (st != TP_OK && result == TP_OK) result = member_fail(b, k, st);
         mb.trial_ms = best;
         if (pair_block_out) pair_block_out[k] = mb.pair_block;
         if (skin_out) skin_out[k] = mb.skin;
+        if (pair_mode_out) pair_mode_out[k] = mb.pair_mode;
         if (ms_out) ms_out[k] = best;
     }
     cudaEventDestroy(e0);

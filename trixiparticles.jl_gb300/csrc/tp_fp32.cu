@@ -33,10 +33,36 @@ struct Kahan {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// Cole EOS on the density deviation.  With the exponent 7 (the dam-break setups) it is the
+// binomial expansion (1 + d)^7 - 1 = d (7 + d (21 + d (35 + d (35 + d (21 + d (7 + d)))))) of
+// d = (rho - rho0) / rho0, six FMAs without cancellation (a few ulp of the exact power); the
+// pair pass evaluates it for every accepted neighbour instead of gathering the pressure, and the
+// pack writes the same value for the particle itself.
 __device__ __forceinline__ float eos32(float drho, const Phys32& P, int clip) {
-    float p = P.B * expm1f(P.gamma * log1pf(drho / P.rho0)) + P.p_bg;
+    float p;
+    if (P.gamma7) {
+        const float d = drho * P.inv_rho0;
+        float q = 7.0f + d;
+        q = fmaf(q, d, 21.0f);
+        q = fmaf(q, d, 35.0f);
+        q = fmaf(q, d, 35.0f);
+        q = fmaf(q, d, 21.0f);
+        q = fmaf(q, d, 7.0f);
+        p = fmaf(P.B * d, q, P.p_bg);
+    } else {
+        p = P.B * expm1f(P.gamma * log1pf(drho / P.rho0)) + P.p_bg;
+    }
     if (clip) p = (p != p || p > 0.0f) ? p : 0.0f;
     return p;
+}
+
+// One 32-byte pair record {test, velocity} with a single 256-bit load (the record is 32-byte
+// aligned: one sector), through the read-only path.
+__device__ __forceinline__ void load_rec32(const float4* __restrict__ rec, int s, float4& t,
+                                           float4& v) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w), "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(rec + 2 * (size_t)s));
 }
 
 __device__ __forceinline__ float eos32_inverse_dev(float p, const Phys32& P) {
@@ -62,6 +88,7 @@ struct Pack32 {
     float4* test;  // {ox, oy, oz, rho - rho0}
     float4* vel;   // {vx, vy, vz, m / rho}
     float* pres;   // p
+    float4* rec;   // {test, vel} in one 32-byte record (the list pair pass)
     const int* src_perm;  // kick! path: without a rebuild, slot s packs caller particle perm[s]
     GridDesc g;
     double cs32, rho0;
@@ -90,8 +117,11 @@ struct Pack32 {
         t.w = w.w;
         test[s] = t;
         const float irho = __frcp_rn(P.rho0 + w.w);
-        vel[s] = make_float4(w.x, w.y, w.z, mi * irho);
+        const float4 vr = make_float4(w.x, w.y, w.z, mi * irho);
+        vel[s] = vr;
         pres[s] = eos32(w.w, P, P.fluid_clip);
+        rec[2 * (size_t)s] = t;
+        rec[2 * (size_t)s + 1] = vr;
         if (rebuild && xb_out) {
 #pragma unroll
             for (int d = 0; d < ND; ++d) xb_out[(size_t)s * ND + d] = x[d];
@@ -326,28 +356,29 @@ __device__ __forceinline__ void fw_terms32(const Phys32& P, float4 va, float p_a
     q.r = fmaf((rho_a * vol_b) * sg, vx, q.r);
 }
 
-// List entry e with the candidate's test record cb: the exact test, then the pair terms.
+// List entry e: the candidate's 32-byte record (test and velocity, one 256-bit load), the
+// exact test on the cell-relative difference (cell offset decoded from the entry), then the
+// pair terms with the candidate's pressure from its density deviation (the value the pack wrote
+// for it, recomputed instead of gathered).
 template <int ND, bool STD>
-__device__ __forceinline__ void ff_pair32(const Phys32& P, const float4* off, float4 ta,
-                                          float4 va, float p_a, float rho_a, float ia,
-                                          float drho_a, unsigned e, float4 cb,
-                                          const float4* __restrict__ fvel,
-                                          const float* __restrict__ fpres, FluidSums& q) {
+__device__ __forceinline__ void ff_pair32(const Phys32& P, float4 ta, float4 va, float p_a,
+                                          float rho_a, float ia, float drho_a, unsigned e,
+                                          const float4* __restrict__ frec, FluidSums& q) {
+    float4 cb, vb;
+    load_rec32(frec, (int)(e & kSlotMask), cb, vb);
     float pd0, pd1, pd2;
-    const float d2 = pair_diff<ND>(ta, off, e, cb, pd0, pd1, pd2);
+    const float d2 = pair_diff_decoded<ND>(ta, P.cs, e, cb, pd0, pd1, pd2);
     if (d2 > P.sr2 || d2 < P.az2) return;
-    const int b = (int)(e & kSlotMask);
-    ff_terms32<ND, STD>(P, va, p_a, rho_a, ia, drho_a, pd0, pd1, pd2, d2, cb, fvel[b], fpres[b],
-                        q);
+    ff_terms32<ND, STD>(P, va, p_a, rho_a, ia, drho_a, pd0, pd1, pd2, d2, cb, vb,
+                        eos32(cb.w, P, P.fluid_clip), q);
 }
 
 template <int ND>
-__device__ __forceinline__ void fw_pair32(const Phys32& P, const float4* off, float4 ta,
-                                          float4 va, float p_a, float rho_a, float ia,
-                                          unsigned e, float4 tb,
+__device__ __forceinline__ void fw_pair32(const Phys32& P, float4 ta, float4 va, float p_a,
+                                          float rho_a, float ia, unsigned e, float4 tb,
                                           const float* __restrict__ wpres, FluidSums& q) {
     float pd0, pd1, pd2;
-    const float d2 = pair_diff<ND>(ta, off, e, tb, pd0, pd1, pd2);
+    const float d2 = pair_diff_decoded<ND>(ta, P.cs, e, tb, pd0, pd1, pd2);
     if (d2 > P.sr2 || d2 < P.az2) return;
     fw_terms32<ND>(P, va, p_a, rho_a, ia, pd0, pd1, pd2, d2, tb.w, wpres[e & kSlotMask], q);
 }
@@ -357,6 +388,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
                                                 const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float* __restrict__ fpres,
+                                                const float4* __restrict__ frec,
                                                 const unsigned* __restrict__ ff,
                                                 const int* __restrict__ ffc,
                                                 const unsigned* __restrict__ fw,
@@ -364,8 +396,6 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
                                                 const float4* __restrict__ wtest,
                                                 const float* __restrict__ wpres,
                                                 unsigned* __restrict__ gate, Update32 U) {
-    __shared__ float4 off[kOffsetCodes];
-    fill_offset_table(off, P.cs);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nf) return;
     const float4 ta = ftest[s];  // {offsets, rho - rho0}
@@ -384,52 +414,43 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
     };
     const int nff = ffc[s];
     for (int k = 0; k < (nff & ~3); k += 4) {
-        const uint4 l = list_quad(ff, k, nf, s);
+        const uint4 l = list_quad_stream(ff, k, nf, s);
         FluidSums q;
-        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.x, ftest[l.x & kSlotMask],
-                           fvel, fpres, q);
-        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.y, ftest[l.y & kSlotMask],
-                           fvel, fpres, q);
-        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.z, ftest[l.z & kSlotMask],
-                           fvel, fpres, q);
-        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.w, ftest[l.w & kSlotMask],
-                           fvel, fpres, q);
+        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.x, frec, q);
+        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.y, frec, q);
+        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.z, frec, q);
+        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.w, frec, q);
         settle(q);
     }
     if (nff & 3) {  // the open quad: entries beyond the count are not part of the list
         const int k = nff & ~3, m = nff & 3;
-        const uint4 l = list_quad(ff, k, nf, s);
+        const uint4 l = list_quad_stream(ff, k, nf, s);
         FluidSums q;
-        ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.x, ftest[l.x & kSlotMask],
-                           fvel, fpres, q);
-        if (m > 1)
-            ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.y,
-                               ftest[l.y & kSlotMask], fvel, fpres, q);
-        if (m > 2)
-            ff_pair32<ND, STD>(P, off, ta, va, p_a, rho_a, ia, drho_a, l.z,
-                               ftest[l.z & kSlotMask], fvel, fpres, q);
+        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.x, frec, q);
+        if (m > 1) ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.y, frec, q);
+        if (m > 2) ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.z, frec, q);
         settle(q);
     }
     // the wall neighbours continue the same compensated sums
     const int nfw = fwc[s];
     for (int k = 0; k < (nfw & ~3); k += 4) {
-        const uint4 l = list_quad(fw, k, nf, s);
+        const uint4 l = list_quad_stream(fw, k, nf, s);
         FluidSums q;
-        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.x, wtest[l.x & kSlotMask], wpres, q);
-        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.y, wtest[l.y & kSlotMask], wpres, q);
-        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.z, wtest[l.z & kSlotMask], wpres, q);
-        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.w, wtest[l.w & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.x, wtest[l.x & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.y, wtest[l.y & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.z, wtest[l.z & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.w, wtest[l.w & kSlotMask], wpres, q);
         settle(q);
     }
     if (nfw & 3) {
         const int k = nfw & ~3, m = nfw & 3;
-        const uint4 l = list_quad(fw, k, nf, s);
+        const uint4 l = list_quad_stream(fw, k, nf, s);
         FluidSums q;
-        fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.x, wtest[l.x & kSlotMask], wpres, q);
+        fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.x, wtest[l.x & kSlotMask], wpres, q);
         if (m > 1)
-            fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.y, wtest[l.y & kSlotMask], wpres, q);
+            fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.y, wtest[l.y & kSlotMask], wpres, q);
         if (m > 2)
-            fw_pair32<ND>(P, off, ta, va, p_a, rho_a, ia, l.z, wtest[l.z & kSlotMask], wpres, q);
+            fw_pair32<ND>(P, ta, va, p_a, rho_a, ia, l.z, wtest[l.z & kSlotMask], wpres, q);
         settle(q);
     }
 
@@ -665,6 +686,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         pk.test = h->f_test;
         pk.vel = (float4*)h->f_vel;
         pk.pres = (float*)h->f_aux;
+        pk.rec = (float4*)h->f_rec;
         pk.g = h->grid;
         pk.cs32 = cs32;
         pk.rho0 = h->cfg.reference_density;
@@ -724,8 +746,9 @@ static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
         }
         k_pair32<ND, INTEG, decltype(stdc)::value><<<nblk(nf, h->pair_block), h->pair_block, 0,
                                                      h->stream>>>(
-            P, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux, h->l_ff, h->c_ff,
-            h->l_fw, h->c_fw, h->w_test, h->w_p32, gate, U);
+            P, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux,
+            (const float4*)h->f_rec, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test, h->w_p32, gate,
+            U);
     };
     if (std_cfg)
         run(std::true_type{});

@@ -61,6 +61,9 @@ struct tp_handle {
     void* f_pos = nullptr;     // FP64 form / diagnostics: double4 {x, y, z, p}
     void* f_vel = nullptr;     // FP64: double4 {v, rho};  FP32: float4 {v, m / rho}
     void* f_aux = nullptr;     // FP64: double4 (see the pack);  FP32: float p
+    // FP32 pair record, 32 bytes per slot (one 256-bit load per neighbour):
+    // {ox, oy, oz, rho - rho0, vx, vy, vz, m / rho}
+    void* f_rec = nullptr;
 
     // ---- fluid masses in caller order (FP64) ----
     double* m_f = nullptr;

@@ -86,6 +86,9 @@ struct Phys32 {
     float p_off;
     // derived constants of the FP32 pair kernel (see the FP64 ones)
     float sg_c, half_hinv, visc_k, diff2, az2;
+    // Cole EOS with the exponent 7: evaluated as a polynomial in (rho - rho0) / rho0
+    int gamma7;
+    float inv_rho0;
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

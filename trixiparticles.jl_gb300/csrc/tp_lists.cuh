@@ -44,6 +44,17 @@ __device__ __forceinline__ uint4 list_quad(const unsigned* __restrict__ list, in
     return *reinterpret_cast<const uint4*>(list + list_at(k, stride, s));
 }
 
+// The same for a pass that reads each list entry once: the quad is not allocated in L1, which
+// keeps L1 for the neighbour records the pass gathers (ld.global.nc with L1::no_allocate).
+__device__ __forceinline__ uint4 list_quad_stream(const unsigned* __restrict__ list, int k,
+                                                  int stride, int s) {
+    uint4 q;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(q.x), "=r"(q.y), "=r"(q.z), "=r"(q.w)
+        : "l"(list + list_at(k, stride, s)));
+    return q;
+}
+
 // The same for a list written earlier in the same kernel by the reading thread (the exact pair
 // lists of the fused FP64 pass): plain loads, never the read-only data path.
 __device__ __forceinline__ unsigned list_next_rw(const unsigned* list, int k, int stride, int s,
@@ -93,6 +104,36 @@ __device__ __forceinline__ float pair_diff(float4 ta, const float4* tab, unsigne
     pdz = 0.0f;
     if (ND == 3) {
         pdz = (ta.z - o.z) - cb.z;
+        d2 = fmaf(pdz, pdz, d2);
+    }
+    return d2;
+}
+
+// The cell offset of a list entry as FP32 multiples of the cell size, decoded arithmetically
+// from the code (dx+2) + 5 (dy+2) + 25 (dz+2) (exact for the 125 codes: the digits come from
+// floor((c + 1/2) / 25) and floor((r + 1/2) / 5) in FP32), so that pair differences can be formed
+// without the shared offset table: (o_a - d cs) is fmaf(-d, cs, o_a), the table's rounding.
+__device__ __forceinline__ void entry_cell_offset(unsigned e, float& fx, float& fy, float& fz) {
+    const float c = (float)(e >> kSlotBits);
+    fz = floorf(fmaf(c, 0.04f, 0.02f));
+    const float r = fmaf(-25.0f, fz, c);
+    fy = floorf(fmaf(r, 0.2f, 0.1f));
+    fx = fmaf(-5.0f, fy, r) - 2.0f;
+    fy -= 2.0f;
+    fz -= 2.0f;
+}
+
+template <int ND>
+__device__ __forceinline__ float pair_diff_decoded(float4 ta, float cs, unsigned e, float4 cb,
+                                                   float& pdx, float& pdy, float& pdz) {
+    float fx, fy, fz;
+    entry_cell_offset(e, fx, fy, fz);
+    pdx = fmaf(-fx, cs, ta.x) - cb.x;
+    pdy = fmaf(-fy, cs, ta.y) - cb.y;
+    float d2 = fmaf(pdy, pdy, pdx * pdx);
+    pdz = 0.0f;
+    if (ND == 3) {
+        pdz = fmaf(-fz, cs, ta.z) - cb.z;
         d2 = fmaf(pdz, pdz, d2);
     }
     return d2;

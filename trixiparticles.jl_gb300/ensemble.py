@@ -180,11 +180,13 @@ class Batch:
         n = len(self.groups)
         blk = (ctypes.c_int32 * n)()
         skin = (ctypes.c_double * n)()
+        mode = (ctypes.c_int32 * n)()
         ms = (ctypes.c_double * n)()
-        self._check(self.lib.tp_batch_autotune(self._b, trial_steps, blk, skin, ms))
+        self._check(self.lib.tp_batch_autotune(self._b, trial_steps, blk, skin, mode, ms))
         out = {}
         for k, g in enumerate(self.groups):
-            g.tuned = {"pair_block": int(blk[k]), "skin": float(skin[k]),
+            g.tuned = {"pair_mode": "tiled" if mode[k] == _abi.TP_PAIR_TILED else "lists",
+                       "pair_block": int(blk[k]), "skin": float(skin[k]),
                        "ms_per_step": float(ms[k])}
             out[g.dx] = g.tuned
         return out
@@ -215,8 +217,9 @@ class Batch:
 
 
 def autotune(groups: list[Group], trial_steps: int = 3) -> dict:
-    """Picks (pair_block, skin) per group with the native autotuner (trial steps on scratch
-    copies of the state); leaves each group's handle set to its choice; returns {dx: choice}."""
+    """Picks (pair pass, pair_block, skin) per group with the native autotuner (trial steps on
+    scratch copies of the state); leaves each group's handle set to its choice; returns
+    {dx: choice}."""
     b = Batch(groups)
     try:
         return b.autotune(trial_steps)

@@ -327,8 +327,9 @@ function batch_create(members; steps=5, autotune=true, growth=1.5)
                      b[], Int32(k - 1), v_ptr(v, semi, hds[k]), u_ptr(u, semi, hds[k]), dt))
     end
     autotune && bcheck(ccall((:tp_batch_autotune, libtp), Cint,
-                             (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}),
-                             b[], Int32(3), C_NULL, C_NULL, C_NULL))
+                             (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Ptr{Int32},
+                              Ptr{Float64}),
+                             b[], Int32(6), C_NULL, C_NULL, C_NULL, C_NULL))
     bcheck(ccall((:tp_batch_capture, libtp), Cint, (Ptr{Cvoid}, Int64, Float64),
                  b[], steps, growth))
     return b[]
