@@ -485,6 +485,49 @@ def run_adjoint(pkg, torch, dx=0.01, n_steps=500, every=25, fd_h=1e-4, seed=7):
             "backward_over_fused_step": bwd_step / integ_ms}
 
 
+def run_profile_adjoint(args, dx=0.01, every=25, seed=7):
+    """Profiling mode of the differentiation form: the FP32 adjoint of the 2D dam break at
+    dx = 0.01 (20 000 fluid) over --steps steps (checkpoints every 25), forward then backward,
+    without the finite-difference checks; one summary line.  Used under ncu for the launch list
+    of the backward pass."""
+    import torch
+
+    import __graft_entry__ as g
+
+    pkg = g.load_package()
+    pkg.load_library()
+    dt = 5e-3 * dx
+    tank, eos = pkg.dam_break(2, dx, (2.0, 1.0), (5.366, 4.0), n_layers=3)
+    n = tank.fluid.n_particles
+    rng = np.random.default_rng(seed)
+    v0 = np.zeros((n, 3))
+    v0[:, :2] = rng.normal(0.0, 0.1, (n, 2))
+    v0[:, 2] = tank.fluid.density
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a).reshape(-1), device="cuda")
+    semi = pkg.dam_break_semidiscretization(tank, eos, 1.75 * dx, precision="float32")
+    pkg.semidiscretize(semi, (0.0, 1.0))
+    idx = pkg.adjoint.top_layer_indices(tank)
+    k = min(every, args.steps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stream = torch.cuda.current_stream()
+    ev[0].record(stream)
+    traj = pkg.adjoint.Trajectory(semi, dev(v0), dev(tank.fluid.coordinates), dt=dt,
+                                  n_steps=args.steps, checkpoint_every=k)
+    ev[1].record(stream)
+    loss, ubar = pkg.adjoint.surface_height_loss(traj.u, idx, 2)
+    torch.cuda.synchronize()
+    ev[2].record(stream)
+    traj.pullback(torch.zeros_like(traj.v), ubar)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_adjoint": n, "steps": args.steps, "checkpoint_every": k,
+                      "forward_ms_per_step": ev[0].elapsed_time(ev[1]) / args.steps,
+                      "backward_ms_per_step": ev[2].elapsed_time(ev[3]) / args.steps}),
+          flush=True)
+    semi.close()
+    return 0
+
+
 def run_precision_study(pkg, torch, checkpoints=(100, 500, 1000), jitters=(0.0, 0.05),
                         seed=2024):
     """Precision form against the FP64 drop-in on the dx = 0.0064 geometry: relative L2 errors of
@@ -674,6 +717,9 @@ def main():
     ap.add_argument("--profile-flow-time", type=float, default=0.0,
                     help="--profile-form: start from the dam break advanced this many seconds "
                          "by the precision form (untimed; default 0 = hydrostatic start)")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="profiling mode of the differentiation form: FP32 adjoint of the 2D dam "
+                         "break (dx = 0.01) over --steps steps, forward and backward only")
     ap.add_argument("--profile-ensemble", action="store_true",
                     help="profiling mode of the batching form: default launch shape, one warm-up "
                          "replay and --steps replays of the ensemble graph; used under ncu")
@@ -699,6 +745,8 @@ def main():
         return run_profile_form(args)
     if args.profile_ensemble:
         return run_profile_ensemble(args)
+    if args.profile_adjoint:
+        return run_profile_adjoint(args)
 
     import torch
 
