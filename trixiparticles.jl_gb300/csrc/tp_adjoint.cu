@@ -124,6 +124,21 @@ __device__ __forceinline__ T pos_diff(const double* __restrict__ xa, const doubl
     return d2;
 }
 
+// The per-particle kernels of the adjoint run kAdjLanes threads per particle (or wall particle),
+// each over every kAdjLanes-th entry of its lists: the differentiated problems are small (tens of
+// thousands of particles), and one thread per particle leaves a few warps per SM walking their
+// lists one dependent load at a time.  Lane partial sums are combined with shuffles inside the
+// group of kAdjLanes consecutive lanes.
+constexpr int kAdjLanes = 4;
+
+template <typename T>
+__device__ __forceinline__ T lane_group_sum(T x) {
+#pragma unroll
+    for (int off = kAdjLanes / 2; off > 0; off >>= 1)
+        x += __shfl_down_sync(0xffffffffu, x, off, kAdjLanes);
+    return x;  // complete in the group's first lane
+}
+
 // ------------------------------------------------------------------------------------------
 // Neighbour lists in caller order (entry k of particle i at list[k * n + i]).  The search covers
 // the +-1 cells and reaches a second cell along an axis where the point lies within
@@ -324,13 +339,14 @@ __global__ void __launch_bounds__(128) k_adj_adami(AdjPhys<T> P, int nw,
                                                    const T* __restrict__ pf, T* __restrict__ wp,
                                                    T* __restrict__ wr, T* __restrict__ wnum,
                                                    T* __restrict__ wvol) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nw) return;
-    const double4_32a pw = wpos[w];
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = gt / kAdjLanes, sub = gt % kAdjLanes;
+    const bool active = w < nw;
+    const double4_32a pw = wpos[active ? w : 0];
     const double xw[3] = {pw.x, pw.y, pw.z};
     Acc<T> Ps, V;
-    const int n = wfc[w];
-    for (int k = 0; k < n; ++k) {
+    const int n = active ? wfc[w] : 0;
+    for (int k = sub; k < n; k += kAdjLanes) {
         const int f = wf[(size_t)k * nw + w];
         T pd[3];
         const T d2 = pos_diff<T, ND>(xw, s.x + (size_t)f * ND, pd);
@@ -345,7 +361,8 @@ __global__ void __launch_bounds__(128) k_adj_adami(AdjPhys<T> P, int nw,
         Ps.add(sum * W);
         V.add(W);
     }
-    const T num = Ps.value(), vol = V.value();
+    const T num = lane_group_sum(Ps.value()), vol = lane_group_sum(V.value());
+    if (!active || sub != 0) return;
     T p = num;
     if ((double)vol > 2.220446049250313e-16) p = p / vol;
     if (P.wall_clip) p = (p != p || p > T(0)) ? p : T(0);
@@ -369,8 +386,10 @@ __global__ void __launch_bounds__(128) k_adj_stage(
     const int* __restrict__ fw, const int* __restrict__ fwc, const double4_32a* __restrict__ wpos,
     const T* __restrict__ wp, const T* __restrict__ wr, double* __restrict__ tx,
     T* __restrict__ tv, T* __restrict__ tr, AdjStage<T> S) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= nf) return;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sub = gt % kAdjLanes;
+    const bool active = gt / kAdjLanes < nf;
+    const int a = active ? gt / kAdjLanes : 0;
     const double* xa = src.x + (size_t)a * ND;
     T va[3] = {T(0), T(0), T(0)};
 #pragma unroll
@@ -378,8 +397,8 @@ __global__ void __launch_bounds__(128) k_adj_stage(
     const T ra = src.r[a], p_a = pf[a], rho_a = P.rho0 + ra;
 
     Acc<T> dv[3], dr;
-    const int nff = ffc[a];
-    for (int k = 0; k < nff; ++k) {
+    const int nff = active ? ffc[a] : 0;
+    for (int k = sub; k < nff; k += kAdjLanes) {
         const int b = ff[(size_t)k * nf + a];
         T pd[3];
         const T d2 = pos_diff<T, ND>(xa, src.x + (size_t)b * ND, pd);
@@ -430,8 +449,8 @@ __global__ void __launch_bounds__(128) k_adj_stage(
         }
         dr.add(er);
     }
-    const int nfw = fwc[a];
-    for (int k = 0; k < nfw; ++k) {
+    const int nfw = active ? fwc[a] : 0;
+    for (int k = sub; k < nfw; k += kAdjLanes) {
         const int w = fw[(size_t)k * nf + a];
         const double4_32a pw = wpos[w];
         const double xw[3] = {pw.x, pw.y, pw.z};
@@ -453,11 +472,16 @@ __global__ void __launch_bounds__(128) k_adj_stage(
         }
         dr.add((fdiv(rho_a, rho_w) * m_w) * vg);
     }
+    T dvs[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int d = 0; d < ND; ++d) dvs[d] = lane_group_sum(dv[d].value());
+    const T drs = lane_group_sum(dr.value());
+    if (!active || sub != 0) return;
 
     // CarpenterKennedy2N54 stage on (x, v, rho - rho0): t = A t + dt k ; y = y + B t
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
-        const T kv = dv[d].value() + P.g[d];
+        const T kv = dvs[d] + P.g[d];
         const T tvd = S.first ? S.dt * kv : S.dt * kv + S.A * tv[(size_t)a * ND + d];
         tv[(size_t)a * ND + d] = tvd;
         dst.v[(size_t)a * ND + d] = va[d] + S.B * tvd;
@@ -466,7 +490,7 @@ __global__ void __launch_bounds__(128) k_adj_stage(
         tx[(size_t)a * ND + d] = txd;
         dst.x[(size_t)a * ND + d] = fma(S.Bd, txd, xa[d]);
     }
-    const T kr = dr.value();
+    const T kr = drs;
     const T trd = S.first ? S.dt * kr : S.dt * kr + S.A * tr[a];
     tr[a] = trd;
     dst.r[a] = ra + S.B * trd;
@@ -542,7 +566,8 @@ __global__ void __launch_bounds__(128) k_adj_pair_vjp(
     const int* __restrict__ ff, const int* __restrict__ ffc, const int* __restrict__ fw,
     const int* __restrict__ fwc, const double4_32a* __restrict__ wpos, const T* __restrict__ wp,
     const T* __restrict__ wr, AdjLam<T> L, double* __restrict__ theta) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = gt / kAdjLanes, sub = gt % kAdjLanes;
     double th_alpha = 0.0, th_delta = 0.0, th_g = 0.0;
     if (a < nf) {
         const double* xa = s.x + (size_t)a * ND;
@@ -556,12 +581,14 @@ __global__ void __launch_bounds__(128) k_adj_pair_vjp(
         const T ra = s.r[a], p_a = pf[a], rho_a = P.rho0 + ra;
         T xa_bar[3] = {T(0), T(0), T(0)}, va_bar[3] = {T(0), T(0), T(0)};
         T ra_bar = T(0), pa_bar = T(0);
-        // gravity: dv_a += |g| ghat
+        // gravity: dv_a += |g| ghat (once per particle)
+        if (sub == 0) {
 #pragma unroll
-        for (int d = 0; d < ND; ++d) th_g += (double)Lv[d] * (double)P.ghat[d];
+            for (int d = 0; d < ND; ++d) th_g += (double)Lv[d] * (double)P.ghat[d];
+        }
 
         const int nff = ffc[a];
-        for (int k = 0; k < nff; ++k) {
+        for (int k = sub; k < nff; k += kAdjLanes) {
             const int b = ff[(size_t)k * nf + a];
             T pd[3];
             const T d2 = pos_diff<T, ND>(xa, s.x + (size_t)b * ND, pd);
@@ -680,7 +707,7 @@ __global__ void __launch_bounds__(128) k_adj_pair_vjp(
         }
 
         const int nfw = fwc[a];
-        for (int k = 0; k < nfw; ++k) {
+        for (int k = sub; k < nfw; k += kAdjLanes) {
             const int w = fw[(size_t)k * nf + a];
             const double4_32a pw = wpos[w];
             const double xw[3] = {pw.x, pw.y, pw.z};
@@ -747,7 +774,8 @@ __global__ void __launch_bounds__(128) k_adj_adami_vjp(
     const int* __restrict__ wfc, AState<T> s, const T* __restrict__ pf,
     const T* __restrict__ wp, const T* __restrict__ wnum, const T* __restrict__ wvol,
     AdjLam<T> L, double* __restrict__ theta) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = gt / kAdjLanes, sub = gt % kAdjLanes;
     double th_g = 0.0;
     if (w < nw) {
         const T p = wp[w], num = wnum[w], vol = wvol[w];
@@ -762,7 +790,7 @@ __global__ void __launch_bounds__(128) k_adj_adami_vjp(
             const double4_32a pw = wpos[w];
             const double xw[3] = {pw.x, pw.y, pw.z};
             const int n = wfc[w];
-            for (int k = 0; k < n; ++k) {
+            for (int k = sub; k < n; k += kAdjLanes) {
                 const int f = wf[(size_t)k * nw + w];
                 T pd[3];
                 const T d2 = pos_diff<T, ND>(xw, s.x + (size_t)f * ND, pd);
@@ -1167,7 +1195,7 @@ tp_status wall_state(tp_handle* h, const AdjPhys<T>& P, AState<T> s, const ListS
     AdjointState& A = *h->adj;
     k_adj_pressure<T><<<nb(A.nf, 256), 256, 0, h->stream>>>(P, s.r, W.pf, A.nf);
     if (A.nw > 0)
-        k_adj_adami<T, ND><<<nb(A.nw, 128), 128, 0, h->stream>>>(
+        k_adj_adami<T, ND><<<nb((long)A.nw * kAdjLanes, 128), 128, 0, h->stream>>>(
             P, A.nw, (const double4_32a*)h->w_pos, L.wf, L.wfc, s, (const T*)W.pf, W.wp, W.wr,
             W.wnum, W.wvol);
     ADJ_LAUNCHED(h, "adjoint wall state");
@@ -1202,7 +1230,7 @@ tp_status forward_step(tp_handle* h, const AdjPhys<T>& P, double dt, AState<T> f
         S.Bd = kCK2N54_B[i];
         S.dtd = dt;
         S.first = i == 0;
-        k_adj_stage<T, ND><<<nb(A.nf, 128), 128, 0, h->stream>>>(
+        k_adj_stage<T, ND><<<nb((long)A.nf * kAdjLanes, 128), 128, 0, h->stream>>>(
             P, A.nf, src, dst, (const T*)W.pf, (const T*)A.mf, L.ff, L.ffc, L.fw, L.fwc,
             (const double4_32a*)h->w_pos, (const T*)W.wp, (const T*)W.wr, A.tx, (T*)A.tv,
             (T*)A.tr, S);
@@ -1359,11 +1387,12 @@ tp_status backward_impl(tp_handle* h, double* v_bar, double* u_bar, double* para
                 }
                 k_adj_seed<T, ND><<<nb(std::max(A.nf, A.nw), 256), 256, 0, h->stream>>>(
                     L, (T)kCK2N54_A[i], (T)kCK2N54_B[i], (T)A.dt, A.nf, A.nw);
-                k_adj_pair_vjp<T, ND><<<nb(A.nf, 128), 128, 0, h->stream>>>(
+                k_adj_pair_vjp<T, ND><<<nb((long)A.nf * kAdjLanes, 128), 128, 0, h->stream>>>(
                     P, A.nf, U, (const T*)W.pf, (const T*)A.mf, LS.ff, LS.ffc, LS.fw, LS.fwc,
                     (const double4_32a*)h->w_pos, (const T*)W.wp, (const T*)W.wr, L, A.theta);
                 if (A.nw > 0)
-                    k_adj_adami_vjp<T, ND><<<nb(A.nw, 128), 128, 0, h->stream>>>(
+                    k_adj_adami_vjp<T, ND><<<nb((long)A.nw * kAdjLanes, 128), 128, 0,
+                                             h->stream>>>(
                         P, A.nw, (const double4_32a*)h->w_pos, LS.wf, LS.wfc, U, (const T*)W.pf,
                         (const T*)W.wp, (const T*)W.wnum, (const T*)W.wvol, L, A.theta);
                 k_adj_eos_vjp<T><<<nb(A.nf, 256), 256, 0, h->stream>>>(P, U.r, L, A.nf);
