@@ -331,8 +331,9 @@ def cpu_baseline(semi, tank, cfg, v, u, state):
 
 
 def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
-    """Batching form: 512 seeded 2D dam breaks (FP32), three spacing groups as the branches of
-    one CUDA graph of `steps_per_replay` CK2N54 steps; autotuned launch shape and skin.
+    """Batching form: 512 seeded 2D dam breaks (FP32), three spacing groups in one CUDA graph of
+    `steps_per_replay` CK2N54 steps; autotuned launch shape and skin; both graph layouts (the
+    groups as parallel branches, one persistent pair launch per stage) timed, the faster kept.
     Aggregate particle-steps/s over all instances, plus the agreement of one instance per group
     with the same instance run alone."""
     e = pkg.ensemble
@@ -341,20 +342,37 @@ def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
     groups = e.build_ensemble(specs)
     setup_s = time.perf_counter() - t0
     tuned = e.autotune(groups, trial_steps=6)
-    eg = e.EnsembleGraph(groups, steps_per_replay)
-    eg.reset()
-    eg.replay()  # warm-up replay
-    torch.cuda.synchronize()
     reps = max(1, min(args.steps, 4))
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launch = torch.cuda.current_stream()  # CUDAGraph.replay launches on the current stream
-    ev0.record(launch)
-    for _ in range(reps):
-        eg.replay()
-    ev1.record(launch)
-    torch.cuda.synchronize()
-    eg.check()
-    ms = ev0.elapsed_time(ev1)
+
+    def time_graph(eg):
+        eg.reset()
+        eg.replay()  # warm-up replay
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launch = torch.cuda.current_stream()  # the batch graph launches on the current stream
+        ev0.record(launch)
+        for _ in range(reps):
+            eg.replay()
+        ev1.record(launch)
+        torch.cuda.synchronize()
+        eg.check()
+        return ev0.elapsed_time(ev1)
+
+    # both graph layouts of the same groups and tuning: the groups as parallel branches, and
+    # one persistent pair launch per stage for all groups (possible when every group runs the
+    # list pass); the faster one is the form's number
+    layouts = {}
+    eg = e.EnsembleGraph(groups, steps_per_replay)
+    layouts["branches"] = time_graph(eg)
+    if all(g.tuned["pair_mode"] == "lists" for g in groups):
+        eg.close()
+        eg = e.EnsembleGraph(groups, steps_per_replay, persistent=True)
+        layouts["persistent"] = time_graph(eg)
+        if layouts["persistent"] > layouts["branches"]:
+            eg.close()
+            eg = e.EnsembleGraph(groups, steps_per_replay)
+    best = "persistent" if eg.persistent else "branches"
+    ms = layouts[best]
     steps = reps * steps_per_replay
     n = eg.n_particles
     # agreement with the single-instance path after one replay from the initial state
@@ -384,7 +402,10 @@ def run_ensemble(pkg, torch, args, n_instances=512, seed=0, steps_per_replay=5):
                        f"dt = 5e-3 dx",
            "value": n * steps / (ms / 1e3), "unit": UNIT, "particles": n,
            "n_fluid": eg.n_fluid, "steps": steps, "ms_per_step": ms / steps,
-           "graph": f"{len(groups)} concurrent branches x {steps_per_replay} steps per replay",
+           "graph": (f"{len(groups)} groups x {steps_per_replay} steps per replay, "
+                     + ("one persistent pair launch per stage for all groups"
+                        if best == "persistent" else "the groups as concurrent branches")),
+           "ms_per_step_by_layout": {k: v / steps for k, v in layouts.items()},
            "autotuned": {str(k): v for k, v in tuned.items()},
            "per_instance_agreement": agree, "host_setup_s": round(setup_s, 2)}
     for g in groups:
@@ -673,7 +694,8 @@ def run_profile_ensemble(args, n_instances=512, seed=0, steps_per_replay=5):
     pkg.load_library()
     e = pkg.ensemble
     groups = e.build_ensemble(e.ensemble_specs(n_instances, seed))
-    eg = e.EnsembleGraph(groups, steps_per_replay)
+    eg = e.EnsembleGraph(groups, steps_per_replay,
+                         persistent=args.batch_layout == "persistent")
     eg.reset()
     eg.replay()
     torch.cuda.synchronize()
@@ -687,7 +709,8 @@ def run_profile_ensemble(args, n_instances=512, seed=0, steps_per_replay=5):
     eg.check()
     steps = max(1, args.steps) * steps_per_replay
     ms = ev0.elapsed_time(ev1)
-    print(json.dumps({"profile_ensemble": n_instances, "particles": eg.n_particles,
+    print(json.dumps({"profile_ensemble": n_instances, "layout": args.batch_layout,
+                      "particles": eg.n_particles,
                       "groups": [{"dx": gr.dx, "particles": gr.n_particles} for gr in groups],
                       "steps": steps, "ms_per_step": ms / steps,
                       "value": eg.n_particles * steps / (ms / 1e3)}), flush=True)
@@ -723,6 +746,9 @@ def main():
     ap.add_argument("--profile-ensemble", action="store_true",
                     help="profiling mode of the batching form: default launch shape, one warm-up "
                          "replay and --steps replays of the ensemble graph; used under ncu")
+    ap.add_argument("--batch-layout", default="branches", choices=["branches", "persistent"],
+                    help="graph layout of --profile-ensemble: the groups as parallel branches, "
+                         "or one persistent pair launch per stage for all groups")
     ap.add_argument("--pair-mode", type=int, default=None, choices=[0, 1, 2],
                     help="pair pass of --profile-form: 0 gather (lists), 1 symmetric (FP64), "
                          "2 tiled (FP32)")

@@ -391,6 +391,17 @@ tp_status tp_batch_capture(tp_batch* b, int64_t steps, double growth);
 tp_status tp_batch_launch(tp_batch* b, void* stream);
 tp_status tp_batch_sync(tp_batch* b);
 int64_t tp_batch_steps(const tp_batch* b);
+/*
+ * How tp_batch_capture records the members (no counterpart in the reference).
+ * TP_BATCH_BRANCHES (default): every member's fused integrator is one parallel branch of the
+ * graph.  TP_BATCH_PERSISTENT (FP32 members on neighbour lists, at most 6, one ndims and model
+ * setup): the members' neighbour search, pack and Adami passes stay parallel branches, and the
+ * pair stage of all members is one persistent launch per Runge-Kutta stage whose blocks take
+ * 256-slot tiles of the members (largest member first) from a work counter.  Results equal the
+ * branches mode bit for bit.  A mode change drops the captured graph.
+ */
+enum { TP_BATCH_BRANCHES = 0, TP_BATCH_PERSISTENT = 1 };
+tp_status tp_batch_set_mode(tp_batch* b, int32_t mode);
 const char* tp_batch_last_error(const tp_batch* b);
 
 /* Last error message of the handle (or of the last failed tp_create when h is NULL). */

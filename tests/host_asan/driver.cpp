@@ -118,6 +118,23 @@ static int run(int nd, int precision) {
     bad |= tp_batch_launch(b, nullptr) != TP_OK;
     bad |= tp_batch_launch(b, nullptr) != TP_OK;
     bad |= tp_batch_sync(b) != TP_OK;
+    // persistent mode: FP32 members on neighbour lists only
+    bad |= tp_batch_set_mode(b, 7) != TP_ERR_ARGUMENT;
+    bad |= tp_batch_set_mode(b, TP_BATCH_PERSISTENT) != TP_OK;
+    bad |= tp_batch_steps(b) != 0;  // a mode change drops the graph
+    {
+        const tp_status want = precision == TP_PRECISION_FP32 && mode == TP_PAIR_GATHER
+                                   ? TP_OK
+                                   : TP_ERR_UNSUPPORTED;
+        bad |= tp_batch_capture(b, 2, 1.5) != want;
+        if (want == TP_OK) {
+            bad |= tp_batch_steps(b) != 2;
+            bad |= tp_batch_launch(b, nullptr) != TP_OK;
+            bad |= tp_batch_sync(b) != TP_OK;
+        }
+    }
+    bad |= tp_batch_set_mode(b, TP_BATCH_BRANCHES) != TP_OK;
+    bad |= tp_batch_capture(b, 1, 1.5) != TP_OK;
     bad |= tp_batch_destroy(b) != TP_OK;
     tp_config back;
     bad |= tp_get_config(h, &back) != TP_OK;

@@ -38,6 +38,8 @@ cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t, cudaEvent_t) { *ms = 0;
 cudaError_t cudaGetDevice(int* d) { *d = 0; return cudaSuccess; }
 cudaError_t cudaMemGetInfo(size_t* f, size_t* t) { *f = (size_t)1 << 34; *t = (size_t)1 << 35; return cudaSuccess; }
 cudaError_t cudaGetSymbolAddress(void** p, const void* s) { *p = (void*)s; return cudaSuccess; }
+cudaError_t cudaDeviceGetAttribute(int* v, cudaDeviceAttr, int) { *v = 1; return cudaSuccess; }
+cudaError_t cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(int* n, const void*, int, size_t, unsigned) { *n = 1; return cudaSuccess; }
 cudaError_t cudaLaunchKernel(const void*, dim3, dim3, void**, size_t, cudaStream_t) { return cudaSuccess; }
 unsigned __cudaPushCallConfiguration(dim3, dim3, size_t, void*) { return 0; }
 cudaError_t __cudaPopCallConfiguration(dim3*, dim3*, size_t*, void*) { return cudaSuccess; }

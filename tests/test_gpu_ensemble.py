@@ -124,3 +124,41 @@ def test_autotune_choice_keeps_results(pkg, cuda):
         for j in range(len(g.instances)):
             _close(e.instance_state(g, j), r[j])
         g.semi.close()
+
+
+def test_persistent_batch_equals_branches(pkg, cuda):
+    """The persistent capture (one pair launch per stage for every group, a work queue of
+    256-slot tiles) runs the same per-slot list pass as the branch capture: equal bit for bit."""
+    e = pkg.ensemble
+    specs = _specs(pkg)
+    runs = []
+    for persistent in (False, True):
+        groups = e.build_ensemble(specs)
+        eg = e.EnsembleGraph(groups, K, persistent=persistent)
+        eg.reset()
+        eg.replay()
+        cuda.cuda.synchronize()
+        eg.check()
+        runs.append([(g.v.cpu().numpy(), g.u.cpu().numpy()) for g in groups])
+        eg.close()
+        for g in groups:
+            g.semi.close()
+    for (vb, ub), (vp, up) in zip(*runs):
+        assert np.array_equal(vb, vp)
+        assert np.array_equal(ub, up)
+
+
+def test_persistent_mode_rejects_tiled_members(pkg, cuda):
+    e = pkg.ensemble
+    _abi = pkg._abi
+    groups = e.build_ensemble(_specs(pkg, n=3, seed=5))
+    b = e.Batch(groups)  # binds the handles
+    groups[0].semi._call("tp_set_pair_mode", _abi.TP_PAIR_TILED)
+    b.set_mode(True)
+    with pytest.raises(_abi.TpError):
+        b.capture(2)
+    b.set_mode(False)
+    b.capture(2)
+    b.close()
+    for g in groups:
+        g.semi.close()

@@ -123,6 +123,7 @@ PROTOTYPES = [
      [c_void_p, c_int32, POINTER(c_int32), POINTER(c_double), POINTER(c_int32),
       POINTER(c_double)]),
     ("tp_batch_capture", c_int32, [c_void_p, c_int64, c_double]),
+    ("tp_batch_set_mode", c_int32, [c_void_p, c_int32]),
     ("tp_batch_launch", c_int32, [c_void_p, c_void_p]),
     ("tp_batch_sync", c_int32, [c_void_p]),
     ("tp_batch_steps", c_int64, [c_void_p]),
@@ -133,6 +134,8 @@ PROTOTYPES = [
 TP_PAIR_GATHER = 0
 TP_PAIR_SYMMETRIC = 1
 TP_PAIR_TILED = 2
+TP_BATCH_BRANCHES = 0
+TP_BATCH_PERSISTENT = 1
 TP_NOALLOC_MAX_PARTICLES = 262144
 TP_NOALLOC_MAX_CELLS = 524288
 

@@ -1089,16 +1089,20 @@ tp_status tp_drift(tp_handle* h, double* du_ode, const double* v_ode, const doub
     return TP_OK;
 }
 
-tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double t0, double dt,
-                              int64_t n_steps) {
-    (void)t0;
-    tp_status st = ready(h);
-    if (st != TP_OK) return st;
-    if (n_steps < 0 || !std::isfinite(dt))
-        return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: bad step count or dt");
+}  // extern "C"
+
+namespace tp {
+
+// ---- the fused integrator in pieces (tp_integrate_ck2n54; the batching form's persistent
+// capture interleaves the members' stages around one pair launch) ----
+
+// Everything before the first stage: capture checks, state and lists, the caller state loaded
+// into slot order, the rebuild gate.  `capturing` receives whether the stream is being captured.
+tp_status integrator_begin(tp_handle* h, double* v_ode, double* u_ode, int64_t n_steps,
+                           bool* capturing) {
+    (void)n_steps;
+    tp_status st = TP_OK;
     const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
-    if (nf == 0 || n_steps == 0) return TP_OK;
-    if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: null array");
     // Under stream capture nothing may synchronise or allocate: list capacities and the
     // integrator state must have been set up by tp_prepare_lists, and timing must be off.
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1169,60 +1173,92 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     TP_LAUNCHED(h, "gate init");
     h->launches += 1;
 
-    for (int64_t step = 0; step < n_steps; ++step) {
-        for (int stage = 0; stage < 5; ++stage) {
-            PhysState& src = h->st[h->cur];
-            PhysState& dst = h->st[1 - h->cur];
-            mark(h, 0);
-            // displacement since the last rebuild (slot order of src = order of x_build): at the
-            // first stage of the call a pass over the loaded state; later the previous pair
-            // stage has collected it from the positions it wrote (gate[3]), and the advance
-            // also consumes the forced flag (the pair kernels read gate[0..2] to know whether
-            // this stage moved the state, so none writes them)
-            if (step + stage == 0) {
-                if (nd == 2)
-                    k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build,
-                                                                             nf, h->gate);
-                else
-                    k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build,
-                                                                             nf, h->gate);
-            } else {
-                k_gate_advance<<<1, 32, 0, h->stream>>>(h->gate);
-            }
-            h->launches += 1;
-            TP_DBG(h, "displacement");
-            st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);
-            if (st != TP_OK) return st;
-            if (f32)
-                fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst, h->gate);
-            else
-                fp64_pack(h, src.u, (const double*)src.v, (const double*)src.m, &src, &dst,
-                          h->gate);
-            TP_LAUNCHED(h, "pack");
-            h->launches += 1;
-            TP_DBG(h, "pack");
-            st = build_lists(h, h->skin, h->gate);
-            if (st != TP_OK) return st;
-            mark(h, 1);
-            if (f32)
-                fp32_adami(h);
-            else
-                fp64_adami(h);
-            TP_LAUNCHED(h, "adami");
-            TP_DBG(h, "adami");
-            mark(h, 2);
-            if (f32)
-                fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0);
-            else
-                fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
-            TP_LAUNCHED(h, "pair stage");
-            TP_DBG(h, "pair stage");
-            mark(h, 3);
-            h->launches += 1 + (h->cfg.n_wall > 0);
-            h->cur = 1 - h->cur;
-        }
-    }
+    *capturing = cap != cudaStreamCaptureStatusNone;
+    return TP_OK;
+}
 
+// The stage's displacement check, neighbour search (gated), pack, lists (gated) and Adami pass.
+tp_status integrator_stage_pre(tp_handle* h, int64_t step, int stage) {
+    tp_status st = TP_OK;
+    const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    PhysState& src = h->st[h->cur];
+    PhysState& dst = h->st[1 - h->cur];
+    mark(h, 0);
+    // displacement since the last rebuild (slot order of src = order of x_build): at the
+    // first stage of the call a pass over the loaded state; later the previous pair
+    // stage has collected it from the positions it wrote (gate[3]), and the advance
+    // also consumes the forced flag (the pair kernels read gate[0..2] to know whether
+    // this stage moved the state, so none writes them)
+    if (step + stage == 0) {
+        if (nd == 2)
+            k_displacement<2><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build,
+                                                                     nf, h->gate);
+        else
+            k_displacement<3><<<nblk(nf, 256), 256, 0, h->stream>>>(src.u, h->x_build,
+                                                                     nf, h->gate);
+    } else {
+        k_gate_advance<<<1, 32, 0, h->stream>>>(h->gate);
+    }
+    h->launches += 1;
+    TP_DBG(h, "displacement");
+    st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);
+    if (st != TP_OK) return st;
+    if (f32)
+        fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst, h->gate);
+    else
+        fp64_pack(h, src.u, (const double*)src.v, (const double*)src.m, &src, &dst,
+                  h->gate);
+    TP_LAUNCHED(h, "pack");
+    h->launches += 1;
+    TP_DBG(h, "pack");
+    st = build_lists(h, h->skin, h->gate);
+    if (st != TP_OK) return st;
+    mark(h, 1);
+    if (f32)
+        fp32_adami(h);
+    else
+        fp64_adami(h);
+    TP_LAUNCHED(h, "adami");
+    TP_DBG(h, "adami");
+    mark(h, 2);
+    return TP_OK;
+}
+
+// The stage's pair pass with the fused CK2N54 update; with `desc` (FP32 form) the pass is not
+// launched and desc receives it for the batched persistent pass.
+tp_status integrator_stage_pair(tp_handle* h, int stage, double dt, Pair32Member* desc) {
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    PhysState& src = h->st[h->cur];
+    PhysState& dst = h->st[1 - h->cur];
+    if (desc) {
+        if (!f32) return fail(h, TP_ERR_UNSUPPORTED, "the persistent pair pass is FP32 only");
+        fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0, desc);
+        return TP_OK;
+    }
+    if (f32)
+        fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0);
+    else
+        fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
+    return TP_OK;
+}
+
+// After the stage's pair pass: bookkeeping and the swap of the ping-pong states.
+tp_status integrator_stage_post(tp_handle* h) {
+    TP_LAUNCHED(h, "pair stage");
+    TP_DBG(h, "pair stage");
+    mark(h, 3);
+    h->launches += 1 + (h->cfg.n_wall > 0);
+    h->cur = 1 - h->cur;
+    return TP_OK;
+}
+
+// After the last stage: the final state back to caller order.
+tp_status integrator_end(tp_handle* h, double* v_ode, double* u_ode, bool capturing) {
+    const int nf = (int)h->cfg.n_fluid, nd = h->cfg.ndims;
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    const cudaStreamCaptureStatus cap =
+        capturing ? cudaStreamCaptureStatusActive : cudaStreamCaptureStatusNone;
     PhysState& sf = h->st[h->cur];
     const double rho0 = h->cfg.reference_density;
     if (nd == 2) {
@@ -1248,6 +1284,34 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     h->records_order = 2;  // records of the last stage, in the order of the final state
     finish_timing(h);
     return TP_OK;
+}
+
+}  // namespace tp
+
+extern "C" {
+
+tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double t0, double dt,
+                              int64_t n_steps) {
+    (void)t0;
+    tp_status st = ready(h);
+    if (st != TP_OK) return st;
+    if (n_steps < 0 || !std::isfinite(dt))
+        return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: bad step count or dt");
+    const int nf = (int)h->cfg.n_fluid;
+    if (nf == 0 || n_steps == 0) return TP_OK;
+    if (!v_ode || !u_ode) return fail(h, TP_ERR_ARGUMENT, "tp_integrate_ck2n54: null array");
+    bool capturing = false;
+    st = integrator_begin(h, v_ode, u_ode, n_steps, &capturing);
+    if (st != TP_OK) return st;
+    for (int64_t step = 0; step < n_steps; ++step) {
+        for (int stage = 0; stage < 5; ++stage) {
+            st = integrator_stage_pre(h, step, stage);
+            if (st == TP_OK) st = integrator_stage_pair(h, stage, dt, nullptr);
+            if (st == TP_OK) st = integrator_stage_post(h);
+            if (st != TP_OK) return st;
+        }
+    }
+    return integrator_end(h, v_ode, u_ode, capturing);
 }
 
 tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid) {

@@ -25,9 +25,24 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
 void fp32_init_wall_state(tp_handle* h);
 void fp32_adami(tp_handle* h);
 void fp32_pair_kick(tp_handle* h, double* dv);
-// src: the stage's source state (read in place when the stage did not rebuild); st: destination
+// src: the stage's source state (read in place when the stage did not rebuild); st: destination.
+// With `desc` the pass is not launched: desc receives what the batched persistent pass needs.
 void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
-                     double dt, int first);
+                     double dt, int first, Pair32Member* desc = nullptr);
+// The batched persistent FP32 pair pass over B's members (same ndims and model switches).
+bool fp32_batch_pair_std(const Phys32& P);
+tp_status fp32_batch_pair(const Pair32Batch& B, int nd, bool std_cfg, unsigned* counter,
+                          cudaStream_t stream);
+
+// The fused integrator in pieces (tp_api.cu): tp_integrate_ck2n54 is begin, then per stage
+// pre / pair / post, then end; the batching form's persistent capture interleaves its members'
+// stages around one pair launch.
+tp_status integrator_begin(tp_handle* h, double* v_ode, double* u_ode, int64_t n_steps,
+                           bool* capturing);
+tp_status integrator_stage_pre(tp_handle* h, int64_t step, int stage);
+tp_status integrator_stage_pair(tp_handle* h, int stage, double dt, Pair32Member* desc);
+tp_status integrator_stage_post(tp_handle* h);
+tp_status integrator_end(tp_handle* h, double* v_ode, double* u_ode, bool capturing);
 
 // API layer services used by the differentiation form (tp_api.cu)
 tp_status api_fail(tp_handle* h, tp_status st, const std::string& msg);

@@ -9,6 +9,13 @@
 // caller stream.  tp_batch_autotune times trial steps of every member on scratch copies of its
 // state over the pair pass (neighbour lists or, in the FP32 form, cell tiles staged in shared
 // memory) x neighbour-list skins x pair-kernel block sizes and keeps the fastest combination.
+//
+// Persistent mode (tp_batch_set_mode(b, TP_BATCH_PERSISTENT), FP32 members on neighbour lists):
+// the graph keeps the members' neighbour search, pack and Adami passes as parallel branches but
+// joins them before every pair stage, which is one persistent launch for all members: about as
+// many blocks as fit on the GPU take work items (a 256-slot tile of one member, the largest
+// member first) from a counter until all members' slots are done.
+#include <algorithm>
 #include <cmath>
 #include <new>
 #include <string>
@@ -36,10 +43,14 @@ struct tp_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long steps = 0;
+    int mode = TP_BATCH_BRANCHES;
+    unsigned* counter = nullptr;  // work-item counter of the persistent pair pass (device)
     std::string last_error;
 };
 
 namespace {
+
+using namespace tp;
 
 tp_status bfail(tp_batch* b, tp_status st, const std::string& msg) {
     if (b) b->last_error = msg;
@@ -64,6 +75,95 @@ void drop_graph(tp_batch* b) {
     b->exec = nullptr;
     b->graph = nullptr;
     b->steps = 0;
+}
+
+// The members' stages interleaved around one persistent pair launch per stage (see the file
+// comment); called between cudaStreamBeginCapture and cudaStreamEndCapture on b->main.
+tp_status record_persistent(tp_batch* b, int64_t steps) {
+    const size_t n = b->m.size();
+    std::vector<size_t> order(n);
+    for (size_t k = 0; k < n; ++k) order[k] = k;
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+        tp_config cx{}, cy{};
+        tp_get_config(b->m[x].h, &cx);
+        tp_get_config(b->m[y].h, &cy);
+        return cx.n_fluid > cy.n_fluid;
+    });
+    tp_config c0{};
+    tp_get_config(b->m[0].h, &c0);
+    B_CUDA(b, cudaEventRecord(b->fork, b->main));
+    std::vector<char> capturing(n, 0);
+    for (size_t k = 0; k < n; ++k) {
+        tp_batch::Member& mb = b->m[k];
+        B_CUDA(b, cudaStreamWaitEvent(mb.stream, b->fork, 0));
+        bool cap = false;
+        tp_status st = integrator_begin(mb.h, mb.v, mb.u, steps, &cap);
+        if (st != TP_OK) return member_fail(b, k, st);
+        capturing[k] = cap;
+    }
+    bool std_cfg = true;
+    for (int64_t step = 0; step < steps; ++step) {
+        for (int stage = 0; stage < 5; ++stage) {
+            for (size_t k = 0; k < n; ++k) {
+                tp_batch::Member& mb = b->m[k];
+                tp_status st = integrator_stage_pre(mb.h, step, stage);
+                if (st != TP_OK) return member_fail(b, k, st);
+                B_CUDA(b, cudaEventRecord(mb.join, mb.stream));
+                B_CUDA(b, cudaStreamWaitEvent(b->main, mb.join, 0));
+            }
+            Pair32Batch B{};
+            B.n = (int)n;
+            int tiles = 0;
+            for (size_t r = 0; r < n; ++r) {
+                const size_t k = order[r];
+                tp_status st = integrator_stage_pair(b->m[k].h, stage, b->m[k].dt, &B.m[r]);
+                if (st != TP_OK) return member_fail(b, k, st);
+                B.tile0[r] = tiles;
+                tiles += (B.m[r].nf + kBatchTile - 1) / kBatchTile;
+                std_cfg = std_cfg && fp32_batch_pair_std(B.m[r].P);
+            }
+            B.tile0[n] = tiles;
+            if (fp32_batch_pair(B, c0.ndims, std_cfg, b->counter, b->main) != TP_OK)
+                return bfail(b, TP_ERR_CUDA, "tp_batch_capture: persistent pair launch failed");
+            B_CUDA(b, cudaEventRecord(b->fork, b->main));
+            for (size_t k = 0; k < n; ++k) {
+                tp_batch::Member& mb = b->m[k];
+                B_CUDA(b, cudaStreamWaitEvent(mb.stream, b->fork, 0));
+                tp_status st = integrator_stage_post(mb.h);
+                if (st != TP_OK) return member_fail(b, k, st);
+            }
+        }
+    }
+    for (size_t k = 0; k < n; ++k) {
+        tp_batch::Member& mb = b->m[k];
+        tp_status st = integrator_end(mb.h, mb.v, mb.u, capturing[k] != 0);
+        if (st != TP_OK) return member_fail(b, k, st);
+        B_CUDA(b, cudaEventRecord(mb.join, mb.stream));
+        B_CUDA(b, cudaStreamWaitEvent(b->main, mb.join, 0));
+    }
+    return TP_OK;
+}
+
+// Persistent mode needs FP32 members on neighbour lists with one ndims and one model setup.
+tp_status check_persistent(tp_batch* b) {
+    if (b->m.size() > (size_t)kBatchMaxMembers)
+        return bfail(b, TP_ERR_UNSUPPORTED, "persistent mode: at most " +
+                                                std::to_string(kBatchMaxMembers) + " members");
+    tp_config c0{};
+    tp_get_config(b->m[0].h, &c0);
+    for (size_t k = 0; k < b->m.size(); ++k) {
+        tp_config c{};
+        tp_get_config(b->m[k].h, &c);
+        if (c.precision != TP_PRECISION_FP32 || b->m[k].h->pair_mode != TP_PAIR_GATHER)
+            return bfail(b, TP_ERR_UNSUPPORTED,
+                         "persistent mode: every member must be an FP32 handle on neighbour lists");
+        if (c.ndims != c0.ndims || c.viscosity_model != c0.viscosity_model ||
+            c.density_diffusion_model != c0.density_diffusion_model ||
+            (c.viscosity_beta == 0.0) != (c0.viscosity_beta == 0.0))
+            return bfail(b, TP_ERR_UNSUPPORTED,
+                         "persistent mode: members must share ndims and the model switches");
+    }
+    return TP_OK;
 }
 
 // Scratch copies of a member's state (autotuning and warm-up never touch the caller's state).
@@ -113,6 +213,7 @@ tp_status tp_batch_create(tp_handle* const* handles, int32_t n, tp_batch** out) 
     }
     cudaError_t e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(unsigned));
     for (auto& mb : b->m) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mb.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&mb.join, cudaEventDisableTiming);
@@ -139,6 +240,7 @@ tp_status tp_batch_destroy(tp_batch* b) {
     }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->main) cudaStreamDestroy(b->main);
+    if (b->counter) cudaFree(b->counter);
     delete b;
     return TP_OK;
 }
@@ -244,6 +346,10 @@ tp_status tp_batch_capture(tp_batch* b, int64_t steps, double growth) {
     if (!b) return TP_ERR_ARGUMENT;
     if (steps <= 0) return bfail(b, TP_ERR_ARGUMENT, "tp_batch_capture: steps <= 0");
     drop_graph(b);
+    if (b->mode == TP_BATCH_PERSISTENT) {
+        tp_status pr = check_persistent(b);
+        if (pr != TP_OK) return pr;
+    }
     // fixed list capacities, integrator state and a warm-up step (on scratch) per member
     for (size_t k = 0; k < b->m.size(); ++k) {
         tp_batch::Member& mb = b->m[k];
@@ -259,6 +365,23 @@ tp_status tp_batch_capture(tp_batch* b, int64_t steps, double growth) {
         if (st != TP_OK) return member_fail(b, k, st);
     }
     B_CUDA(b, cudaDeviceSynchronize());
+    if (b->mode == TP_BATCH_PERSISTENT) {
+        B_CUDA(b, cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+        tp_status pr = record_persistent(b, steps);
+        cudaGraph_t g = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(b->main, &g);
+        if (pr != TP_OK || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (pr != TP_OK) return pr;
+            return bfail(b, TP_ERR_CUDA, std::string("tp_batch_capture: ") +
+                                             cudaGetErrorString(ee));
+        }
+        b->graph = g;
+        B_CUDA(b, cudaGraphInstantiate(&b->exec, b->graph, 0));
+        b->steps = steps;
+        return TP_OK;
+    }
     B_CUDA(b, cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
     tp_status result = TP_OK;
     cudaError_t ce = cudaEventRecord(b->fork, b->main);
@@ -307,6 +430,16 @@ tp_status tp_batch_sync(tp_batch* b) {
 }
 
 int64_t tp_batch_steps(const tp_batch* b) { return b ? (int64_t)b->steps : 0; }
+
+tp_status tp_batch_set_mode(tp_batch* b, int32_t mode) {
+    if (!b) return TP_ERR_ARGUMENT;
+    if (mode != TP_BATCH_BRANCHES && mode != TP_BATCH_PERSISTENT)
+        return bfail(b, TP_ERR_ARGUMENT,
+                     "tp_batch_set_mode: mode must be TP_BATCH_BRANCHES or TP_BATCH_PERSISTENT");
+    if (mode != b->mode) drop_graph(b);
+    b->mode = mode;
+    return TP_OK;
+}
 
 const char* tp_batch_last_error(const tp_batch* b) {
     return b ? b->last_error.c_str() : "null batch";

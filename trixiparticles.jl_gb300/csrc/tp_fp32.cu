@@ -206,28 +206,6 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __res
     wvol[w] = (double)vw;
 }
 
-struct Update32 {
-    double* dv;       // kick: dv_ode (caller order, FP64) indexed by perm
-    const int* perm;
-    double g[3];
-    // integrator (slot order): the destination state; the pass reads the positions and
-    // registers from it when this stage's pack moved the state there (a rebuild), else from the
-    // source state in place
-    double* u;
-    double* tu;
-    float4* v_out;
-    float4* tv;
-    const double* u_in;
-    const double* tu_in;
-    const float4* tv_in;
-    // displacement check of the next stage (optional): positions of the last rebuild (slot
-    // order) and the gate word that collects the largest squared displacement
-    const double* xb;
-    unsigned* gate_next;
-    double A, B, dt;
-    float Af, Bf, dtf;
-    int first;
-};
 
 // Stage update of one fluid slot from its compensated sums: the kick! path writes dv (gravity
 // added) in caller order; the integrator applies the fused CK2N54 register update (FP32
@@ -383,20 +361,21 @@ __device__ __forceinline__ void fw_pair32(const Phys32& P, float4 ta, float4 va,
     fw_terms32<ND>(P, va, p_a, rho_a, ia, pd0, pd1, pd2, d2, tb.w, wpres[e & kSlotMask], q);
 }
 
+// One fluid slot s of the list pass (a thread's whole work; shared by the per-handle kernel and
+// the batched persistent pass).
 template <int ND, bool INTEGRATE, bool STD>
-__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
-                                                const float4* __restrict__ ftest,
-                                                const float4* __restrict__ fvel,
-                                                const float* __restrict__ fpres,
-                                                const float4* __restrict__ frec,
-                                                const unsigned* __restrict__ ff,
-                                                const int* __restrict__ ffc,
-                                                const unsigned* __restrict__ fw,
-                                                const int* __restrict__ fwc,
-                                                const float4* __restrict__ wtest,
-                                                const float* __restrict__ wpres,
-                                                unsigned* __restrict__ gate, Update32 U) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
+                                            const float4* __restrict__ ftest,
+                                            const float4* __restrict__ fvel,
+                                            const float* __restrict__ fpres,
+                                            const float4* __restrict__ frec,
+                                            const unsigned* __restrict__ ff,
+                                            const int* __restrict__ ffc,
+                                            const unsigned* __restrict__ fw,
+                                            const int* __restrict__ fwc,
+                                            const float4* __restrict__ wtest,
+                                            const float* __restrict__ wpres,
+                                            unsigned* __restrict__ gate, const Update32& U) {
     if (s >= nf) return;
     const float4 ta = ftest[s];  // {offsets, rho - rho0}
     const float4 va = fvel[s];   // {v, m / rho}
@@ -455,6 +434,47 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
     }
 
     pair32_finish<ND, INTEGRATE>(U, s, va, drho_a, a0, a1, a2, ar, gate);
+}
+
+template <int ND, bool INTEGRATE, bool STD>
+__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
+                                                const float4* __restrict__ ftest,
+                                                const float4* __restrict__ fvel,
+                                                const float* __restrict__ fpres,
+                                                const float4* __restrict__ frec,
+                                                const unsigned* __restrict__ ff,
+                                                const int* __restrict__ ffc,
+                                                const unsigned* __restrict__ fw,
+                                                const int* __restrict__ fwc,
+                                                const float4* __restrict__ wtest,
+                                                const float* __restrict__ wpres,
+                                                unsigned* __restrict__ gate, Update32 U) {
+    pair32_slot<ND, INTEGRATE, STD>(P, blockIdx.x * blockDim.x + threadIdx.x, nf, ftest, fvel,
+                                    fpres, frec, ff, ffc, fw, fwc, wtest, wpres,
+                                    gate, U);
+}
+
+// Batched persistent pair pass: one launch advances the pair stage of every member of a batch.
+// The launch keeps about as many blocks as fit on the GPU; each block takes work items -- a tile
+// of kBatchTile consecutive slots of one member, the largest member's tiles first -- from a
+// counter in global memory (atomicAdd) until none is left, and runs the list pass on them.
+template <int ND, bool STD>
+__global__ void __launch_bounds__(kBatchTile, 5) k_batch_pair32(const __grid_constant__ Pair32Batch B,
+                                                                 unsigned* __restrict__ counter) {
+    __shared__ int item;
+    for (;;) {
+        __syncthreads();  // every thread has read the previous item
+        if (threadIdx.x == 0) item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = item;
+        if (it >= B.tile0[B.n]) return;
+        int m = 0;
+        while (m + 1 < B.n && it >= B.tile0[m + 1]) ++m;
+        const Pair32Member& M = B.m[m];
+        const int s = (it - B.tile0[m]) * kBatchTile + threadIdx.x;
+        pair32_slot<ND, true, STD>(M.P, s, M.nf, M.ftest, M.fvel, M.fpres, M.frec, M.ff, M.ffc,
+                                   M.fw, M.fwc, M.wtest, M.wpres, M.gate, M.U);
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -769,8 +789,8 @@ void fp32_pair_kick(tp_handle* h, double* dv) {
 }
 
 void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
-                     double dt, int first) {
-    if (h->cfg.n_fluid == 0) return;
+                     double dt, int first, Pair32Member* desc) {
+    if (h->cfg.n_fluid == 0 && !desc) return;
     Update32 U{};
     U.perm = h->f_perm;
     for (int d = 0; d < 3; ++d) U.g[d] = h->cfg.acceleration[d];
@@ -790,10 +810,56 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
     U.Bf = (float)B;
     U.dtf = (float)dt;
     U.first = first;
+    if (desc) {  // the batched persistent pass launches it (fp32_batch_pair)
+        Pair32Member& M = *desc;
+        M.P = h->phys32;
+        M.nf = (int)h->cfg.n_fluid;
+        M.ftest = h->f_test;
+        M.fvel = (const float4*)h->f_vel;
+        M.fpres = (const float*)h->f_aux;
+        M.frec = (const float4*)h->f_rec;
+        M.ff = h->l_ff;
+        M.ffc = h->c_ff;
+        M.fw = h->l_fw;
+        M.fwc = h->c_fw;
+        M.wtest = h->w_test;
+        M.wpres = h->w_p32;
+        M.gate = h->gate;
+        M.U = U;
+        return;
+    }
     if (h->cfg.ndims == 2)
         launch_pair32<2, true>(h, h->gate, U);
     else
         launch_pair32<3, true>(h, h->gate, U);
+}
+
+bool fp32_batch_pair_std(const Phys32& P) { return P.visc && P.beta == 0.0f && P.diff; }
+
+tp_status fp32_batch_pair(const Pair32Batch& B, int nd, bool std_cfg, unsigned* counter,
+                          cudaStream_t stream) {
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto run = [&](auto ndc, auto stdc) {
+        constexpr int ND = decltype(ndc)::value;
+        constexpr bool S = decltype(stdc)::value;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_pair32<ND, S>,
+                                                              kBatchTile, 0);
+        const int blocks = std::max(1, std::min(B.tile0[B.n], std::max(per_sm, 1) * sms));
+        if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned), stream);
+        if (e == cudaSuccess) k_batch_pair32<ND, S><<<blocks, kBatchTile, 0, stream>>>(B, counter);
+    };
+    if (nd == 2) {
+        if (std_cfg) run(std::integral_constant<int, 2>{}, std::true_type{});
+        else run(std::integral_constant<int, 2>{}, std::false_type{});
+    } else {
+        if (std_cfg) run(std::integral_constant<int, 3>{}, std::true_type{});
+        else run(std::integral_constant<int, 3>{}, std::false_type{});
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e == cudaSuccess ? TP_OK : TP_ERR_CUDA;
 }
 
 }  // namespace tp

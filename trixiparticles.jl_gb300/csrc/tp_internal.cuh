@@ -91,6 +91,58 @@ struct Phys32 {
     float inv_rho0;
 };
 
+// Stage update of the FP32 pair pass (kick! output or fused CK2N54 register update).
+struct Update32 {
+    double* dv;       // kick: dv_ode (caller order, FP64) indexed by perm
+    const int* perm;
+    double g[3];
+    // integrator (slot order): the destination state; the pass reads the positions and
+    // registers from it when this stage's pack moved the state there (a rebuild), else from the
+    // source state in place
+    double* u;
+    double* tu;
+    float4* v_out;
+    float4* tv;
+    const double* u_in;
+    const double* tu_in;
+    const float4* tv_in;
+    // displacement check of the next stage (optional): positions of the last rebuild (slot
+    // order) and the gate word that collects the largest squared displacement
+    const double* xb;
+    unsigned* gate_next;
+    double A, B, dt;
+    float Af, Bf, dtf;
+    int first;
+};
+
+// One member of the batched persistent FP32 pair pass: everything its list pass reads.
+struct Pair32Member {
+    Phys32 P;
+    int nf;
+    const float4* ftest;
+    const float4* fvel;
+    const float* fpres;
+    const float4* frec;
+    const unsigned* ff;
+    const int* ffc;
+    const unsigned* fw;
+    const int* fwc;
+    const float4* wtest;
+    const float* wpres;
+    unsigned* gate;
+    Update32 U;
+};
+
+constexpr int kBatchMaxMembers = 6;
+constexpr int kBatchTile = 256;  // slots per work item of the persistent pass (one per thread)
+
+// Kernel parameter of the persistent pass (passed by value, read in place as __grid_constant__).
+struct Pair32Batch {
+    Pair32Member m[kBatchMaxMembers];
+    int tile0[kBatchMaxMembers + 1];  // first work item of each member; tile0[n] = total
+    int n;
+};
+
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

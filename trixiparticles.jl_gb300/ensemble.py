@@ -191,6 +191,12 @@ class Batch:
             out[g.dx] = g.tuned
         return out
 
+    def set_mode(self, persistent: bool) -> None:
+        """Graph layout of the next capture: the groups as parallel branches (default), or one
+        persistent pair launch per stage for all groups (FP32 groups on neighbour lists)."""
+        self._check(self.lib.tp_batch_set_mode(
+            self._b, _abi.TP_BATCH_PERSISTENT if persistent else _abi.TP_BATCH_BRANCHES))
+
     def capture(self, steps: int, growth: float = 1.5) -> None:
         self._check(self.lib.tp_batch_capture(self._b, ctypes.c_int64(steps),
                                               ctypes.c_double(growth)))
@@ -230,12 +236,19 @@ def autotune(groups: list[Group], trial_steps: int = 3) -> dict:
 class EnsembleGraph:
     """K CarpenterKennedy2N54 steps of every group as one CUDA graph (tp_batch_capture): one
     branch per spacing group (the groups run concurrently), each branch the group's fused
-    integrator (neighbour-list upkeep, Adami, pair kernel with the stage update)."""
+    integrator (neighbour-list upkeep, Adami, pair kernel with the stage update).  With
+    `persistent`, the groups' pair passes of a stage are one persistent launch over all groups
+    (a work queue of 256-slot tiles) between the branches' neighbour-list upkeep and their
+    next stage."""
 
-    def __init__(self, groups: list[Group], steps_per_replay: int, growth: float = 1.5):
+    def __init__(self, groups: list[Group], steps_per_replay: int, growth: float = 1.5,
+                 persistent: bool = False):
         self.groups = groups
         self.k = steps_per_replay
+        self.persistent = persistent
         self.batch = Batch(groups)
+        if persistent:
+            self.batch.set_mode(True)
         self.batch.capture(steps_per_replay, growth)
 
     @property

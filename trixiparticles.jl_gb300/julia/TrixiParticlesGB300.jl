@@ -312,7 +312,9 @@ end
 
 # ---- Batching form: several Semidiscretizations per CUDA-graph launch ----------------------
 # members: Vector of (semi, v::CuArray, u::CuArray, dt).  Returns the batch pointer.
-function batch_create(members; steps=5, autotune=true, growth=1.5)
+# persistent=true: one work-queue pair launch per stage for all members (FP32 members on
+# neighbour lists); the default records the members as parallel graph branches.
+function batch_create(members; steps=5, autotune=true, growth=1.5, persistent=false)
     hds = [handle(m[1]) for m in members]
     hs = [hd.ptr for hd in hds]
     b = Ref{Ptr{Cvoid}}(C_NULL)
@@ -330,6 +332,8 @@ function batch_create(members; steps=5, autotune=true, growth=1.5)
                              (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}, Ptr{Int32},
                               Ptr{Float64}),
                              b[], Int32(6), C_NULL, C_NULL, C_NULL, C_NULL))
+    persistent && bcheck(ccall((:tp_batch_set_mode, libtp), Cint, (Ptr{Cvoid}, Int32),
+                               b[], Int32(1)))
     bcheck(ccall((:tp_batch_capture, libtp), Cint, (Ptr{Cvoid}, Int64, Float64),
                  b[], steps, growth))
     return b[]
