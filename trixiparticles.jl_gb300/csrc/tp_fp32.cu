@@ -14,9 +14,9 @@
 //   * positions and their Runge-Kutta register stay FP64 (the drift! accumulation); velocity
 //     and density registers are FP32.
 // The neighbour set is the FP32 one: |o_a - o_b + shift|^2 <= (2h)^2 evaluated in FP32.
-// A neighbour gather is 36 bytes from three slot-ordered arrays (test {offsets, rho - rho0},
-// velocity {v, m / rho}, pressure): neighbouring lanes gather nearby slots, so small records keep
-// many of them in one cache line.
+// The list pair pass gathers one 32-byte record per candidate ({offsets, rho - rho0} and
+// {v, m / rho}, one sector) and recomputes the candidate's pressure from rho - rho0; it takes the
+// fluid candidates two at a time through the packed FP32 instructions of sm_100+.
 #include "tp_api_internal.h"
 #include "tp_lists.cuh"
 
@@ -266,9 +266,9 @@ __device__ __forceinline__ void pair32_finish(const Update32& U, int s, float4 v
 // each quad's partials enter the per-particle Kahan-compensated sums (blocked compensation: a
 // partial holds at most four terms, so its rounding is that of a four-term sum, and the running
 // sum over the ~50 quads of a 3D particle stays compensated).
-// Five 256-thread blocks per SM cap the kernel at 48 registers: the pass is bound by the L1 data
-// pipe serving its neighbour gathers and by their latency, and the extra resident warps hide
-// more of it.
+// The pass is bound by the L1 data pipe serving its neighbour gathers.  The packed form needs 64
+// registers (four 256-thread blocks per SM); capped at 48 it spills and loses to the scalar form,
+// which runs five blocks at 48.
 // STD: the configuration of the dam-break setups (Monaghan viscosity with beta = 0, Molteni-
 // Colagrossi diffusion) with the model switches resolved at compile time, and the viscosity
 // switch v_ab . x_ab < 0 taken as min(v_ab . x_ab, 0) instead of a branch.
@@ -351,6 +351,121 @@ __device__ __forceinline__ void ff_pair32(const Phys32& P, float4 ta, float4 va,
                         eos32(cb.w, P, P.fluid_clip), q);
 }
 
+// ---- two list candidates per instruction: the packed FP32 arithmetic of sm_100+ (one FFMA2,
+// FADD2 or FMUL2 computes both halves of a float2, each rounded as the scalar operation) ----
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+
+// The slot's own values, each in both halves of a pair.
+struct Own2 {
+    float2 tx, ty, tz, vx, vy, vz, pa, rhoa, nia, drhoa;  // nia = -1 / rho_a
+};
+
+// Partial sums of a quad: the .x halves collect the first, third candidate, the .y halves the
+// second, fourth.
+struct FluidSums2 {
+    float2 x = {0.0f, 0.0f}, y = {0.0f, 0.0f}, z = {0.0f, 0.0f}, r = {0.0f, 0.0f};
+};
+
+// The entry that stands for "no candidate" in a packed pair: the slot itself at cell offset
+// (0, 0, 0) (code 2 + 5 * 2 + 25 * 2), whose zero distance the exact test rejects.
+__device__ __forceinline__ unsigned self_entry(int s) {
+    return (unsigned)s | (62u << kSlotBits);
+}
+
+// ff_pair32 for the candidates e0 and e1 at once: the same terms, each half rounded as the
+// scalar code rounds it; a candidate that fails the exact test contributes exact zeros (its
+// kernel factor is replaced by 0 after the terms, which stay finite for any two particles).
+template <int ND, bool STD>
+__device__ __forceinline__ void ff_pair32x2(const Phys32& P, const Own2& A, unsigned e0,
+                                            unsigned e1, const float4* __restrict__ frec,
+                                            FluidSums2& q) {
+    float4 c0, v0, c1, v1;
+    load_rec32(frec, (int)(e0 & kSlotMask), c0, v0);
+    load_rec32(frec, (int)(e1 & kSlotMask), c1, v1);
+    // cell offsets of both entries (entry_cell_offset), as the small integers 2 - f
+    const float2 code = make_float2((float)(e0 >> kSlotBits), (float)(e1 >> kSlotBits));
+    float2 fz = fma2(code, f2(0.04f), f2(0.02f));
+    fz = make_float2(floorf(fz.x), floorf(fz.y));
+    const float2 rem = fma2(f2(-25.0f), fz, code);
+    float2 fy = fma2(rem, f2(0.2f), f2(0.1f));
+    fy = make_float2(floorf(fy.x), floorf(fy.y));
+    const float2 nfx = sub2(f2(2.0f), fma2(f2(-5.0f), fy, rem));
+    const float2 nfy = sub2(f2(2.0f), fy);
+    const float2 cs = f2(P.cs);
+    const float2 pdx = sub2(fma2(nfx, cs, A.tx), make_float2(c0.x, c1.x));
+    const float2 pdy = sub2(fma2(nfy, cs, A.ty), make_float2(c0.y, c1.y));
+    float2 d2 = fma2(pdy, pdy, mul2(pdx, pdx));
+    float2 pdz = f2(0.0f);
+    if (ND == 3) {
+        const float2 nfz = sub2(f2(2.0f), fz);
+        pdz = sub2(fma2(nfz, cs, A.tz), make_float2(c0.z, c1.z));
+        d2 = fma2(pdz, pdz, d2);
+    }
+    const bool ok0 = !(d2.x > P.sr2 || d2.x < P.az2);
+    const bool ok1 = !(d2.y > P.sr2 || d2.y < P.az2);
+    if (!(ok0 || ok1)) return;
+
+    const float2 r = mul2(d2, make_float2(rsqrtf(d2.x), rsqrtf(d2.y)));
+    const float2 t = fma2(r, f2(-P.half_hinv), f2(1.0f));
+    float2 sg = mul2(f2(P.sg_c), mul2(mul2(t, t), t));
+    sg = make_float2(ok0 ? sg.x : 0.0f, ok1 ? sg.y : 0.0f);
+    const float2 volb = make_float2(v0.w, v1.w);  // m_b / rho_b
+    const float2 drhob = make_float2(c0.w, c1.w);
+    const float2 vd0 = sub2(A.vx, make_float2(v0.x, v1.x));
+    const float2 vd1 = sub2(A.vy, make_float2(v0.y, v1.y));
+    float2 vr = fma2(vd1, pdy, mul2(vd0, pdx));
+    if (ND == 3) vr = fma2(sub2(A.vz, make_float2(v0.z, v1.z)), pdz, vr);
+    const float2 rhob = add2(f2(P.rho0), drhob);
+    // the candidates' pressures (eos32)
+    float2 pb;
+    if (P.gamma7) {
+        const float2 d = mul2(drhob, f2(P.inv_rho0));
+        float2 s = add2(f2(7.0f), d);
+        s = fma2(s, d, f2(21.0f));
+        s = fma2(s, d, f2(35.0f));
+        s = fma2(s, d, f2(35.0f));
+        s = fma2(s, d, f2(21.0f));
+        s = fma2(s, d, f2(7.0f));
+        pb = fma2(mul2(f2(P.B), d), s, f2(P.p_bg));
+        if (P.fluid_clip)
+            pb = make_float2((pb.x != pb.x || pb.x > 0.0f) ? pb.x : 0.0f,
+                             (pb.y != pb.y || pb.y > 0.0f) ? pb.y : 0.0f);
+    } else {
+        pb = make_float2(eos32(c0.w, P, P.fluid_clip), eos32(c1.w, P, P.fluid_clip));
+    }
+    float2 c = mul2(mul2(volb, A.nia), add2(A.pa, pb));
+    if (STD) {
+        const float2 mb = mul2(volb, rhob);
+        const float2 x = mul2(add2(d2, f2(P.visc_eps_h2)), mul2(f2(0.5f), add2(A.rhoa, rhob)));
+        const float2 R = make_float2(__fdividef(1.0f, x.x), __fdividef(1.0f, x.y));
+        const float2 vneg = make_float2(fminf(vr.x, 0.0f), fminf(vr.y, 0.0f));
+        c = fma2(mul2(mul2(mb, f2(P.visc_k)), vneg), R, c);
+    } else if (P.visc) {
+        auto visc = [&](float vr_, float d2_, float rho_b, float vol_b, float c_) {
+            if (!(vr_ < 0.0f)) return c_;
+            const float m_b = vol_b * rho_b;
+            const float den = d2_ + P.visc_eps_h2;
+            const float rm = 0.5f * (A.rhoa.x + rho_b);
+            const float R = __fdividef(1.0f, den * rm);
+            if (P.beta == 0.0f) return c_ + (m_b * P.visc_k) * vr_ * R;
+            const float mu = (P.visc_h * vr_) * (rm * R);
+            return c_ + (m_b * mu) * (P.visc_ac + P.beta * mu) * (den * R);
+        };
+        c = make_float2(visc(vr.x, d2.x, rhob.x, volb.x, c.x), visc(vr.y, d2.y, rhob.y, volb.y, c.y));
+    }
+    c = mul2(c, sg);
+    q.x = fma2(c, pdx, q.x);
+    q.y = fma2(c, pdy, q.y);
+    if (ND == 3) q.z = fma2(c, pdz, q.z);
+    const float2 dterm =
+        (STD || P.diff) ? mul2(f2(P.diff2), sub2(A.drhoa, drhob)) : f2(0.0f);
+    q.r = fma2(mul2(sg, volb), fma2(A.rhoa, vr, dterm), q.r);
+}
+
 template <int ND>
 __device__ __forceinline__ void fw_pair32(const Phys32& P, float4 ta, float4 va, float p_a,
                                           float rho_a, float ia, unsigned e, float4 tb,
@@ -360,6 +475,10 @@ __device__ __forceinline__ void fw_pair32(const Phys32& P, float4 ta, float4 va,
     if (d2 > P.sr2 || d2 < P.az2) return;
     fw_terms32<ND>(P, va, p_a, rho_a, ia, pd0, pd1, pd2, d2, tb.w, wpres[e & kSlotMask], q);
 }
+
+// Fluid-fluid candidates two at a time with packed FP32 instructions (ff_pair32x2) instead of one
+// at a time (ff_pair32).
+constexpr bool kPacked = true;
 
 // One fluid slot s of the list pass (a thread's whole work; shared by the per-handle kernel and
 // the batched persistent pass).
@@ -392,23 +511,54 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
         ar.add(q.r);
     };
     const int nff = ffc[s];
-    for (int k = 0; k < (nff & ~3); k += 4) {
-        const uint4 l = list_quad_stream(ff, k, nf, s);
-        FluidSums q;
-        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.x, frec, q);
-        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.y, frec, q);
-        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.z, frec, q);
-        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.w, frec, q);
-        settle(q);
-    }
-    if (nff & 3) {  // the open quad: entries beyond the count are not part of the list
-        const int k = nff & ~3, m = nff & 3;
-        const uint4 l = list_quad_stream(ff, k, nf, s);
-        FluidSums q;
-        ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.x, frec, q);
-        if (m > 1) ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.y, frec, q);
-        if (m > 2) ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.z, frec, q);
-        settle(q);
+    if (kPacked) {
+        // two candidates per packed instruction; the halves of a quad's partials are added
+        // before they enter the compensated sums
+        const Own2 A = {f2(ta.x), f2(ta.y), f2(ta.z), f2(va.x), f2(va.y), f2(va.z), f2(p_a),
+                        f2(rho_a), f2(-ia), f2(drho_a)};
+        auto settle2 = [&](const FluidSums2& q2) {
+            FluidSums q;
+            q.x = q2.x.x + q2.x.y;
+            q.y = q2.y.x + q2.y.y;
+            q.z = q2.z.x + q2.z.y;
+            q.r = q2.r.x + q2.r.y;
+            settle(q);
+        };
+        for (int k = 0; k < (nff & ~3); k += 4) {
+            const uint4 l = list_quad_stream(ff, k, nf, s);
+            FluidSums2 q;
+            ff_pair32x2<ND, STD>(P, A, l.x, l.y, frec, q);
+            ff_pair32x2<ND, STD>(P, A, l.z, l.w, frec, q);
+            settle2(q);
+        }
+        if (nff & 3) {  // the open quad: entries beyond the count are not part of the list
+            const int k = nff & ~3, m = nff & 3;
+            const uint4 l = list_quad_stream(ff, k, nf, s);
+            const unsigned none = self_entry(s);
+            FluidSums2 q;
+            ff_pair32x2<ND, STD>(P, A, l.x, m > 1 ? l.y : none, frec, q);
+            if (m > 2) ff_pair32x2<ND, STD>(P, A, l.z, none, frec, q);
+            settle2(q);
+        }
+    } else {
+        for (int k = 0; k < (nff & ~3); k += 4) {
+            const uint4 l = list_quad_stream(ff, k, nf, s);
+            FluidSums q;
+            ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.x, frec, q);
+            ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.y, frec, q);
+            ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.z, frec, q);
+            ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.w, frec, q);
+            settle(q);
+        }
+        if (nff & 3) {  // the open quad: entries beyond the count are not part of the list
+            const int k = nff & ~3, m = nff & 3;
+            const uint4 l = list_quad_stream(ff, k, nf, s);
+            FluidSums q;
+            ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.x, frec, q);
+            if (m > 1) ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.y, frec, q);
+            if (m > 2) ff_pair32<ND, STD>(P, ta, va, p_a, rho_a, ia, drho_a, l.z, frec, q);
+            settle(q);
+        }
     }
     // the wall neighbours continue the same compensated sums
     const int nfw = fwc[s];
@@ -437,7 +587,7 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
 }
 
 template <int ND, bool INTEGRATE, bool STD>
-__global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
+__global__ void __launch_bounds__(256, kPacked ? 4 : 5) k_pair32(Phys32 P, int nf,
                                                 const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float* __restrict__ fpres,
@@ -459,7 +609,7 @@ __global__ void __launch_bounds__(256, 5) k_pair32(Phys32 P, int nf,
 // of kBatchTile consecutive slots of one member, the largest member's tiles first -- from a
 // counter in global memory (atomicAdd) until none is left, and runs the list pass on them.
 template <int ND, bool STD>
-__global__ void __launch_bounds__(kBatchTile, 5) k_batch_pair32(const __grid_constant__ Pair32Batch B,
+__global__ void __launch_bounds__(kBatchTile, kPacked ? 4 : 5) k_batch_pair32(const __grid_constant__ Pair32Batch B,
                                                                  unsigned* __restrict__ counter) {
     __shared__ int item;
     for (;;) {
