@@ -188,6 +188,13 @@ tp_status tp_nhs_debug(tp_handle* h, const double* u_ode, int32_t* cell, int32_t
 tp_status tp_div_fast(tp_handle* h, double x64, const double* y64, double* out64, float x32,
                       const float* y32, float* out32, int64_t n);
 
+/* Diagnostic (parity checks): the pair distance of the FP64 kernels, r[i] = |x_ab| from
+ * d2[i] = |x_ab|^2 (> 0, normal) as the pair and Adami kernels form it (the approximate
+ * reciprocal square root rsqrt.approx.ftz.f64 refined by one third-order step, times d2; the
+ * reference takes sqrt, src/schemes/fluid/weakly_compressible_sph/rhs.jl:27), over n device
+ * elements.  Asynchronous on the handle's stream. */
+tp_status tp_pair_distance(tp_handle* h, const double* d2, double* r, int64_t n);
+
 /* Grid layout: dims[0..2] cells per dimension (padding included), *cell_size = 2h. */
 tp_status tp_grid_info(tp_handle* h, int32_t dims[3], double* cell_size, double lo[3]);
 

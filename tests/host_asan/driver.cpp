@@ -85,6 +85,14 @@ static int run(int nd, int precision) {
     bad |= tp_adjoint_forward(h, v.data(), u.data(), 1e-4, 0, 5) != TP_ERR_ARGUMENT;
     bad |= tp_adjoint_forward(h, v.data(), u.data(), -1e-4, 3, 5) != TP_ERR_ARGUMENT;
     bad |= tp_adjoint_kernel_launches(h) <= 0;
+    // diagnostics: pair distance and div_fast argument checks
+    {
+        std::vector<double> d2(5, 1.0), r(5);
+        bad |= tp_pair_distance(h, d2.data(), r.data(), 5) != TP_OK;
+        bad |= tp_pair_distance(h, nullptr, r.data(), 5) != TP_ERR_ARGUMENT;
+        bad |= tp_pair_distance(h, d2.data(), r.data(), -1) != TP_ERR_ARGUMENT;
+        bad |= tp_pair_distance(h, nullptr, nullptr, 0) != TP_OK;
+    }
     // interpolation: with and without walls, argument checks
     {
         const int64_t np = 7;

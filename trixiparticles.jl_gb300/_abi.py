@@ -93,6 +93,7 @@ PROTOTYPES = [
     ("tp_nhs_debug", c_int32, [c_void_p] + [c_void_p] * 6),
     ("tp_div_fast", c_int32, [c_void_p, c_double, c_void_p, c_void_p, c_float, c_void_p,
                              c_void_p, c_int64]),
+    ("tp_pair_distance", c_int32, [c_void_p, c_void_p, c_void_p, c_int64]),
     ("tp_grid_info", c_int32, [c_void_p, POINTER(c_int32), POINTER(c_double), POINTER(c_double)]),
     ("tp_conservation", c_int32, [c_void_p, c_void_p, POINTER(c_double)]),
     ("tp_sync", c_int32, [c_void_p]),

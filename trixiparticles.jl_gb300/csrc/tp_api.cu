@@ -1362,6 +1362,17 @@ tp_status tp_div_fast(tp_handle* h, double x64, const double* y64, double* out64
     return TP_OK;
 }
 
+tp_status tp_pair_distance(tp_handle* h, const double* d2, double* r, int64_t n) {
+    if (!h) return TP_ERR_ARGUMENT;
+    if (n < 0 || n > (int64_t)1 << 36)
+        return fail(h, TP_ERR_ARGUMENT, "tp_pair_distance: bad element count");
+    if (n == 0) return TP_OK;
+    if (!d2 || !r) return fail(h, TP_ERR_ARGUMENT, "tp_pair_distance: null array");
+    pair_distance_check(h, d2, r, (long long)n);
+    TP_LAUNCHED(h, "pair distance");
+    return TP_OK;
+}
+
 tp_status tp_nhs_debug(tp_handle* h, const double* u_ode, int32_t* cell, int32_t* order,
                        int32_t* nnb_ff, int32_t* nnb_fw, int32_t* nnb_wf) {
     if (!h) return TP_ERR_ARGUMENT;

@@ -18,6 +18,7 @@ void fp64_pair_stage(tp_handle* h, PhysState& st, double A, double B, double dt,
 void fp64_count(tp_handle* h, int* nnb_ff, int* nnb_fw, int* nnb_wf);
 void div_fast_check(tp_handle* h, double x64, const double* y64, double* out64, float x32,
                     const float* y32, float* out32, long long n);
+void pair_distance_check(tp_handle* h, const double* d2, double* r, long long n);
 
 // FP32 precision form (tp_fp32.cu)
 void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,

@@ -36,6 +36,18 @@ __device__ __forceinline__ double fast_inv(double a) {
 
 __device__ __forceinline__ double div_fast(double x, double y) { return x * fast_inv(y); }
 
+// Pair distance r = sqrt(d2) for a normal d2 > 0, with few FP64 instructions: the approximate
+// reciprocal square root y of `rsqrt.approx.ftz.f64` refined by one third-order Householder step
+// for f(y) = y^-2 - d2 (e = 1 - d2 y^2, y' = y (1 + e/2 + 3 e^2 / 8), error O(e^3)), folded into
+// r = d2 y' = t + t e (1/2 + 3 e / 8) with t = d2 y.  Within a few ulp of the rounded sqrt.
+__device__ __forceinline__ double pair_distance(double d2) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d2));
+    const double t = d2 * y;
+    const double e = fma(-t, y, 1.0);
+    return fma(t * e, fma(e, 0.375, 0.5), t);
+}
+
 template <int ND>
 __device__ __forceinline__ double dist2_rn(double p0, double p1, double p2) {
     double d2 = __dadd_rn(__dmul_rn(p0, p0), __dmul_rn(p1, p1));
@@ -301,7 +313,7 @@ __global__ void __launch_bounds__(256) k_filter64(
 //   1 / (rho_a rho_b) and m_b / rho_b from the per-particle fast_inv(rho) of the pack;
 //   the constant sg_c folded into the neighbour records (S_b = sg_c m_b / rho_b, p_b S_b,
 //   2 m_b alpha c h sg_c), so the pressure factor is one FMA and sg is t^3 alone;
-//   r = d^2 rsqrt(d^2); the zero-distance skip `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28)
+//   r from d^2 by pair_distance; the zero-distance skip `distance < sqrt(eps((2h)^2))` (rhs.jl:27-28)
 //   tested as d^2 < eps((2h)^2).
 // Each term equals the reference's expression up to a few ulp of rounding.
 __device__ __forceinline__ double monaghan_coef(const Phys& P, const double4_32a& ab, double rho_b,
@@ -360,7 +372,7 @@ __global__ void __launch_bounds__(256) k_adami64(Phys P, int nw,
         const double pd2 = (ND == 3) ? xw.z - xb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        const double r = d2 > 0.0 ? d2 * rsqrt(d2) : 0.0;
+        const double r = d2 > 0.0 ? pair_distance(d2) : 0.0;
         const double rho_f = fvel[b].w;
         double sum;
         if (FOLD) {
@@ -452,7 +464,7 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        const double r = d2 * rsqrt(d2);  // d2 >= eps((2h)^2): the filter dropped closer pairs
+        const double r = pair_distance(d2);  // d2 >= eps((2h)^2): the filter dropped closer pairs
         const double t = fma(-r, P.half_hinv, 1.0);
         const double t3 = (t * t) * t;  // grad W_ab = sg_c t^3 x_ab, sg_c folded into ab
         const double4_32a vb = fvel[b];
@@ -482,7 +494,7 @@ __global__ void __launch_bounds__(256) k_pair64(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        const double r = d2 * rsqrt(d2);
+        const double r = pair_distance(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
         const double t3 = (t * t) * t;
         const double4_32a sb = wstate[b];  // {p, rho, p S, S = sg_c m / rho}
@@ -542,7 +554,7 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        const double r = d2 * rsqrt(d2);
+        const double r = pair_distance(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
         const double sg = P.sg_c * ((t * t) * t);
         const double4_32a vb = fvel[b];
@@ -599,7 +611,7 @@ __global__ void __launch_bounds__(256) k_pair64s(Phys P, int nf,
         const double pd2 = (ND == 3) ? pa.z - pb.z : 0.0;
         double d2 = pd0 * pd0 + pd1 * pd1;
         if (ND == 3) d2 += pd2 * pd2;
-        const double r = d2 * rsqrt(d2);
+        const double r = pair_distance(d2);
         const double t = fma(-r, P.half_hinv, 1.0);
         const double sg = P.sg_c * ((t * t) * t);
         const double4_32a sb = wstate[b];
@@ -864,6 +876,17 @@ void div_fast_check(tp_handle* h, double x64, const double* y64, double* out64, 
                     const float* y32, float* out32, long long n) {
     k_div_fast<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(x64, y64, out64, x32, y32,
                                                                      out32, n);
+}
+
+// The pair distance of the FP64 kernels over caller arrays (tp_pair_distance).
+__global__ void k_pair_distance(const double* __restrict__ d2, double* __restrict__ r,
+                                long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = pair_distance(d2[i]);
+}
+
+void pair_distance_check(tp_handle* h, const double* d2, double* r, long long n) {
+    k_pair_distance<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(d2, r, n);
 }
 
 }  // namespace tp
