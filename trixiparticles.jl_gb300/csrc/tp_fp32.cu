@@ -65,6 +65,62 @@ __device__ __forceinline__ void load_rec32(const float4* __restrict__ rec, int s
         : "l"(rec + 2 * (size_t)s));
 }
 
+// ---- two list candidates per instruction: the packed FP32 arithmetic of sm_100+ (one FFMA2,
+// FADD2 or FMUL2 computes both halves of a float2, each rounded as the scalar operation) ----
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+
+// Pair differences o_a - o_b + (c_a - c_b) cs of two list entries (pair_diff_decoded for both
+// halves: the cell offsets decoded from the entry codes as the small integers 2 - f, so that
+// (o_a - d cs) is fmaf(2 - f, cs, o_a)); returns |x_ab|^2.
+template <int ND>
+__device__ __forceinline__ float2 pair_diff2(float4 ta, float cs, unsigned e0, unsigned e1,
+                                             float4 c0, float4 c1, float2& pdx, float2& pdy,
+                                             float2& pdz) {
+    const float2 code = make_float2((float)(e0 >> kSlotBits), (float)(e1 >> kSlotBits));
+    float2 fz = fma2(code, f2(0.04f), f2(0.02f));
+    fz = make_float2(floorf(fz.x), floorf(fz.y));
+    const float2 rem = fma2(f2(-25.0f), fz, code);
+    float2 fy = fma2(rem, f2(0.2f), f2(0.1f));
+    fy = make_float2(floorf(fy.x), floorf(fy.y));
+    const float2 nfx = sub2(f2(2.0f), fma2(f2(-5.0f), fy, rem));
+    const float2 nfy = sub2(f2(2.0f), fy);
+    const float2 c = f2(cs);
+    pdx = sub2(fma2(nfx, c, f2(ta.x)), make_float2(c0.x, c1.x));
+    pdy = sub2(fma2(nfy, c, f2(ta.y)), make_float2(c0.y, c1.y));
+    float2 d2 = fma2(pdy, pdy, mul2(pdx, pdx));
+    pdz = f2(0.0f);
+    if (ND == 3) {
+        pdz = sub2(fma2(sub2(f2(2.0f), fz), c, f2(ta.z)), make_float2(c0.z, c1.z));
+        d2 = fma2(pdz, pdz, d2);
+    }
+    return d2;
+}
+
+// eos32 of two density deviations (the same operations, so the same values).
+__device__ __forceinline__ float2 eos32x2(float2 drho, const Phys32& P, int clip) {
+    float2 p;
+    if (P.gamma7) {
+        const float2 d = mul2(drho, f2(P.inv_rho0));
+        float2 q = add2(f2(7.0f), d);
+        q = fma2(q, d, f2(21.0f));
+        q = fma2(q, d, f2(35.0f));
+        q = fma2(q, d, f2(35.0f));
+        q = fma2(q, d, f2(21.0f));
+        q = fma2(q, d, f2(7.0f));
+        p = fma2(mul2(f2(P.B), d), q, f2(P.p_bg));
+        if (clip)
+            p = make_float2((p.x != p.x || p.x > 0.0f) ? p.x : 0.0f,
+                            (p.y != p.y || p.y > 0.0f) ? p.y : 0.0f);
+    } else {
+        p = make_float2(eos32(drho.x, P, clip), eos32(drho.y, P, clip));
+    }
+    return p;
+}
+
 __device__ __forceinline__ float eos32_inverse_dev(float p, const Phys32& P) {
     return P.rho0 * expm1f(log1pf((p - P.p_bg) / P.B) * P.inv_gamma);
 }
@@ -150,10 +206,40 @@ __global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4
     if (s < n) st[s] = make_float4(0.0f, 0.0f, (float)wpos[s].w, 0.0f);
 }
 
-// Per wall slot over its fluid list: the fluid neighbour's offsets and rho - rho0 come with its
-// test record, its pressure from the dense pressure array (20 bytes per pair).  Besides the wall
-// state, the pass leaves m / rho of the wall in the fourth slot of its test record and its
-// pressure in a dense array, which is what the fluid pair pass gathers.
+// Adami terms of the fluid candidates e0 and e1 of a wall (packed FP32; `use1` false leaves the
+// second half out -- its entry is then a copy of the first): with the support test d2 <= (2h)^2
+// and r < 2h, ps += (p_off + p_f + g . (rho_f x_wf)) W(r) and vs += W(r), the fluid pressure from
+// its rho - rho0 by the EOS the pack applies (the same value it writes).
+template <int ND>
+__device__ __forceinline__ void adami_pair2(const Phys32& P, float4 tw, unsigned e0, unsigned e1,
+                                            bool use1, const float4* __restrict__ ftest,
+                                            float2& ps, float2& vs) {
+    const float4 c0 = ftest[e0 & kSlotMask];
+    const float4 c1 = ftest[e1 & kSlotMask];
+    float2 pdx, pdy, pdz;
+    const float2 d2 = pair_diff2<ND>(tw, P.cs, e0, e1, c0, c1, pdx, pdy, pdz);
+    const float2 r = make_float2(sqrtf(d2.x), sqrtf(d2.y));
+    const bool in0 = !(d2.x > P.sr2) && r.x < P.two_h;
+    const bool in1 = use1 && !(d2.y > P.sr2) && r.y < P.two_h;
+    const float2 drho = make_float2(c0.w, c1.w);
+    const float2 rho_f = add2(f2(P.rho0), drho);
+    float2 hp = fma2(f2(P.g[1]), mul2(rho_f, pdy), mul2(f2(P.g[0]), mul2(rho_f, pdx)));
+    if (ND == 3) hp = fma2(f2(P.g[2]), mul2(rho_f, pdz), hp);
+    const float2 sum = add2(add2(f2(P.p_off), eos32x2(drho, P, P.fluid_clip)), hp);
+    const float2 q = mul2(r, f2(P.h_inv));
+    const float2 t = fma2(f2(-0.5f), q, f2(1.0f));
+    const float2 t2 = mul2(t, t);
+    float2 W = mul2(mul2(f2(P.wc2_norm), mul2(t2, t2)), fma2(f2(2.0f), q, f2(1.0f)));
+    W = make_float2(in0 ? W.x : 0.0f, in1 ? W.y : 0.0f);
+    ps = fma2(sum, W, ps);
+    vs = add2(vs, W);
+}
+
+// Per wall slot over its fluid list (the Adami gather): the list walked a quad at a time, the
+// candidates two per packed instruction, each quad's partials added into Kahan-compensated sums;
+// a neighbour gather is its 16-byte test record {offsets, rho - rho0}.  Besides the wall state,
+// the pass leaves m / rho of the wall in the fourth slot of its test record and its pressure in
+// a dense array, which is what the fluid pair pass gathers.
 template <int ND>
 __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __restrict__ wtest,
                                                  const unsigned* __restrict__ wf,
@@ -161,37 +247,20 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __res
                                                  float4* __restrict__ wstate,
                                                  float* __restrict__ wpres,
                                                  double* __restrict__ wvol,
-                                                 const float4* __restrict__ ftest,
-                                                 const float* __restrict__ fpres) {
-    __shared__ float4 off[kOffsetCodes];
-    fill_offset_table(off, P.cs);
+                                                 const float4* __restrict__ ftest) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const float4 tw = wtest[w];
     Kahan Ps, V;
     const int n = wfc[w];
-    uint4 lq;  // the list quad holding entry k
-    for (int k = 0; k < n; ++k) {
-        const unsigned e = list_next(wf, k, nw, w, lq);
-        const int b = (int)(e & kSlotMask);
-        const float4 cb = ftest[b];
-        float pd0, pd1, pd2;
-        const float d2 = pair_diff<ND>(tw, off, e, cb, pd0, pd1, pd2);
-        if (d2 > P.sr2) continue;
-        const float r = sqrtf(d2);
-        const float rho_f = P.rho0 + cb.w;
-        float hp = P.g[0] * (rho_f * pd0) + P.g[1] * (rho_f * pd1);
-        if (ND == 3) hp += P.g[2] * (rho_f * pd2);
-        const float sum = (P.p_off + fpres[b]) + hp;
-        float W = 0.0f;
-        if (r < P.two_h) {
-            const float q = r * P.h_inv;
-            const float t = 1.0f - 0.5f * q;
-            const float t2 = t * t;
-            W = (P.wc2_norm * (t2 * t2)) * (2.0f * q + 1.0f);
-        }
-        Ps.add(sum * W);
-        V.add(W);
+    for (int k = 0; k < n; k += 4) {
+        const uint4 l = list_quad_stream(wf, k, nw, w);
+        const int m = n - k;  // entries of this quad that belong to the list (>= 1)
+        float2 ps = f2(0.0f), vs = f2(0.0f);
+        adami_pair2<ND>(P, tw, l.x, m > 1 ? l.y : l.x, m > 1, ftest, ps, vs);
+        if (m > 2) adami_pair2<ND>(P, tw, l.z, m > 3 ? l.w : l.z, m > 3, ftest, ps, vs);
+        Ps.add(ps.x + ps.y);
+        V.add(vs.x + vs.y);
     }
     float pw = Ps.s - Ps.c;
     const float vw = V.s - V.c;
@@ -351,17 +420,10 @@ __device__ __forceinline__ void ff_pair32(const Phys32& P, float4 ta, float4 va,
                         eos32(cb.w, P, P.fluid_clip), q);
 }
 
-// ---- two list candidates per instruction: the packed FP32 arithmetic of sm_100+ (one FFMA2,
-// FADD2 or FMUL2 computes both halves of a float2, each rounded as the scalar operation) ----
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
-
 // The slot's own values, each in both halves of a pair.
 struct Own2 {
-    float2 tx, ty, tz, vx, vy, vz, pa, rhoa, nia, drhoa;  // nia = -1 / rho_a
+    float4 t;                                       // the slot's test record
+    float2 vx, vy, vz, pa, rhoa, nia, drhoa;        // nia = -1 / rho_a
 };
 
 // Partial sums of a quad: the .x halves collect the first, third candidate, the .y halves the
@@ -386,25 +448,8 @@ __device__ __forceinline__ void ff_pair32x2(const Phys32& P, const Own2& A, unsi
     float4 c0, v0, c1, v1;
     load_rec32(frec, (int)(e0 & kSlotMask), c0, v0);
     load_rec32(frec, (int)(e1 & kSlotMask), c1, v1);
-    // cell offsets of both entries (entry_cell_offset), as the small integers 2 - f
-    const float2 code = make_float2((float)(e0 >> kSlotBits), (float)(e1 >> kSlotBits));
-    float2 fz = fma2(code, f2(0.04f), f2(0.02f));
-    fz = make_float2(floorf(fz.x), floorf(fz.y));
-    const float2 rem = fma2(f2(-25.0f), fz, code);
-    float2 fy = fma2(rem, f2(0.2f), f2(0.1f));
-    fy = make_float2(floorf(fy.x), floorf(fy.y));
-    const float2 nfx = sub2(f2(2.0f), fma2(f2(-5.0f), fy, rem));
-    const float2 nfy = sub2(f2(2.0f), fy);
-    const float2 cs = f2(P.cs);
-    const float2 pdx = sub2(fma2(nfx, cs, A.tx), make_float2(c0.x, c1.x));
-    const float2 pdy = sub2(fma2(nfy, cs, A.ty), make_float2(c0.y, c1.y));
-    float2 d2 = fma2(pdy, pdy, mul2(pdx, pdx));
-    float2 pdz = f2(0.0f);
-    if (ND == 3) {
-        const float2 nfz = sub2(f2(2.0f), fz);
-        pdz = sub2(fma2(nfz, cs, A.tz), make_float2(c0.z, c1.z));
-        d2 = fma2(pdz, pdz, d2);
-    }
+    float2 pdx, pdy, pdz;
+    const float2 d2 = pair_diff2<ND>(A.t, P.cs, e0, e1, c0, c1, pdx, pdy, pdz);
     const bool ok0 = !(d2.x > P.sr2 || d2.x < P.az2);
     const bool ok1 = !(d2.y > P.sr2 || d2.y < P.az2);
     if (!(ok0 || ok1)) return;
@@ -420,23 +465,7 @@ __device__ __forceinline__ void ff_pair32x2(const Phys32& P, const Own2& A, unsi
     float2 vr = fma2(vd1, pdy, mul2(vd0, pdx));
     if (ND == 3) vr = fma2(sub2(A.vz, make_float2(v0.z, v1.z)), pdz, vr);
     const float2 rhob = add2(f2(P.rho0), drhob);
-    // the candidates' pressures (eos32)
-    float2 pb;
-    if (P.gamma7) {
-        const float2 d = mul2(drhob, f2(P.inv_rho0));
-        float2 s = add2(f2(7.0f), d);
-        s = fma2(s, d, f2(21.0f));
-        s = fma2(s, d, f2(35.0f));
-        s = fma2(s, d, f2(35.0f));
-        s = fma2(s, d, f2(21.0f));
-        s = fma2(s, d, f2(7.0f));
-        pb = fma2(mul2(f2(P.B), d), s, f2(P.p_bg));
-        if (P.fluid_clip)
-            pb = make_float2((pb.x != pb.x || pb.x > 0.0f) ? pb.x : 0.0f,
-                             (pb.y != pb.y || pb.y > 0.0f) ? pb.y : 0.0f);
-    } else {
-        pb = make_float2(eos32(c0.w, P, P.fluid_clip), eos32(c1.w, P, P.fluid_clip));
-    }
+    const float2 pb = eos32x2(drhob, P, P.fluid_clip);  // the candidates' pressures
     float2 c = mul2(mul2(volb, A.nia), add2(A.pa, pb));
     if (STD) {
         const float2 mb = mul2(volb, rhob);
@@ -514,8 +543,8 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
     if (kPacked) {
         // two candidates per packed instruction; the halves of a quad's partials are added
         // before they enter the compensated sums
-        const Own2 A = {f2(ta.x), f2(ta.y), f2(ta.z), f2(va.x), f2(va.y), f2(va.z), f2(p_a),
-                        f2(rho_a), f2(-ia), f2(drho_a)};
+        const Own2 A = {ta, f2(va.x), f2(va.y), f2(va.z), f2(p_a), f2(rho_a), f2(-ia),
+                        f2(drho_a)};
         auto settle2 = [&](const FluidSums2& q2) {
             FluidSums q;
             q.x = q2.x.x + q2.x.y;
@@ -889,11 +918,11 @@ void fp32_adami(tp_handle* h) {
     if (h->cfg.ndims == 2)
         k_adami32<2><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_p32, h->w_vol,
-            h->f_test, (const float*)h->f_aux);
+            h->f_test);
     else
         k_adami32<3><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_p32, h->w_vol,
-            h->f_test, (const float*)h->f_aux);
+            h->f_test);
 }
 
 template <int ND, bool INTEG>
