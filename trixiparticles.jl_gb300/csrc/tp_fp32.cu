@@ -506,8 +506,10 @@ __device__ __forceinline__ void fw_pair32(const Phys32& P, float4 ta, float4 va,
 }
 
 // Fluid-fluid candidates two at a time with packed FP32 instructions (ff_pair32x2) instead of one
-// at a time (ff_pair32).
-constexpr bool kPacked = true;
+// at a time (ff_pair32): in 3D (the 512-instance 2D ensemble measured 0.7 % faster with the scalar
+// form, whose 48 registers keep five blocks per SM).
+template <int ND>
+constexpr bool kPackedPairs = ND == 3;
 
 // One fluid slot s of the list pass (a thread's whole work; shared by the per-handle kernel and
 // the batched persistent pass).
@@ -540,7 +542,7 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
         ar.add(q.r);
     };
     const int nff = ffc[s];
-    if (kPacked) {
+    if (kPackedPairs<ND>) {
         // two candidates per packed instruction; the halves of a quad's partials are added
         // before they enter the compensated sums
         const Own2 A = {ta, f2(va.x), f2(va.y), f2(va.z), f2(p_a), f2(rho_a), f2(-ia),
@@ -616,7 +618,7 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
 }
 
 template <int ND, bool INTEGRATE, bool STD>
-__global__ void __launch_bounds__(256, kPacked ? 4 : 5) k_pair32(Phys32 P, int nf,
+__global__ void __launch_bounds__(256, kPackedPairs<ND> ? 4 : 5) k_pair32(Phys32 P, int nf,
                                                 const float4* __restrict__ ftest,
                                                 const float4* __restrict__ fvel,
                                                 const float* __restrict__ fpres,
@@ -638,7 +640,7 @@ __global__ void __launch_bounds__(256, kPacked ? 4 : 5) k_pair32(Phys32 P, int n
 // of kBatchTile consecutive slots of one member, the largest member's tiles first -- from a
 // counter in global memory (atomicAdd) until none is left, and runs the list pass on them.
 template <int ND, bool STD>
-__global__ void __launch_bounds__(kBatchTile, kPacked ? 4 : 5) k_batch_pair32(const __grid_constant__ Pair32Batch B,
+__global__ void __launch_bounds__(kBatchTile, kPackedPairs<ND> ? 4 : 5) k_batch_pair32(const __grid_constant__ Pair32Batch B,
                                                                  unsigned* __restrict__ counter) {
     __shared__ int item;
     for (;;) {
