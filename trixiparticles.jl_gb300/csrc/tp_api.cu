@@ -861,6 +861,21 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
     A(dalloc(&h->d_err, 1));
     A(cudaMallocHost((void**)&h->h_err, 4 * sizeof(int)));
+    {
+        // the cell origins (cmin + c) * cs32 per axis, computed once here with the FP64 multiply
+        // the device would do (exact for cell indices below 2^29: a 24-bit FP32 cell size)
+        const GridDesc& g = h->grid;
+        const double cs32 = (double)(float)g.cs;
+        std::vector<double> org((size_t)(g.n[0] + g.n[1] + g.n[2]));
+        size_t k = 0;
+        for (int d = 0; d < 3; ++d)
+            for (int c = 0; c < g.n[d]; ++c) org[k++] = (double)(g.cmin[d] + c) * cs32;
+        A(dalloc(&h->grid_org, org.size()));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->grid_org, org.data(), org.size() * sizeof(double),
+                           cudaMemcpyHostToDevice);
+        h->grid.org = h->grid_org;
+    }
     if (e == cudaSuccess) e = cudaMemset(h->f_count, 0, nc * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->gate, 0, 5 * sizeof(unsigned));
@@ -890,6 +905,7 @@ tp_status tp_destroy(tp_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
+                    h->grid_org,
                     h->d_max, h->e_ff, h->e_fw, h->e_wf, h->ec_ff, h->ec_fw, h->acc, h->spv};
     for (void* p : more)
         if (p) cudaFree(p);

@@ -105,6 +105,7 @@ struct tp_handle {
     // GB300 in both forms, at rest and in a 3 m/s flow (shorter lists outweigh the rebuilds).
     double skin = 0.05;
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
+    double* grid_org = nullptr;  // per-axis cell origins of the FP32 cell size (GridDesc::org)
     unsigned* gate = nullptr;   // {force, max squared displacement bits, squared threshold bits,
                                 //  next stage's displacement bits, rebuilds let through}
     int* d_max = nullptr;       // scratch for the largest cell occupancy

@@ -38,6 +38,9 @@ struct GridDesc {
     int cmin[3];
     int n[3];
     int ncells;
+    // optional (device): the cell origins (cmin + c) * cs32 of the FP32 cell size per axis, axis d
+    // from org + n[0] (d > 0) + n[1] (d > 1), so that the test records take no FP64 product
+    const double* org = nullptr;
 };
 
 // Physical parameters, precomputed on the host in FP64 following the reference expressions.

@@ -438,9 +438,15 @@ __device__ __forceinline__ float4 test_record_in(const double* x, const GridDesc
     int c[3];
     key_to_coords(key, g, c);
     float o[3] = {0.0f, 0.0f, 0.0f};
+    if (g.org) {  // the same exact products from the origin table (FP64 throughput is scarce)
+        const int base[3] = {0, g.n[0], g.n[0] + g.n[1]};
 #pragma unroll
-    for (int d = 0; d < ND; ++d)
-        o[d] = (float)__dsub_rn(x[d], __dmul_rn((double)(g.cmin[d] + c[d]), cs32));
+        for (int d = 0; d < ND; ++d) o[d] = (float)__dsub_rn(x[d], __ldg(g.org + base[d] + c[d]));
+    } else {
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+            o[d] = (float)__dsub_rn(x[d], __dmul_rn((double)(g.cmin[d] + c[d]), cs32));
+    }
     return make_float4(o[0], o[1], o[2], (float)c[0]);
 }
 
