@@ -593,7 +593,8 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
                 h->w_start,
                 h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate);
         if (nw > 0)
-            k_build_wall_lists<ND><<<nblk(nw, 128), 128, 0, h->stream>>>(
+            k_build_wall_lists<ND><<<std::min(nblk(nw, 128), 8 * h->num_sms), 128, 0,
+                                     h->stream>>>(
                 h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_skey, h->f_start,
                 h->l_wf,
                 h->c_wf, h->cap_wf, h->d_err, gate);
@@ -861,6 +862,11 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
     A(dalloc(&h->d_err, 1));
     A(cudaMallocHost((void**)&h->h_err, 4 * sizeof(int)));
+    {
+        int dev = 0;
+        A(cudaGetDevice(&dev));
+        A(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev));
+    }
     {
         // the cell origins (cmin + c) * cs32 per axis, computed once here with the FP64 multiply
         // the device would do (exact for cell indices below 2^29: a 24-bit FP32 cell size)

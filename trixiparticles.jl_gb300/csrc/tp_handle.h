@@ -106,6 +106,7 @@ struct tp_handle {
     double skin = 0.05;
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
     double* grid_org = nullptr;  // per-axis cell origins of the FP32 cell size (GridDesc::org)
+    int num_sms = 1;             // multiprocessors of the device (fixed-grid launches)
     unsigned* gate = nullptr;   // {force, max squared displacement bits, squared threshold bits,
                                 //  next stage's displacement bits, rebuilds let through}
     int* d_max = nullptr;       // scratch for the largest cell occupancy

@@ -184,6 +184,9 @@ __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__
     if ((threadIdx.x & 31) == 0 && d2 > 0.0f) atomicMax(&gate[1], __float_as_uint(d2));
 }
 
+// Widest x extent (in cells beyond the first) of a lane group of the candidate search.
+constexpr int kGroupSpan = 2;
+
 // Warp-cooperative candidate search: lanes are grouped by their (cy, cz) row; for each searched
 // row the group's candidates form one contiguous slot range (cells are linearised x fastest),
 // which the warp streams through shared memory 32 test records at a time, and every lane tests
@@ -226,10 +229,13 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
     const float r2box = rbox * rbox;
     unsigned todo = __ballot_sync(FULL, active);
     while (todo) {
+        // a group: the lowest pending lane and the pending lanes of its row at most kGroupSpan
+        // cells further along x (slot order puts them after it), so that a warp whose slots sit
+        // at both ends of a row (the two side walls of a tank) does not search the whole row
         const int leader = __ffs(todo) - 1;
         const int yz0 = __shfl_sync(FULL, yz, leader);
         const int cx0 = __shfl_sync(FULL, c[0], leader);
-        const bool ing = active && (yz == yz0);
+        const bool ing = active && ((todo >> lane) & 1u) && (yz == yz0) && (c[0] - cx0 <= kGroupSpan);
         const unsigned grp = __ballot_sync(FULL, ing);
         todo &= ~grp;
         const int cy = yz0 % g.n[1], cz = yz0 / g.n[1];
@@ -394,7 +400,9 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     if (n1 > cap_ff || n2 > cap_fw) atomicOr(err, TP_ERRBIT_CAPACITY);
 }
 
-// Wall slots: wall-fluid lists (the Adami gather).
+// Wall slots: wall-fluid lists (the Adami gather).  Most wall slots of a tank have no fluid in
+// reach and finish their search at once, so the launch keeps a fixed grid of resident blocks that
+// walk the 128-slot tiles (tile = blockIdx.x, + gridDim.x, ...) instead of one block per tile.
 template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     GridDesc g, float cs, float m, float r2f, int nw, const float4* __restrict__ wtest,
@@ -409,17 +417,21 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     float4* cand = cand_all[threadIdx.x >> 5];
     int2* cidx = cidx_all[threadIdx.x >> 5];
     unsigned* lbuf = &lbuf_all[0][threadIdx.x];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = s < nw;
-    const int si = active ? s : 0;
-    const float4 ta = wtest[si];
-    int c[3];
-    key_to_coords(wskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
-                                    cidx, lbuf, wf, nw, cap_wf, s);
-    if (!active) return;
-    wfc[s] = min(n1, cap_wf);
-    if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
+    const int ntiles = (nw + 127) / 128;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int s = tile * 128 + threadIdx.x;
+        const bool active = s < nw;
+        const int si = active ? s : 0;
+        const float4 ta = wtest[si];
+        int c[3];
+        key_to_coords(wskey[si], g, c);
+        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
+                                        cidx, lbuf, wf, nw, cap_wf, s);
+        if (active) {
+            wfc[s] = min(n1, cap_wf);
+            if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
+        }
+    }
 }
 
 // Largest cell occupancy of a freshly counted histogram (list capacity sizing).
