@@ -476,11 +476,11 @@ tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tm
                 k_cell_keys<3, true><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key,
                                                                            h->f_count, h->d_err);
         } else if (h->cfg.ndims == 2)
-            k_cell_keys<2><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
-                                                                 h->d_err, gate);
+            k_cell_keys<2><<<std::min(nblk(n, 256), 8 * h->num_sms), 256, 0, h->stream>>>(
+                u, n, h->grid, key, h->f_count, h->d_err, gate);
         else
-            k_cell_keys<3><<<nblk(n, 256), 256, 0, h->stream>>>(u, n, h->grid, key, h->f_count,
-                                                                 h->d_err, gate);
+            k_cell_keys<3><<<std::min(nblk(n, 256), 8 * h->num_sms), 256, 0, h->stream>>>(
+                u, n, h->grid, key, h->f_count, h->d_err, gate);
         TP_LAUNCHED(h, "cell keys");
         h->launches += 1;
         TP_DBG(h, "cell keys");
@@ -500,7 +500,8 @@ tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tm
     h->launches += 3;
     TP_DBG(h, "cell scan");
     if (n > 0) {
-        k_scatter<<<nblk(n, 256), 256, 0, h->stream>>>(key, n, h->f_cursor, tmp, gate);
+        k_scatter<<<std::min(nblk(n, 256), 8 * h->num_sms), 256, 0, h->stream>>>(
+            key, n, h->f_cursor, tmp, gate);
         TP_LAUNCHED(h, "cell scatter");
         h->launches += 1;
         TP_DBG(h, "cell scatter");
@@ -588,16 +589,18 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
         // the tiled FP32 pair pass enumerates its candidates itself: no fluid lists
         const bool fluid_lists = h->pair_mode != TP_PAIR_TILED;
         if (nf > 0 && fluid_lists)
-            k_build_fluid_lists<ND><<<nblk(nf, 128), 128, 0, h->stream>>>(
+            k_build_fluid_lists<ND><<<std::min(nblk(nf, 128), 8 * h->num_sms), 128, 0,
+                                      h->stream>>>(
                 h->grid, cs, m, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_skey,
                 h->w_start,
-                h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate);
+                h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate,
+                TileQueue{h->tile_ctr});
         if (nw > 0)
             k_build_wall_lists<ND><<<std::min(nblk(nw, 128), 8 * h->num_sms), 128, 0,
                                      h->stream>>>(
                 h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_skey, h->f_start,
                 h->l_wf,
-                h->c_wf, h->cap_wf, h->d_err, gate);
+                h->c_wf, h->cap_wf, h->d_err, gate, TileQueue{h->tile_ctr + 2});
     };
     if (h->cfg.ndims == 2)
         run(std::integral_constant<int, 2>{});
@@ -857,6 +860,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc(&h->c_fw, nf));
     A(dalloc(&h->c_wf, nw));
     A(dalloc(&h->gate, 5));
+    A(dalloc(&h->tile_ctr, 4));
     A(dalloc(&h->d_max, 1));
     h->red_blocks = 256;
     A(dalloc(&h->red_partial, (size_t)h->red_blocks * 5));
@@ -885,6 +889,7 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     if (e == cudaSuccess) e = cudaMemset(h->f_count, 0, nc * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->gate, 0, 5 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(h->tile_ctr, 0, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(h->w_start, 0, (nc + 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->c_ff, 0, std::max<size_t>(nf, 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->c_fw, 0, std::max<size_t>(nf, 1) * sizeof(int));
@@ -911,7 +916,7 @@ tp_status tp_destroy(tp_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* more[] = {h->l_ff, h->l_fw, h->l_wf, h->c_ff, h->c_fw, h->c_wf, h->x_build, h->gate,
-                    h->grid_org,
+                    h->grid_org, h->tile_ctr,
                     h->d_max, h->e_ff, h->e_fw, h->e_wf, h->ec_ff, h->ec_fw, h->acc, h->spv};
     for (void* p : more)
         if (p) cudaFree(p);

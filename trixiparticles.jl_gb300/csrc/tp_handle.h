@@ -107,6 +107,7 @@ struct tp_handle {
     double* x_build = nullptr;  // fluid positions at the last rebuild (slot order)
     double* grid_org = nullptr;  // per-axis cell origins of the FP32 cell size (GridDesc::org)
     int num_sms = 1;             // multiprocessors of the device (fixed-grid launches)
+    unsigned* tile_ctr = nullptr;  // TileQueue counters of the fluid and wall list builds (2 + 2)
     unsigned* gate = nullptr;   // {force, max squared displacement bits, squared threshold bits,
                                 //  next stage's displacement bits, rebuilds let through}
     int* d_max = nullptr;       // scratch for the largest cell occupancy

@@ -368,7 +368,30 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
     return cnt;
 }
 
-// Fluid slots: fluid-fluid and fluid-wall lists.
+// Tiles of a fixed grid of resident blocks: each block takes the next 128-slot tile from
+// ctr[0] until none is left (a closed gate then costs one short launch, and heavy tiles are
+// spread over the blocks as they come); the last block to finish resets ctr[0..1] to zero for
+// the next launch.
+struct TileQueue {
+    unsigned* ctr;
+    __device__ __forceinline__ int next(int* slot) const {
+        __syncthreads();  // every thread has read the previous tile
+        if (threadIdx.x == 0) *slot = (int)atomicAdd(ctr, 1u);
+        __syncthreads();
+        return *slot;
+    }
+    __device__ __forceinline__ void done() const {
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(ctr + 1, 1u) == gridDim.x - 1) {
+                ctr[0] = 0u;
+                ctr[1] = 0u;
+            }
+        }
+    }
+};
+
+// Fluid slots: fluid-fluid and fluid-wall lists, over the tiles of a TileQueue.
 template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     GridDesc g, float cs, float m, float r2f, int nf, const float4* __restrict__ ftest,
@@ -376,49 +399,55 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     const float4* __restrict__ wtest, const int* __restrict__ wskey,
     const int* __restrict__ wstart, unsigned* __restrict__ ff,
     int* __restrict__ ffc, int cap_ff, unsigned* __restrict__ fw, int* __restrict__ fwc,
-    int cap_fw, int* __restrict__ err, const unsigned* __restrict__ gate) {
+    int cap_fw, int* __restrict__ err, const unsigned* __restrict__ gate, TileQueue q) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
     __shared__ int2 cidx_all[4][32];
     __shared__ unsigned lbuf_all[kListChunk][128];
+    __shared__ int tile_slot;
     float4* cand = cand_all[threadIdx.x >> 5];
     int2* cidx = cidx_all[threadIdx.x >> 5];
     unsigned* lbuf = &lbuf_all[0][threadIdx.x];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = s < nf;
-    const int si = active ? s : 0;
-    const float4 ta = ftest[si];
-    int c[3];
-    key_to_coords(fskey[si], g, c);
-    const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
-                                    cidx, lbuf, ff, nf, cap_ff, s);
-    const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, cand,
-                                    cidx, lbuf, fw, nf, cap_fw, s);
-    if (!active) return;
-    ffc[s] = min(n1, cap_ff);
-    fwc[s] = min(n2, cap_fw);
-    if (n1 > cap_ff || n2 > cap_fw) atomicOr(err, TP_ERRBIT_CAPACITY);
+    const int ntiles = (nf + 127) / 128;
+    for (int tile = q.next(&tile_slot); tile < ntiles; tile = q.next(&tile_slot)) {
+        const int s = tile * 128 + threadIdx.x;
+        const bool active = s < nf;
+        const int si = active ? s : 0;
+        const float4 ta = ftest[si];
+        int c[3];
+        key_to_coords(fskey[si], g, c);
+        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
+                                        cidx, lbuf, ff, nf, cap_ff, s);
+        const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, cand,
+                                        cidx, lbuf, fw, nf, cap_fw, s);
+        if (active) {
+            ffc[s] = min(n1, cap_ff);
+            fwc[s] = min(n2, cap_fw);
+            if (n1 > cap_ff || n2 > cap_fw) atomicOr(err, TP_ERRBIT_CAPACITY);
+        }
+    }
+    q.done();
 }
 
-// Wall slots: wall-fluid lists (the Adami gather).  Most wall slots of a tank have no fluid in
-// reach and finish their search at once, so the launch keeps a fixed grid of resident blocks that
-// walk the 128-slot tiles (tile = blockIdx.x, + gridDim.x, ...) instead of one block per tile.
+// Wall slots: wall-fluid lists (the Adami gather), over the tiles of a TileQueue (most wall
+// slots of a tank have no fluid in reach and finish their search at once).
 template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     GridDesc g, float cs, float m, float r2f, int nw, const float4* __restrict__ wtest,
     const int* __restrict__ wskey, const float4* __restrict__ ftest,
     const int* __restrict__ fskey, const int* __restrict__ fstart, unsigned* __restrict__ wf,
     int* __restrict__ wfc, int cap_wf,
-    int* __restrict__ err, const unsigned* __restrict__ gate) {
+    int* __restrict__ err, const unsigned* __restrict__ gate, TileQueue q) {
     if (!gate_open(gate)) return;
     __shared__ float4 cand_all[4][32];
     __shared__ int2 cidx_all[4][32];
     __shared__ unsigned lbuf_all[kListChunk][128];
+    __shared__ int tile_slot;
     float4* cand = cand_all[threadIdx.x >> 5];
     int2* cidx = cidx_all[threadIdx.x >> 5];
     unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int ntiles = (nw + 127) / 128;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int tile = q.next(&tile_slot); tile < ntiles; tile = q.next(&tile_slot)) {
         const int s = tile * 128 + threadIdx.x;
         const bool active = s < nw;
         const int si = active ? s : 0;
@@ -432,6 +461,7 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
             if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
         }
     }
+    q.done();
 }
 
 // Largest cell occupancy of a freshly counted histogram (list capacity sizing).

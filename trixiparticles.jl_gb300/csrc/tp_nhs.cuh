@@ -47,20 +47,23 @@ __global__ void __launch_bounds__(256) k_cell_keys(const double* __restrict__ u,
     if (!gate_open(gate)) return;
     // gate[4] counts the rebuilds the gate let through (diagnostics, tp_rebuild_count)
     if (gate && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(const_cast<unsigned*>(gate) + 4, 1u);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
-    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    if (!valid) return;
-    double x[3] = {0.0, 0.0, 0.0};
+    // any grid: the blocks stride over the particles (block-uniform trip count)
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
+        double x[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
-    int c[3];
-    const int e = cell_coords<ND>(x, g, c);
-    if (e) atomicOr(err, e);
-    const int k = LEX ? c[2] + g.n[2] * (c[1] + g.n[1] * c[0]) : cell_key(c, g);
-    key[i] = k;
-    const unsigned peers = __match_any_sync(vmask, k);
-    if (lane_id() == __ffs(peers) - 1) atomicAdd(&count[k], __popc(peers));
+        for (int d = 0; d < ND; ++d) x[d] = u[(size_t)i * ND + d];
+        int c[3];
+        const int e = cell_coords<ND>(x, g, c);
+        if (e) atomicOr(err, e);
+        const int k = LEX ? c[2] + g.n[2] * (c[1] + g.n[1] * c[0]) : cell_key(c, g);
+        key[i] = k;
+        const unsigned peers = __match_any_sync(vmask, k);
+        if (lane_id() == __ffs(peers) - 1) atomicAdd(&count[k], __popc(peers));
+    }
 }
 
 // Block-wide exclusive scan of kScanItems values per thread; returns the block total.
@@ -179,17 +182,19 @@ static __global__ void __launch_bounds__(256) k_scatter(const int* __restrict__ 
                                                  int* __restrict__ cursor, int* __restrict__ tmp,
                                                  const unsigned* __restrict__ gate = nullptr) {
     if (!gate_open(gate)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
-    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    if (!valid) return;
-    const int k = key[i];
-    const unsigned peers = __match_any_sync(vmask, k);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (lane_id() == leader) base = atomicAdd(&cursor[k], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    tmp[base + __popc(peers & lanemask_lt())] = i;
+    for (int b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
+        const int k = key[i];
+        const unsigned peers = __match_any_sync(vmask, k);
+        const int leader = __ffs(peers) - 1;
+        int base = 0;
+        if (lane_id() == leader) base = atomicAdd(&cursor[k], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        tmp[base + __popc(peers & lanemask_lt())] = i;
+    }
 }
 
 // Final slot = cell start + rank of the source index among the cell's particles.  The packer
