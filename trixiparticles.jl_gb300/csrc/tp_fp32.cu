@@ -65,13 +65,7 @@ __device__ __forceinline__ void load_rec32(const float4* __restrict__ rec, int s
         : "l"(rec + 2 * (size_t)s));
 }
 
-// ---- two list candidates per instruction: the packed FP32 arithmetic of sm_100+ (one FFMA2,
-// FADD2 or FMUL2 computes both halves of a float2, each rounded as the scalar operation) ----
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+// ---- two list candidates per instruction (the packed FP32 helpers of tp_lists.cuh) ----
 
 // Pair differences o_a - o_b + (c_a - c_b) cs of two list entries (pair_diff_decoded for both
 // halves: the cell offsets decoded from the entry codes as the small integers 2 - f, so that

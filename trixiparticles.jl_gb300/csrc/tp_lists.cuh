@@ -184,6 +184,22 @@ __global__ void __launch_bounds__(256) k_displacement(const double* __restrict__
     if ((threadIdx.x & 31) == 0 && d2 > 0.0f) atomicMax(&gate[1], __float_as_uint(d2));
 }
 
+// The packed FP32 arithmetic of sm_100+: one FFMA2, FADD2 or FMUL2 computes both halves of a
+// float2, each rounded as the scalar operation.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+
+// Staging buffer of one warp of the candidate search: up to 32 compacted records as {slot, x
+// cell} and separate coordinate arrays, so that two consecutive entries load as one int4 / float2
+// (two spare entries keep those loads in bounds).
+struct __align__(16) SearchStage {
+    int2 jc[34];
+    float x[34], y[34], z[34];
+};
+
 // Widest x extent (in cells beyond the first) of a lane group of the candidate search.
 constexpr int kGroupSpan = 2;
 
@@ -206,7 +222,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                                             const int* __restrict__ start,
                                             const int* __restrict__ skey,
                                             const float4* __restrict__ test, float r2f,
-                                            float4* cand, int2* cidx, unsigned* lbuf,
+                                            SearchStage* st, unsigned* lbuf,
                                             unsigned* __restrict__ list, int stride, int cap,
                                             int s) {
     const unsigned FULL = 0xffffffffu;
@@ -288,6 +304,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                 }
                 const float sy = fmaf(-(float)dy, cs, oa.y);
                 const float sz = fmaf(-(float)dz, cs, oa.z);
+                const float2 xl2 = f2(xlane), sy2 = f2(sy), sz2 = f2(sz);
                 const float ryz = fmaf(ey, ey, ez * ez);
                 const unsigned rowcode = 5u * (unsigned)(dy + 2) + 25u * (unsigned)(dz + 2);
                 // the next chunk's records are loaded while the current one is tested
@@ -332,31 +349,36 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                     const unsigned hits = __ballot_sync(FULL, rel);
                     if (rel) {
                         const int pos = __popc(hits & ((1u << lane) - 1u));
-                        cand[pos] = cb;
-                        cidx[pos] = make_int2(j, cxb);
+                        st->jc[pos] = make_int2(j, cxb);
+                        st->x[pos] = cb.x;
+                        st->y[pos] = cb.y;
+                        st->z[pos] = cb.z;
                     }
                     __syncwarp();
+                    // every lane tests the staged records, two per packed instruction (the scalar
+                    // test's arithmetic), and appends its hits in staging order
                     const int nrel = __popc(hits);
-                    for (int i = 0; i < nrel; ++i) {
-                        const float4 cb = cand[i];
-                        const int2 jc = cidx[i];
-                        const int jj = jc.x;
-                        const float pdx = xlane - cb.x;
-                        const float pdy = sy - cb.y;
-                        float d2 = fmaf(pdy, pdy, pdx * pdx);
+                    auto append = [&](int jj, int cxj) {
+                        const unsigned code = rowcode + (unsigned)(cxj - c[0] + 2);
+                        if (cnt < cap) {
+                            lbuf[(cnt & 7) * bs] = (unsigned)jj | (code << kSlotBits);
+                            if ((cnt & 7) == 7) flush(cnt >> 3);
+                        }
+                        ++cnt;
+                    };
+                    for (int i = 0; i < nrel; i += 2) {
+                        const float2 pdx = sub2(xl2, *reinterpret_cast<const float2*>(&st->x[i]));
+                        const float2 pdy = sub2(sy2, *reinterpret_cast<const float2*>(&st->y[i]));
+                        float2 d2 = fma2(pdy, pdy, mul2(pdx, pdx));
                         if (ND == 3) {
-                            const float pdz = sz - cb.z;
-                            d2 = fmaf(pdz, pdz, d2);
+                            const float2 pdz =
+                                sub2(sz2, *reinterpret_cast<const float2*>(&st->z[i]));
+                            d2 = fma2(pdz, pdz, d2);
                         }
-                        if (jj >= mlo && jj < mhi && d2 <= r2f) {
-                            const unsigned code =
-                                rowcode + (unsigned)(jc.y - c[0] + 2);
-                            if (cnt < cap) {
-                                lbuf[(cnt & 7) * bs] = (unsigned)jj | (code << kSlotBits);
-                                if ((cnt & 7) == 7) flush(cnt >> 3);
-                            }
-                            ++cnt;
-                        }
+                        const int4 jj = *reinterpret_cast<const int4*>(&st->jc[i]);
+                        if (jj.x >= mlo && jj.x < mhi && d2.x <= r2f) append(jj.x, jj.y);
+                        if (i + 1 < nrel && jj.z >= mlo && jj.z < mhi && d2.y <= r2f)
+                            append(jj.z, jj.w);
                     }
                     __syncwarp();
                 }
@@ -401,12 +423,10 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     int* __restrict__ ffc, int cap_ff, unsigned* __restrict__ fw, int* __restrict__ fwc,
     int cap_fw, int* __restrict__ err, const unsigned* __restrict__ gate, TileQueue q) {
     if (!gate_open(gate)) return;
-    __shared__ float4 cand_all[4][32];
-    __shared__ int2 cidx_all[4][32];
+    __shared__ SearchStage stage_all[4];
     __shared__ unsigned lbuf_all[kListChunk][128];
     __shared__ int tile_slot;
-    float4* cand = cand_all[threadIdx.x >> 5];
-    int2* cidx = cidx_all[threadIdx.x >> 5];
+    SearchStage* st = &stage_all[threadIdx.x >> 5];
     unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int ntiles = (nf + 127) / 128;
     for (int tile = q.next(&tile_slot); tile < ntiles; tile = q.next(&tile_slot)) {
@@ -416,10 +436,10 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
         const float4 ta = ftest[si];
         int c[3];
         key_to_coords(fskey[si], g, c);
-        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
-                                        cidx, lbuf, ff, nf, cap_ff, s);
-        const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, cand,
-                                        cidx, lbuf, fw, nf, cap_fw, s);
+        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, st,
+                                        lbuf, ff, nf, cap_ff, s);
+        const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, st,
+                                        lbuf, fw, nf, cap_fw, s);
         if (active) {
             ffc[s] = min(n1, cap_ff);
             fwc[s] = min(n2, cap_fw);
@@ -439,12 +459,10 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     int* __restrict__ wfc, int cap_wf,
     int* __restrict__ err, const unsigned* __restrict__ gate, TileQueue q) {
     if (!gate_open(gate)) return;
-    __shared__ float4 cand_all[4][32];
-    __shared__ int2 cidx_all[4][32];
+    __shared__ SearchStage stage_all[4];
     __shared__ unsigned lbuf_all[kListChunk][128];
     __shared__ int tile_slot;
-    float4* cand = cand_all[threadIdx.x >> 5];
-    int2* cidx = cidx_all[threadIdx.x >> 5];
+    SearchStage* st = &stage_all[threadIdx.x >> 5];
     unsigned* lbuf = &lbuf_all[0][threadIdx.x];
     const int ntiles = (nw + 127) / 128;
     for (int tile = q.next(&tile_slot); tile < ntiles; tile = q.next(&tile_slot)) {
@@ -454,8 +472,8 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
         const float4 ta = wtest[si];
         int c[3];
         key_to_coords(wskey[si], g, c);
-        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, cand,
-                                        cidx, lbuf, wf, nw, cap_wf, s);
+        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, st,
+                                        lbuf, wf, nw, cap_wf, s);
         if (active) {
             wfc[s] = min(n1, cap_wf);
             if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
