@@ -11,7 +11,7 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def dam_break_case(pkg, ndims, dx, fluid, tank, layers=3, precision="float64", h_factor=1.75,
-                   jitter=0.0, seed=0, alpha=0.02, delta=0.1):
+                   jitter=0.0, seed=0, alpha=0.02, delta=0.1, beta=0.0):
     """A dam-break Semidiscretization (not yet on the device) plus its tank."""
     tank_, eos = pkg.dam_break(ndims, dx, fluid, tank, n_layers=layers)
     if jitter:
@@ -19,7 +19,7 @@ def dam_break_case(pkg, ndims, dx, fluid, tank, layers=3, precision="float64", h
         tank_.fluid.coordinates += rng.uniform(-jitter * dx, jitter * dx,
                                                tank_.fluid.coordinates.shape)
     semi = pkg.dam_break_semidiscretization(tank_, eos, h_factor * dx, precision=precision,
-                                            alpha=alpha, delta=delta)
+                                            alpha=alpha, delta=delta, beta=beta)
     return semi, tank_
 
 

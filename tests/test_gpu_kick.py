@@ -205,3 +205,32 @@ def test_fp32_modes_switch_back_and_forth(pkg, orc, cuda):
         g = dv.cpu().numpy().reshape(-1, nd + 1)
         assert rel_l2(g[:, :nd], r[:, :nd]) <= 2e-5
     semi.close()
+
+
+@pytest.mark.parametrize("switches", [dict(beta=0.5), dict(delta=None), dict(beta=0.5, delta=None)],
+                         ids=["beta", "no-diffusion", "beta-no-diffusion"])
+def test_kick_fp32_model_switches_match_oracle(pkg, orc, cuda, switches):
+    """The FP32 list pass outside the dam-break configuration (Monaghan beta != 0, no density
+    diffusion: the kernels' general path, in 3D through the packed two-candidate evaluation)
+    against the oracle, with the FP32 form's tolerances."""
+    torch = cuda
+    case = CASES[2]
+    semi, tank = dam_break_case(pkg, case["ndims"], case["dx"], case["fluid"], case["tank"],
+                                jitter=case["jitter"], seed=5, precision="float32", **switches)
+    ode = pkg.semidiscretize(semi, (0.0, 1.0))
+    v, u = _state(tank, case)
+    v_t = torch.as_tensor(v.ravel(), device=semi.device)
+    u_t = torch.as_tensor(u.ravel(), device=semi.device)
+    dv = torch.full_like(v_t, float("nan"))
+    pkg.kick(dv, v_t, u_t, ode.p, 0.0)
+    semi.sync()
+    model = oracle_model(orc, semi, tank)
+    dv_ref, st = model.kick(v, u)
+    assert st == 0
+    nd = case["ndims"]
+    g = dv.cpu().numpy().reshape(-1, nd + 1)
+    r = dv_ref.reshape(-1, nd + 1)
+    assert np.all(np.isfinite(g))
+    assert rel_l2(g[:, :nd], r[:, :nd]) <= 2e-5
+    assert rel_l2(g[:, nd], r[:, nd]) <= 1e-4
+    semi.close()

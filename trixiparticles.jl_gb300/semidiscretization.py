@@ -592,17 +592,18 @@ def solve(ode: ODEProblem, alg: CarpenterKennedy2N54, *, dt: float, n_steps: int
 
 def dam_break_semidiscretization(tank, eos, smoothing_length: float, *, precision="float64",
                                  alpha=0.02, delta=0.1, gravity=9.81, wall_clip=True,
-                                 device: int = 0) -> Semidiscretization:
+                                 beta=0.0, device: int = 0) -> Semidiscretization:
     """The dam-break system pair of examples/fluid/dam_break_2d.jl with a FullGridCellList over
-    the tank's wall particles (examples/fluid/dam_break_2d_gpu.jl:30-33)."""
+    the tank's wall particles (examples/fluid/dam_break_2d_gpu.jl:30-33).  `beta`: the Monaghan
+    beta (0 in the examples); `delta=None`: no density diffusion."""
     nd = tank.fluid.ndims
     kern = WendlandC2Kernel(nd)
     acc = (0.0, -gravity) if nd == 2 else (0.0, -gravity, 0.0)
     fluid = WeaklyCompressibleSPHSystem(
         tank.fluid, smoothing_kernel=kern, smoothing_length=smoothing_length,
         density_calculator=ContinuityDensity(), state_equation=eos, acceleration=acc,
-        viscosity=ArtificialViscosityMonaghan(alpha=alpha, beta=0.0),
-        density_diffusion=DensityDiffusionMolteniColagrossi(delta=delta))
+        viscosity=ArtificialViscosityMonaghan(alpha=alpha, beta=beta),
+        density_diffusion=None if delta is None else DensityDiffusionMolteniColagrossi(delta=delta))
     bm = BoundaryModelDummyParticles(
         tank.boundary.density, tank.boundary.mass, AdamiPressureExtrapolation(), kern,
         smoothing_length, state_equation=eos, clip_negative_pressure=wall_clip)
