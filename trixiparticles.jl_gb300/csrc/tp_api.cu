@@ -492,9 +492,10 @@ tp_status sort_particles(tp_handle* h, const double* u, int n, int* key, int* tm
     }
     const int nc = h->grid.ncells;
     const int nb = nblk(nc, kScanTile);
-    k_scan_reduce<<<nb, kScanThreads, 0, h->stream>>>(h->f_count, nc, h->scan_partial, gate);
+    const int grid = std::min(nb, 2 * h->num_sms);  // 1024-thread blocks walk the tiles
+    k_scan_reduce<<<grid, kScanThreads, 0, h->stream>>>(h->f_count, nc, h->scan_partial, gate);
     k_scan_partials<<<1, kScanThreads, 0, h->stream>>>(h->scan_partial, nb, gate);
-    k_scan_final<<<nb, kScanThreads, 0, h->stream>>>(h->f_count, nc, h->scan_partial, start,
+    k_scan_final<<<grid, kScanThreads, 0, h->stream>>>(h->f_count, nc, h->scan_partial, start,
                                                      h->f_cursor, gate);
     TP_LAUNCHED(h, "cell scan");
     h->launches += 3;

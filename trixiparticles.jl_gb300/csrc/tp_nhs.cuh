@@ -104,27 +104,33 @@ __device__ __forceinline__ int block_exclusive_scan(int (&v)[kScanItems], int* w
     return total;
 }
 
+// Per-tile sums of the histogram.  Any grid: the blocks walk the tiles (tile = blockIdx.x,
+// + gridDim.x, ...), so that a closed gate costs one short launch over a large grid of cells.
 static __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int* __restrict__ count, int n,
                                                              int* __restrict__ partial,
                                                              const unsigned* __restrict__ gate = nullptr) {
     if (!gate_open(gate)) return;
     __shared__ int sm[33];
-    const int base = blockIdx.x * kScanTile;
-    int s = 0;
+    const int nb = (n + kScanTile - 1) / kScanTile;
+    for (int tile = blockIdx.x; tile < nb; tile += gridDim.x) {
+        const int base = tile * kScanTile;
+        int s = 0;
 #pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-        int idx = base + j * kScanThreads + threadIdx.x;
-        if (idx < n) s += count[idx];
-    }
+        for (int j = 0; j < kScanItems; ++j) {
+            int idx = base + j * kScanThreads + threadIdx.x;
+            if (idx < n) s += count[idx];
+        }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        int t = (threadIdx.x < (kScanThreads >> 5)) ? sm[threadIdx.x] : 0;
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int t = (threadIdx.x < (kScanThreads >> 5)) ? sm[threadIdx.x] : 0;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-        if (threadIdx.x == 0) partial[blockIdx.x] = t;
+            for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+            if (threadIdx.x == 0) partial[tile] = t;
+        }
+        __syncthreads();  // sm is reused by the next tile
     }
 }
 
@@ -153,6 +159,7 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_partials(int* __re
 }
 
 // start[c] = exclusive prefix of count; cursor[c] = start[c]; count[c] = 0; start[n] = total.
+// Any grid, as k_scan_reduce.
 static __global__ void __launch_bounds__(kScanThreads) k_scan_final(int* __restrict__ count, int n,
                                                             const int* __restrict__ partial,
                                                             int* __restrict__ start,
@@ -160,22 +167,25 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_final(int* __restr
                                                             const unsigned* __restrict__ gate = nullptr) {
     if (!gate_open(gate)) return;
     __shared__ int ws[33];
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    int v[kScanItems];
+    const int nb = (n + kScanTile - 1) / kScanTile;
+    for (int tile = blockIdx.x; tile < nb; tile += gridDim.x) {
+        const int base = tile * kScanTile + threadIdx.x * kScanItems;
+        int v[kScanItems];
 #pragma unroll
-    for (int j = 0; j < kScanItems; ++j) v[j] = (base + j < n) ? count[base + j] : 0;
-    const int total = block_exclusive_scan(v, ws);
-    const int off = partial[blockIdx.x];
+        for (int j = 0; j < kScanItems; ++j) v[j] = (base + j < n) ? count[base + j] : 0;
+        const int total = block_exclusive_scan(v, ws);
+        const int off = partial[tile];
 #pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-        int idx = base + j;
-        if (idx < n) {
-            start[idx] = v[j] + off;
-            if (cursor) cursor[idx] = v[j] + off;
-            count[idx] = 0;
+        for (int j = 0; j < kScanItems; ++j) {
+            int idx = base + j;
+            if (idx < n) {
+                start[idx] = v[j] + off;
+                if (cursor) cursor[idx] = v[j] + off;
+                count[idx] = 0;
+            }
         }
+        if (tile == nb - 1 && threadIdx.x == 0) start[n] = off + total;
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[n] = off + total;
 }
 
 static __global__ void __launch_bounds__(256) k_scatter(const int* __restrict__ key, int n,
