@@ -239,12 +239,11 @@ __global__ void k_store(const double* __restrict__ u, const void* __restrict__ v
     }
 }
 
-template <bool F32>
-__global__ void k_scatter_pressure(const void* __restrict__ rec, const int* __restrict__ perm,
+__global__ void k_scatter_pressure(const double4_32a* __restrict__ rec, const int* __restrict__ perm,
                                    double* __restrict__ p, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    p[perm[s]] = F32 ? (double)((const float*)rec)[s] : ((const double4_32a*)rec)[s].w;
+    p[perm[s]] = rec[s].w;
 }
 
 template <bool F32>
@@ -1353,11 +1352,10 @@ tp_status tp_fluid_pressure(tp_handle* h, double* p_fluid) {
                     "reordered (sort, interpolation, adjoint); call tp_kick first");
     const int* ids = h->records_order == 2 ? h->st[h->cur].id : h->f_perm;
     if (h->cfg.precision == TP_PRECISION_FP32)
-        k_scatter_pressure<true><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_aux, ids, p_fluid,
-                                                                        nf);
+        fp32_scatter_pressure(h, ids, p_fluid);
     else
-        k_scatter_pressure<false><<<nblk(nf, 256), 256, 0, h->stream>>>(h->f_pos, ids, p_fluid,
-                                                                         nf);
+        k_scatter_pressure<<<nblk(nf, 256), 256, 0, h->stream>>>((const double4_32a*)h->f_pos,
+                                                                 ids, p_fluid, nf);
     TP_LAUNCHED(h, "fluid pressure");
     return TP_OK;
 }

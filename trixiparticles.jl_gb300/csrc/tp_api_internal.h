@@ -31,6 +31,7 @@ void fp32_pair_kick(tp_handle* h, double* dv);
 void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
                      double dt, int first, Pair32Member* desc = nullptr);
 // The batched persistent FP32 pair pass over B's members (same ndims and model switches).
+void fp32_scatter_pressure(tp_handle* h, const int* ids, double* p_fluid);
 bool fp32_batch_pair_std(const Phys32& P);
 tp_status fp32_batch_pair(const Pair32Batch& B, int nd, bool std_cfg, unsigned* counter,
                           cudaStream_t stream);

@@ -168,8 +168,10 @@ struct Pack32 {
         test[s] = t;
         const float irho = __frcp_rn(P.rho0 + w.w);
         const float4 vr = make_float4(w.x, w.y, w.z, mi * irho);
-        vel[s] = vr;
-        pres[s] = eos32(w.w, P, P.fluid_clip);
+        if (vel) {  // the tiled pass's dense arrays (the list pass reads the records)
+            vel[s] = vr;
+            pres[s] = eos32(w.w, P, P.fluid_clip);
+        }
         rec[2 * (size_t)s] = t;
         rec[2 * (size_t)s + 1] = vr;
         if (rebuild && xb_out) {
@@ -510,8 +512,6 @@ constexpr bool kPackedPairs = ND == 3;
 template <int ND, bool INTEGRATE, bool STD>
 __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
                                             const float4* __restrict__ ftest,
-                                            const float4* __restrict__ fvel,
-                                            const float* __restrict__ fpres,
                                             const float4* __restrict__ frec,
                                             const unsigned* __restrict__ ff,
                                             const int* __restrict__ ffc,
@@ -521,9 +521,9 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
                                             const float* __restrict__ wpres,
                                             unsigned* __restrict__ gate, const Update32& U) {
     if (s >= nf) return;
-    const float4 ta = ftest[s];  // {offsets, rho - rho0}
-    const float4 va = fvel[s];   // {v, m / rho}
-    const float p_a = fpres[s];
+    const float4 ta = ftest[s];               // {offsets, rho - rho0}
+    const float4 va = frec[2 * (size_t)s + 1];  // {v, m / rho}
+    const float p_a = eos32(ta.w, P, P.fluid_clip);  // the pack's value
     const float drho_a = ta.w;
     const float rho_a = P.rho0 + drho_a;
     const float ia = __frcp_rn(rho_a);  // the pack's 1 / rho
@@ -614,8 +614,6 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
 template <int ND, bool INTEGRATE, bool STD>
 __global__ void __launch_bounds__(256, kPackedPairs<ND> ? 4 : 5) k_pair32(Phys32 P, int nf,
                                                 const float4* __restrict__ ftest,
-                                                const float4* __restrict__ fvel,
-                                                const float* __restrict__ fpres,
                                                 const float4* __restrict__ frec,
                                                 const unsigned* __restrict__ ff,
                                                 const int* __restrict__ ffc,
@@ -624,8 +622,8 @@ __global__ void __launch_bounds__(256, kPackedPairs<ND> ? 4 : 5) k_pair32(Phys32
                                                 const float4* __restrict__ wtest,
                                                 const float* __restrict__ wpres,
                                                 unsigned* __restrict__ gate, Update32 U) {
-    pair32_slot<ND, INTEGRATE, STD>(P, blockIdx.x * blockDim.x + threadIdx.x, nf, ftest, fvel,
-                                    fpres, frec, ff, ffc, fw, fwc, wtest, wpres,
+    pair32_slot<ND, INTEGRATE, STD>(P, blockIdx.x * blockDim.x + threadIdx.x, nf, ftest, frec,
+                                    ff, ffc, fw, fwc, wtest, wpres,
                                     gate, U);
 }
 
@@ -647,7 +645,7 @@ __global__ void __launch_bounds__(kBatchTile, kPackedPairs<ND> ? 4 : 5) k_batch_
         while (m + 1 < B.n && it >= B.tile0[m + 1]) ++m;
         const Pair32Member& M = B.m[m];
         const int s = (it - B.tile0[m]) * kBatchTile + threadIdx.x;
-        pair32_slot<ND, true, STD>(M.P, s, M.nf, M.ftest, M.fvel, M.fpres, M.frec, M.ff, M.ffc,
+        pair32_slot<ND, true, STD>(M.P, s, M.nf, M.ftest, M.frec, M.ff, M.ffc,
                                    M.fw, M.fwc, M.wtest, M.wpres, M.gate, M.U);
     }
 }
@@ -879,8 +877,9 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         pk.src_perm = (!S32 && gate) ? h->f_perm : nullptr;
         pk.xb_out = h->x_build;
         pk.test = h->f_test;
-        pk.vel = (float4*)h->f_vel;
-        pk.pres = (float*)h->f_aux;
+        const bool dense = h->pair_mode == TP_PAIR_TILED;
+        pk.vel = dense ? (float4*)h->f_vel : nullptr;
+        pk.pres = dense ? (float*)h->f_aux : nullptr;
         pk.rec = (float4*)h->f_rec;
         pk.g = h->grid;
         pk.cs32 = cs32;
@@ -941,9 +940,8 @@ static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
         }
         k_pair32<ND, INTEG, decltype(stdc)::value><<<nblk(nf, h->pair_block), h->pair_block, 0,
                                                      h->stream>>>(
-            P, nf, h->f_test, (const float4*)h->f_vel, (const float*)h->f_aux,
-            (const float4*)h->f_rec, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test, h->w_p32, gate,
-            U);
+            P, nf, h->f_test, (const float4*)h->f_rec, h->l_ff, h->c_ff, h->l_fw, h->c_fw,
+            h->w_test, h->w_p32, gate, U);
     };
     if (std_cfg)
         run(std::true_type{});
@@ -990,8 +988,6 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
         M.P = h->phys32;
         M.nf = (int)h->cfg.n_fluid;
         M.ftest = h->f_test;
-        M.fvel = (const float4*)h->f_vel;
-        M.fpres = (const float*)h->f_aux;
         M.frec = (const float4*)h->f_rec;
         M.ff = h->l_ff;
         M.ffc = h->c_ff;
@@ -1007,6 +1003,20 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
         launch_pair32<2, true>(h, h->gate, U);
     else
         launch_pair32<3, true>(h, h->gate, U);
+}
+
+// p of every fluid slot to caller order (tp_fluid_pressure): the Cole EOS of the record's
+// rho - rho0, the value the pack and the pair pass use.
+__global__ void k_scatter_pressure32(Phys32 P, const float4* __restrict__ test,
+                                     const int* __restrict__ perm, double* __restrict__ p, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) p[perm[s]] = (double)eos32(test[s].w, P, P.fluid_clip);
+}
+
+void fp32_scatter_pressure(tp_handle* h, const int* ids, double* p_fluid) {
+    const int nf = (int)h->cfg.n_fluid;
+    k_scatter_pressure32<<<nblk(nf, 256), 256, 0, h->stream>>>(h->phys32, h->f_test, ids, p_fluid,
+                                                               nf);
 }
 
 bool fp32_batch_pair_std(const Phys32& P) { return P.visc && P.beta == 0.0f && P.diff; }

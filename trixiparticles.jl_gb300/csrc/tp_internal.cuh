@@ -8,7 +8,8 @@
 //                 faux[s] = double4_32a {p S, S, p_off + p - rho g.x, 2 m alpha c h sg_c} with
 //                 S = sg_c m / rho (gather pair mode; the symmetric mode keeps {m, m/rho, 1/rho,
 //                 2 m alpha c h})
-//     FP32 form:  fvel[s] = float4 {vx, vy, vz, m / rho}   faux[s] = float p
+//     FP32 form:  fvel[s] = float4 {vx, vy, vz, m / rho}   faux[s] = float p (written for the
+//                 tiled pair pass; the list pass reads frec[2s..2s+1] = {test, vel})
 //   wall records, sorted once (walls are static), the state rewritten by the Adami pass:
 //     wpos[s] = double4_32a {x, y, z, m}, wtest[s] = float4 {ox, oy, oz, cx} (FP32 form: the
 //     fourth slot is m / rho of the last Adami pass)
@@ -123,8 +124,6 @@ struct Pair32Member {
     Phys32 P;
     int nf;
     const float4* ftest;
-    const float4* fvel;
-    const float* fpres;
     const float4* frec;
     const unsigned* ff;
     const int* ffc;
