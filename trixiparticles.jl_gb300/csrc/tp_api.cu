@@ -584,6 +584,11 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
     const float cs = (float)h->grid.cs;
     // the search reaches two cells towards faces closer than r_list - cs (1e-5 cs rounding margin)
     const float m = (float)(r - h->grid.cs + 1e-5 * h->grid.cs);
+    // the fluid test records {offsets, rho - rho0}: the first half of the FP32 form's 32-byte
+    // records (stride 2), the FP64 form's test array
+    const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
+    const float4* ftest = f32 ? (const float4*)h->f_rec : h->f_test;
+    const int fstride = f32 ? 2 : 1;
     auto run = [&](auto ndc) {
         constexpr int ND = decltype(ndc)::value;
         // the tiled FP32 pair pass enumerates its candidates itself: no fluid lists
@@ -591,14 +596,16 @@ tp_status build_lists(tp_handle* h, double skin, const unsigned* gate) {
         if (nf > 0 && fluid_lists)
             k_build_fluid_lists<ND><<<std::min(nblk(nf, 128), 8 * h->num_sms), 128, 0,
                                       h->stream>>>(
-                h->grid, cs, m, r2f, nf, h->f_test, h->f_skey, h->f_start, h->w_test, h->w_skey,
+                h->grid, cs, m, r2f, nf, ftest, fstride, h->f_skey, h->f_start, h->w_test,
+                h->w_skey,
                 h->w_start,
                 h->l_ff, h->c_ff, h->cap_ff, h->l_fw, h->c_fw, h->cap_fw, h->d_err, gate,
                 TileQueue{h->tile_ctr});
         if (nw > 0)
             k_build_wall_lists<ND><<<std::min(nblk(nw, 128), 8 * h->num_sms), 128, 0,
                                      h->stream>>>(
-                h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, h->f_test, h->f_skey, h->f_start,
+                h->grid, cs, m, r2f, nw, h->w_test, h->w_skey, ftest, fstride, h->f_skey,
+                h->f_start,
                 h->l_wf,
                 h->c_wf, h->cap_wf, h->d_err, gate, TileQueue{h->tile_ctr + 2});
     };

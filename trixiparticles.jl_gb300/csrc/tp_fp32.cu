@@ -165,7 +165,7 @@ struct Pack32 {
         // hold what a neighbour gather needs and nothing else: 36 bytes per pair
         float4 t = test_record_in<ND>(x, g, cs32, key);
         t.w = w.w;
-        test[s] = t;
+        if (test) test[s] = t;  // the tiled pass's dense array (the list pass reads the records)
         const float irho = __frcp_rn(P.rho0 + w.w);
         const float4 vr = make_float4(w.x, w.y, w.z, mi * irho);
         if (vel) {  // the tiled pass's dense arrays (the list pass reads the records)
@@ -208,10 +208,10 @@ __global__ void k_wall_state32_init(const double4_32a* __restrict__ wpos, float4
 // its rho - rho0 by the EOS the pack applies (the same value it writes).
 template <int ND>
 __device__ __forceinline__ void adami_pair2(const Phys32& P, float4 tw, unsigned e0, unsigned e1,
-                                            bool use1, const float4* __restrict__ ftest,
+                                            bool use1, const float4* __restrict__ frec,
                                             float2& ps, float2& vs) {
-    const float4 c0 = ftest[e0 & kSlotMask];
-    const float4 c1 = ftest[e1 & kSlotMask];
+    const float4 c0 = frec[2 * (size_t)(e0 & kSlotMask)];  // {offsets, rho - rho0}
+    const float4 c1 = frec[2 * (size_t)(e1 & kSlotMask)];
     float2 pdx, pdy, pdz;
     const float2 d2 = pair_diff2<ND>(tw, P.cs, e0, e1, c0, c1, pdx, pdy, pdz);
     const float2 r = make_float2(sqrtf(d2.x), sqrtf(d2.y));
@@ -233,7 +233,7 @@ __device__ __forceinline__ void adami_pair2(const Phys32& P, float4 tw, unsigned
 
 // Per wall slot over its fluid list (the Adami gather): the list walked a quad at a time, the
 // candidates two per packed instruction, each quad's partials added into Kahan-compensated sums;
-// a neighbour gather is its 16-byte test record {offsets, rho - rho0}.  Besides the wall state,
+// a neighbour gather is the first half of its 32-byte record: {offsets, rho - rho0}.  Besides the wall state,
 // the pass leaves m / rho of the wall in the fourth slot of its test record and its pressure in
 // a dense array, which is what the fluid pair pass gathers.
 template <int ND>
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __res
                                                  float4* __restrict__ wstate,
                                                  float* __restrict__ wpres,
                                                  double* __restrict__ wvol,
-                                                 const float4* __restrict__ ftest) {
+                                                 const float4* __restrict__ frec) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const float4 tw = wtest[w];
@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(256) k_adami32(Phys32 P, int nw, float4* __res
         const uint4 l = list_quad_stream(wf, k, nw, w);
         const int m = n - k;  // entries of this quad that belong to the list (>= 1)
         float2 ps = f2(0.0f), vs = f2(0.0f);
-        adami_pair2<ND>(P, tw, l.x, m > 1 ? l.y : l.x, m > 1, ftest, ps, vs);
-        if (m > 2) adami_pair2<ND>(P, tw, l.z, m > 3 ? l.w : l.z, m > 3, ftest, ps, vs);
+        adami_pair2<ND>(P, tw, l.x, m > 1 ? l.y : l.x, m > 1, frec, ps, vs);
+        if (m > 2) adami_pair2<ND>(P, tw, l.z, m > 3 ? l.w : l.z, m > 3, frec, ps, vs);
         Ps.add(ps.x + ps.y);
         V.add(vs.x + vs.y);
     }
@@ -511,7 +511,6 @@ constexpr bool kPackedPairs = ND == 3;
 // the batched persistent pass).
 template <int ND, bool INTEGRATE, bool STD>
 __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
-                                            const float4* __restrict__ ftest,
                                             const float4* __restrict__ frec,
                                             const unsigned* __restrict__ ff,
                                             const int* __restrict__ ffc,
@@ -521,7 +520,7 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
                                             const float* __restrict__ wpres,
                                             unsigned* __restrict__ gate, const Update32& U) {
     if (s >= nf) return;
-    const float4 ta = ftest[s];               // {offsets, rho - rho0}
+    const float4 ta = frec[2 * (size_t)s];      // {offsets, rho - rho0}
     const float4 va = frec[2 * (size_t)s + 1];  // {v, m / rho}
     const float p_a = eos32(ta.w, P, P.fluid_clip);  // the pack's value
     const float drho_a = ta.w;
@@ -613,7 +612,6 @@ __device__ __forceinline__ void pair32_slot(const Phys32& P, int s, int nf,
 
 template <int ND, bool INTEGRATE, bool STD>
 __global__ void __launch_bounds__(256, kPackedPairs<ND> ? 4 : 5) k_pair32(Phys32 P, int nf,
-                                                const float4* __restrict__ ftest,
                                                 const float4* __restrict__ frec,
                                                 const unsigned* __restrict__ ff,
                                                 const int* __restrict__ ffc,
@@ -622,8 +620,8 @@ __global__ void __launch_bounds__(256, kPackedPairs<ND> ? 4 : 5) k_pair32(Phys32
                                                 const float4* __restrict__ wtest,
                                                 const float* __restrict__ wpres,
                                                 unsigned* __restrict__ gate, Update32 U) {
-    pair32_slot<ND, INTEGRATE, STD>(P, blockIdx.x * blockDim.x + threadIdx.x, nf, ftest, frec,
-                                    ff, ffc, fw, fwc, wtest, wpres,
+    pair32_slot<ND, INTEGRATE, STD>(P, blockIdx.x * blockDim.x + threadIdx.x, nf, frec, ff,
+                                    ffc, fw, fwc, wtest, wpres,
                                     gate, U);
 }
 
@@ -645,7 +643,7 @@ __global__ void __launch_bounds__(kBatchTile, kPackedPairs<ND> ? 4 : 5) k_batch_
         while (m + 1 < B.n && it >= B.tile0[m + 1]) ++m;
         const Pair32Member& M = B.m[m];
         const int s = (it - B.tile0[m]) * kBatchTile + threadIdx.x;
-        pair32_slot<ND, true, STD>(M.P, s, M.nf, M.ftest, M.frec, M.ff, M.ffc,
+        pair32_slot<ND, true, STD>(M.P, s, M.nf, M.frec, M.ff, M.ffc,
                                    M.fw, M.fwc, M.wtest, M.wpres, M.gate, M.U);
     }
 }
@@ -876,8 +874,8 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         }
         pk.src_perm = (!S32 && gate) ? h->f_perm : nullptr;
         pk.xb_out = h->x_build;
-        pk.test = h->f_test;
         const bool dense = h->pair_mode == TP_PAIR_TILED;
+        pk.test = dense ? h->f_test : nullptr;
         pk.vel = dense ? (float4*)h->f_vel : nullptr;
         pk.pres = dense ? (float*)h->f_aux : nullptr;
         pk.rec = (float4*)h->f_rec;
@@ -913,11 +911,11 @@ void fp32_adami(tp_handle* h) {
     if (h->cfg.ndims == 2)
         k_adami32<2><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_p32, h->w_vol,
-            h->f_test);
+            (const float4*)h->f_rec);
     else
         k_adami32<3><<<nblk(nw, h->pair_block), h->pair_block, 0, h->stream>>>(
             h->phys32, nw, h->w_test, h->l_wf, h->c_wf, (float4*)h->w_state, h->w_p32, h->w_vol,
-            h->f_test);
+            (const float4*)h->f_rec);
 }
 
 template <int ND, bool INTEG>
@@ -940,8 +938,8 @@ static void launch_pair32(tp_handle* h, unsigned* gate, const Update32& U) {
         }
         k_pair32<ND, INTEG, decltype(stdc)::value><<<nblk(nf, h->pair_block), h->pair_block, 0,
                                                      h->stream>>>(
-            P, nf, h->f_test, (const float4*)h->f_rec, h->l_ff, h->c_ff, h->l_fw, h->c_fw,
-            h->w_test, h->w_p32, gate, U);
+            P, nf, (const float4*)h->f_rec, h->l_ff, h->c_ff, h->l_fw, h->c_fw, h->w_test,
+            h->w_p32, gate, U);
     };
     if (std_cfg)
         run(std::true_type{});
@@ -987,7 +985,6 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
         Pair32Member& M = *desc;
         M.P = h->phys32;
         M.nf = (int)h->cfg.n_fluid;
-        M.ftest = h->f_test;
         M.frec = (const float4*)h->f_rec;
         M.ff = h->l_ff;
         M.ffc = h->c_ff;
@@ -1007,16 +1004,16 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
 
 // p of every fluid slot to caller order (tp_fluid_pressure): the Cole EOS of the record's
 // rho - rho0, the value the pack and the pair pass use.
-__global__ void k_scatter_pressure32(Phys32 P, const float4* __restrict__ test,
+__global__ void k_scatter_pressure32(Phys32 P, const float4* __restrict__ rec,
                                      const int* __restrict__ perm, double* __restrict__ p, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < n) p[perm[s]] = (double)eos32(test[s].w, P, P.fluid_clip);
+    if (s < n) p[perm[s]] = (double)eos32(rec[2 * (size_t)s].w, P, P.fluid_clip);
 }
 
 void fp32_scatter_pressure(tp_handle* h, const int* ids, double* p_fluid) {
     const int nf = (int)h->cfg.n_fluid;
-    k_scatter_pressure32<<<nblk(nf, 256), 256, 0, h->stream>>>(h->phys32, h->f_test, ids, p_fluid,
-                                                               nf);
+    k_scatter_pressure32<<<nblk(nf, 256), 256, 0, h->stream>>>(
+        h->phys32, (const float4*)h->f_rec, ids, p_fluid, nf);
 }
 
 bool fp32_batch_pair_std(const Phys32& P) { return P.visc && P.beta == 0.0f && P.diff; }

@@ -123,7 +123,6 @@ struct Update32 {
 struct Pair32Member {
     Phys32 P;
     int nf;
-    const float4* ftest;
     const float4* frec;
     const unsigned* ff;
     const int* ffc;

@@ -221,7 +221,8 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                                             const int c[3], float4 oa,
                                             const int* __restrict__ start,
                                             const int* __restrict__ skey,
-                                            const float4* __restrict__ test, float r2f,
+                                            const float4* __restrict__ test, int tstride,
+                                            float r2f,
                                             SearchStage* st, unsigned* lbuf,
                                             unsigned* __restrict__ list, int stride, int cap,
                                             int s) {
@@ -311,7 +312,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                 float4 nxt = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 int nkey = 0;
                 if (lo + lane < hi) {
-                    nxt = test[lo + lane];
+                    nxt = test[(size_t)(lo + lane) * tstride];
                     nkey = skey[lo + lane];
                 }
                 for (int base = lo; base < hi; base += 32) {
@@ -321,7 +322,7 @@ __device__ __forceinline__ int warp_collect(const GridDesc& g, float cs, float m
                     const int key = nkey;
                     int cxb = 0;
                     if (j + 32 < hi) {
-                        nxt = test[j + 32];
+                        nxt = test[(size_t)(j + 32) * tstride];
                         nkey = skey[j + 32];
                     }
                     if (j < hi) {
@@ -417,7 +418,7 @@ struct TileQueue {
 template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
     GridDesc g, float cs, float m, float r2f, int nf, const float4* __restrict__ ftest,
-    const int* __restrict__ fskey, const int* __restrict__ fstart,
+    int fstride, const int* __restrict__ fskey, const int* __restrict__ fstart,
     const float4* __restrict__ wtest, const int* __restrict__ wskey,
     const int* __restrict__ wstart, unsigned* __restrict__ ff,
     int* __restrict__ ffc, int cap_ff, unsigned* __restrict__ fw, int* __restrict__ fwc,
@@ -433,13 +434,13 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
         const int s = tile * 128 + threadIdx.x;
         const bool active = s < nf;
         const int si = active ? s : 0;
-        const float4 ta = ftest[si];
+        const float4 ta = ftest[(size_t)si * fstride];
         int c[3];
         key_to_coords(fskey[si], g, c);
-        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, st,
-                                        lbuf, ff, nf, cap_ff, s);
-        const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, r2f, st,
-                                        lbuf, fw, nf, cap_fw, s);
+        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, fstride,
+                                        r2f, st, lbuf, ff, nf, cap_ff, s);
+        const int n2 = warp_collect<ND>(g, cs, m, active, c, ta, wstart, wskey, wtest, 1, r2f,
+                                        st, lbuf, fw, nf, cap_fw, s);
         if (active) {
             ffc[s] = min(n1, cap_ff);
             fwc[s] = min(n2, cap_fw);
@@ -454,7 +455,7 @@ __global__ void __launch_bounds__(128, 8) k_build_fluid_lists(
 template <int ND>
 __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
     GridDesc g, float cs, float m, float r2f, int nw, const float4* __restrict__ wtest,
-    const int* __restrict__ wskey, const float4* __restrict__ ftest,
+    const int* __restrict__ wskey, const float4* __restrict__ ftest, int fstride,
     const int* __restrict__ fskey, const int* __restrict__ fstart, unsigned* __restrict__ wf,
     int* __restrict__ wfc, int cap_wf,
     int* __restrict__ err, const unsigned* __restrict__ gate, TileQueue q) {
@@ -472,8 +473,8 @@ __global__ void __launch_bounds__(128, 8) k_build_wall_lists(
         const float4 ta = wtest[si];
         int c[3];
         key_to_coords(wskey[si], g, c);
-        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, r2f, st,
-                                        lbuf, wf, nw, cap_wf, s);
+        const int n1 = warp_collect<ND>(g, cs, m, active, c, ta, fstart, fskey, ftest, fstride,
+                                        r2f, st, lbuf, wf, nw, cap_wf, s);
         if (active) {
             wfc[s] = min(n1, cap_wf);
             if (n1 > cap_wf) atomicOr(err, TP_ERRBIT_CAPACITY);
