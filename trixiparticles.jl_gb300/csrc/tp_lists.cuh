@@ -64,13 +64,6 @@ __device__ __forceinline__ unsigned list_next_rw(const unsigned* list, int k, in
     return r == 0 ? q.x : r == 1 ? q.y : r == 2 ? q.z : q.w;
 }
 
-// Entry k of slot s from the quad q that holds it, loading the next quad when k reaches it.
-__device__ __forceinline__ unsigned list_next(const unsigned* __restrict__ list, int k,
-                                              int stride, int s, uint4& q) {
-    if ((k & 3) == 0) q = list_quad(list, k, stride, s);
-    const int r = k & 3;
-    return r == 0 ? q.x : r == 1 ? q.y : r == 2 ? q.z : q.w;
-}
 constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;
 
 // Cell offsets of the 125 entry codes times the FP32 cell size, {dx cs, dy cs, dz cs, 0} at
