@@ -6,7 +6,7 @@ the same C types, every `ccall` names an exported function with the header's arg
 dispatch selects `Semidiscretization{<:GB300Backend}` through the reference's first type
 parameter (src/general/semidiscretization.jl:78), the search is looked up through the
 reference's handler accessor (src/general/neighborhood_search.jl:397-416), and the Julia block
-of INTEGRATION.md makes the same calls.
+of the repository's integration guide makes the same calls.
 """
 import re
 from pathlib import Path
@@ -149,7 +149,7 @@ def julia_config_fields(text):
 def _integration_julia_block():
     text = INTEGRATION.read_text()
     blocks = re.findall(r"```julia\n(.*?)```", text, re.S)
-    assert blocks, "INTEGRATION.md has no Julia block"
+    assert blocks, "the integration guide has no Julia block"
     return "\n".join(blocks)
 
 
