@@ -851,7 +851,10 @@ tp_status tp_create(const tp_config* cfg, tp_handle** out) {
     A(dalloc((double4_32a**)&h->f_pos, nf));
     A(dalloc((double4_32a**)&h->f_vel, nf));
     A(dalloc((double4_32a**)&h->f_aux, nf));
-    if (cfg->precision == TP_PRECISION_FP32) A(dalloc((double4_32a**)&h->f_rec, nf));
+    if (cfg->precision == TP_PRECISION_FP32) {
+        A(dalloc((double4_32a**)&h->f_rec, nf));
+        A(dalloc((double4_32a**)&h->f_rec2, nf));
+    }
     A(dalloc(&h->m_f, nf));
     A(dalloc(&h->w_key, nw));
     A(dalloc(&h->w_tmp, nw));
@@ -917,7 +920,8 @@ tp_status tp_destroy(tp_handle* h) {
     adjoint_release(h);
     void* ptrs[] = {h->f_key,   h->f_tmp,   h->f_perm,  h->f_skey,        h->f_count,
                     h->f_start, h->f_cursor, h->scan_partial, h->f_test, h->f_pos,
-                    h->f_vel,   h->f_aux,   h->f_rec,   h->m_f,     h->w_key,   h->w_tmp,
+                    h->f_vel,   h->f_aux,   h->f_rec,   h->f_rec2,  h->m_f,     h->w_key,
+                    h->w_tmp,
                     h->w_perm,  h->w_skey,  h->w_start, h->w_pos,         h->w_test,
                     h->w_state, h->w_p32,   h->w_vol,   h->red_partial, h->d_err};
     for (void* p : ptrs)
@@ -1208,6 +1212,8 @@ tp_status integrator_begin(tp_handle* h, double* v_ode, double* u_ode, int64_t n
     h->launches += 1;
 
     *capturing = cap != cudaStreamCaptureStatusNone;
+    h->rec_prev_fused = false;  // the first stage packs the loaded state
+    h->rec_fuse_pending = false;
     return TP_OK;
 }
 
@@ -1239,7 +1245,7 @@ tp_status integrator_stage_pre(tp_handle* h, int64_t step, int stage) {
     st = sort_particles(h, src.u, nf, h->f_key, h->f_tmp, h->f_start, h->gate);
     if (st != TP_OK) return st;
     if (f32)
-        fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst, h->gate);
+        fp32_pack(h, nullptr, nullptr, nullptr, &src, &dst, h->gate, h->rec_prev_fused);
     else
         fp64_pack(h, src.u, (const double*)src.v, (const double*)src.m, &src, &dst,
                   h->gate);
@@ -1260,18 +1266,23 @@ tp_status integrator_stage_pre(tp_handle* h, int64_t step, int stage) {
 }
 
 // The stage's pair pass with the fused CK2N54 update; with `desc` (FP32 form) the pass is not
-// launched and desc receives it for the batched persistent pass.
-tp_status integrator_stage_pair(tp_handle* h, int stage, double dt, Pair32Member* desc) {
+// launched and desc receives it for the batched persistent pass.  In the FP32 list form every
+// stage but the call's last also writes the next stage's records (the next pack then runs only
+// for a rebuild).
+tp_status integrator_stage_pair(tp_handle* h, int stage, double dt, Pair32Member* desc,
+                                bool last_stage) {
     const bool f32 = h->cfg.precision == TP_PRECISION_FP32;
     PhysState& src = h->st[h->cur];
     PhysState& dst = h->st[1 - h->cur];
+    const bool fuse = f32 && h->pair_mode != TP_PAIR_TILED && !last_stage;
+    h->rec_fuse_pending = fuse;
     if (desc) {
         if (!f32) return fail(h, TP_ERR_UNSUPPORTED, "the persistent pair pass is FP32 only");
-        fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0, desc);
+        fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0, desc, fuse);
         return TP_OK;
     }
     if (f32)
-        fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0);
+        fp32_pair_stage(h, src, dst, kA[stage], kB[stage], dt, stage == 0, nullptr, fuse);
     else
         fp64_pair_stage(h, dst, kA[stage], kB[stage], dt, stage == 0);
     return TP_OK;
@@ -1284,6 +1295,9 @@ tp_status integrator_stage_post(tp_handle* h) {
     mark(h, 3);
     h->launches += 1 + (h->cfg.n_wall > 0);
     h->cur = 1 - h->cur;
+    if (h->rec_fuse_pending) std::swap(h->f_rec, h->f_rec2);  // the records just written
+    h->rec_prev_fused = h->rec_fuse_pending;
+    h->rec_fuse_pending = false;
     return TP_OK;
 }
 
@@ -1315,6 +1329,7 @@ tp_status integrator_end(tp_handle* h, double* v_ode, double* u_ode, bool captur
     h->launches += 1;
     // a captured call has not run yet: the next eager call starts cold
     h->lists_owner = cap == cudaStreamCaptureStatusNone ? 2 : 0;
+    h->rec_prev_fused = false;
     h->records_order = 2;  // records of the last stage, in the order of the final state
     finish_timing(h);
     return TP_OK;
@@ -1340,7 +1355,9 @@ tp_status tp_integrate_ck2n54(tp_handle* h, double* v_ode, double* u_ode, double
     for (int64_t step = 0; step < n_steps; ++step) {
         for (int stage = 0; stage < 5; ++stage) {
             st = integrator_stage_pre(h, step, stage);
-            if (st == TP_OK) st = integrator_stage_pair(h, stage, dt, nullptr);
+            if (st == TP_OK)
+                st = integrator_stage_pair(h, stage, dt, nullptr,
+                                           step == n_steps - 1 && stage == 4);
             if (st == TP_OK) st = integrator_stage_post(h);
             if (st != TP_OK) return st;
         }

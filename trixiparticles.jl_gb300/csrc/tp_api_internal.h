@@ -22,14 +22,15 @@ void pair_distance_check(tp_handle* h, const double* d2, double* r, long long n)
 
 // FP32 precision form (tp_fp32.cu)
 void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
-               const PhysState* src, PhysState* dst, const unsigned* gate);
+               const PhysState* src, PhysState* dst, const unsigned* gate,
+               bool skip_in_place = false);
 void fp32_init_wall_state(tp_handle* h);
 void fp32_adami(tp_handle* h);
 void fp32_pair_kick(tp_handle* h, double* dv);
 // src: the stage's source state (read in place when the stage did not rebuild); st: destination.
 // With `desc` the pass is not launched: desc receives what the batched persistent pass needs.
 void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
-                     double dt, int first, Pair32Member* desc = nullptr);
+                     double dt, int first, Pair32Member* desc = nullptr, bool fuse_next = false);
 // The batched persistent FP32 pair pass over B's members (same ndims and model switches).
 void fp32_scatter_pressure(tp_handle* h, const int* ids, double* p_fluid);
 bool fp32_batch_pair_std(const Phys32& P);
@@ -42,7 +43,8 @@ tp_status fp32_batch_pair(const Pair32Batch& B, int nd, bool std_cfg, unsigned* 
 tp_status integrator_begin(tp_handle* h, double* v_ode, double* u_ode, int64_t n_steps,
                            bool* capturing);
 tp_status integrator_stage_pre(tp_handle* h, int64_t step, int stage);
-tp_status integrator_stage_pair(tp_handle* h, int stage, double dt, Pair32Member* desc);
+tp_status integrator_stage_pair(tp_handle* h, int stage, double dt, Pair32Member* desc,
+                                bool last_stage);
 tp_status integrator_stage_post(tp_handle* h);
 tp_status integrator_end(tp_handle* h, double* v_ode, double* u_ode, bool capturing);
 

@@ -116,7 +116,8 @@ tp_status record_persistent(tp_batch* b, int64_t steps) {
             int tiles = 0;
             for (size_t r = 0; r < n; ++r) {
                 const size_t k = order[r];
-                tp_status st = integrator_stage_pair(b->m[k].h, stage, b->m[k].dt, &B.m[r]);
+                tp_status st = integrator_stage_pair(b->m[k].h, stage, b->m[k].dt, &B.m[r],
+                                                     step == steps - 1 && stage == 4);
                 if (st != TP_OK) return member_fail(b, k, st);
                 B.tile0[r] = tiles;
                 tiles += (B.m[r].nf + kBatchTile - 1) / kBatchTile;

@@ -140,10 +140,14 @@ struct Pack32 {
     float* pres;   // p
     float4* rec;   // {test, vel} in one 32-byte record (the list pair pass)
     const int* src_perm;  // kick! path: without a rebuild, slot s packs caller particle perm[s]
+    // integrator stages after the first: without a rebuild the previous pair stage has written
+    // the records already (Update32::rec_next), so the pass packs nothing
+    bool skip_in_place;
     GridDesc g;
     double cs32, rho0;
     Phys32 P;
     __device__ void operator()(int i, int s, int key, bool rebuild) const {
+        if (!rebuild && skip_in_place) return;
         if (!rebuild && src_perm) i = src_perm[s];
         double x[3] = {0, 0, 0};
 #pragma unroll
@@ -320,6 +324,19 @@ __device__ __forceinline__ void pair32_finish(const Update32& U, int s, float4 v
         }
         if (U.gate_next)
             gate_max_displacement(U.gate_next, displacement2<ND>(un, U.xb + (size_t)s * ND));
+        if (U.rec_next) {
+            // the next stage's records of the new state (what its pack would write without a
+            // rebuild: offsets in the slot's reference cell, rho - rho0, v, m / rho), and the id /
+            // mass copy that pack would make
+            const float mi = U.m_in[s];
+            float4 t = test_record_in<ND>(un, U.grid, U.cs32, U.skey[s]);
+            t.w = vout[3];
+            U.rec_next[2 * (size_t)s] = t;
+            U.rec_next[2 * (size_t)s + 1] =
+                make_float4(vout[0], vout[1], vout[2], mi * __frcp_rn(U.rho0 + vout[3]));
+            U.id_out[s] = U.id_in[s];
+            U.m_out[s] = mi;
+        }
     }
 }
 
@@ -851,7 +868,7 @@ inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 }
 
 void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
-               const PhysState* src, PhysState* dst, const unsigned* gate) {
+               const PhysState* src, PhysState* dst, const unsigned* gate, bool skip_in_place) {
     const int n = (int)h->cfg.n_fluid;
     if (n == 0) return;
     const double cs32 = (double)(float)h->grid.cs;
@@ -879,6 +896,7 @@ void fp32_pack(tp_handle* h, const double* u, const double* v, const double* m,
         pk.vel = dense ? (float4*)h->f_vel : nullptr;
         pk.pres = dense ? (float*)h->f_aux : nullptr;
         pk.rec = (float4*)h->f_rec;
+        pk.skip_in_place = skip_in_place;
         pk.g = h->grid;
         pk.cs32 = cs32;
         pk.rho0 = h->cfg.reference_density;
@@ -960,7 +978,7 @@ void fp32_pair_kick(tp_handle* h, double* dv) {
 }
 
 void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A, double B,
-                     double dt, int first, Pair32Member* desc) {
+                     double dt, int first, Pair32Member* desc, bool fuse_next) {
     if (h->cfg.n_fluid == 0 && !desc) return;
     Update32 U{};
     U.perm = h->f_perm;
@@ -981,6 +999,17 @@ void fp32_pair_stage(tp_handle* h, const PhysState& src, PhysState& st, double A
     U.Bf = (float)B;
     U.dtf = (float)dt;
     U.first = first;
+    if (fuse_next) {  // the next stage's records into the other buffer (swapped after the stage)
+        U.rec_next = (float4*)h->f_rec2;
+        U.skey = h->f_skey;
+        U.grid = h->grid;
+        U.cs32 = (double)(float)h->grid.cs;
+        U.rho0 = h->phys32.rho0;
+        U.id_in = st.id;          // the next stage's source: this stage's destination
+        U.id_out = src.id;        // the next stage's destination
+        U.m_in = (const float*)st.m;
+        U.m_out = (float*)src.m;
+    }
     if (desc) {  // the batched persistent pass launches it (fp32_batch_pair)
         Pair32Member& M = *desc;
         M.P = h->phys32;

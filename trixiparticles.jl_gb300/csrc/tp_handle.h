@@ -64,6 +64,11 @@ struct tp_handle {
     // FP32 pair record, 32 bytes per slot (one 256-bit load per neighbour):
     // {ox, oy, oz, rho - rho0, vx, vy, vz, m / rho}
     void* f_rec = nullptr;
+    // the other record buffer of the FP32 integrator: a pair stage writes the next stage's records
+    // there (the in-place pack of a stage without a rebuild is then skipped) and the two swap
+    void* f_rec2 = nullptr;
+    bool rec_prev_fused = false;    // the previous pair stage wrote this stage's records
+    bool rec_fuse_pending = false;  // this stage's pair pass writes the next stage's records
 
     // ---- fluid masses in caller order (FP64) ----
     double* m_f = nullptr;

@@ -117,6 +117,18 @@ struct Update32 {
     double A, B, dt;
     float Af, Bf, dtf;
     int first;
+    // optional: the next stage's 32-byte records of the new state (rec_next[2s], [2s + 1]) as the
+    // next stage's pack would write them without a rebuild, with the slot's reference cell skey[s],
+    // and the id / mass copy into the destination state
+    float4* rec_next;
+    const int* skey;
+    GridDesc grid;
+    double cs32;
+    float rho0;
+    const int* id_in;
+    int* id_out;
+    const float* m_in;
+    float* m_out;
 };
 
 // One member of the batched persistent FP32 pair pass: everything its list pass reads.
